@@ -1,0 +1,192 @@
+/*
+ * tad_dftd4_gb300.h -- C ABI of the GB300 DFT-D4 dispersion library.
+ *
+ * The library evaluates the DFT-D4 dispersion energy (atom-resolved) and its
+ * gradient for a zero-padded batch of structures, on one CUDA device.  It is
+ * the compiled replacement for tad-dftd4's ``dftd4()`` path
+ * (``src/tad_dftd4/disp.py:44-146``): coordination number, EEQ charges,
+ * Gaussian reference weights with charge scaling, C6 by Casimir-Polder
+ * integration, the rational (BJ) two-body term and the ATM three-body term.
+ *
+ * Conventions (the same as the reference):
+ *  - ``numbers`` holds atomic numbers, 0 marks a padding slot;
+ *  - positions are in Bohr, energies in Hartree, gradients in Eh/Bohr;
+ *  - arrays are C-contiguous, batch-major: numbers[b * n_pad + i].
+ *
+ * Memory: nothing is allocated by the library.  Every device buffer
+ * (element tables, workspace, outputs) is owned by the caller; the workspace
+ * size comes from ``d4_workspace_size``.  All pointers named ``d_*`` or
+ * documented as "device" are device pointers.  ``stream`` is a
+ * ``cudaStream_t`` passed as ``void*``; work is enqueued on it and every
+ * call returns without synchronising.  Calls on different streams with
+ * different workspaces are independent.
+ *
+ * Errors: every entry point returns a ``d4_status`` code.  Input problems
+ * that can only be seen on the device (atomic number outside the tables,
+ * a non-positive EEQ pivot, non-finite input) are reported through the
+ * ``status`` word of the workspace; read it with ``d4_read_status`` after
+ * the stream has been synchronised.
+ */
+#ifndef TAD_DFTD4_GB300_H
+#define TAD_DFTD4_GB300_H
+
+#include <stddef.h>
+#include <stdint.h>
+
+#ifdef __cplusplus
+extern "C" {
+#endif
+
+#define D4_ABI_VERSION 1
+#define D4_NREF 7   /* reference systems per element (reference/d4/params.py) */
+#define D4_NFREQ 23 /* imaginary frequencies of the Casimir-Polder grid (utils.py:52-80) */
+
+typedef enum d4_status {
+  D4_OK = 0,
+  D4_ERR_ARGUMENT = 1,         /* null pointer, bad size or flag */
+  D4_ERR_WORKSPACE = 2,        /* workspace smaller than d4_workspace_size() */
+  D4_ERR_CUDA = 3,             /* a CUDA launch failed; see d4_last_cuda_error() */
+  D4_ERR_ELEMENT = 4,          /* atomic number outside the element tables */
+  D4_ERR_EEQ_SINGULAR = 5,     /* EEQ matrix not positive definite */
+  D4_ERR_NONFINITE = 6,        /* non-finite position or charge */
+  D4_ERR_TOO_MANY_ELEMENTS = 7 /* D4S: more distinct elements than slots */
+} d4_status;
+
+/* Model variants (tad_dftd4.model): D4Model and D4SModel. */
+typedef enum d4_model_kind { D4_MODEL_D4 = 0, D4_MODEL_D4S = 1 } d4_model_kind;
+
+/* Flags for d4_dispersion. */
+#define D4_FLAG_GRADIENT 1u    /* also compute dE/dR (d_gradient must be set) */
+#define D4_FLAG_CHARGES_IN 2u  /* use batch->d_charges_in instead of the EEQ solve */
+#define D4_FLAG_MIXED 4u       /* precision form: FP32 pair/triple maths, FP64 sums */
+#define D4_FLAG_PARAM_GRAD 8u  /* also compute dE/d(s6, s8, s10, a1, a2, s9, alp) */
+
+/*
+ * Element tables, device pointers.  Row 0 is the dummy element.  The first
+ * group has ``n_ref_elem`` rows (104 in tad-dftd4), the second ``n_elem``
+ * rows (119).  ``alpha`` is produced by d4_prepare_alpha().
+ */
+typedef struct d4_tables {
+  int32_t n_ref_elem;
+  int32_t n_elem;
+  const double *alpha;        /* [n_ref_elem][7][23] reference polarisabilities */
+  const double *refcovcn;     /* [n_ref_elem][7] reference coordination numbers */
+  const int64_t *refc;        /* [n_ref_elem][7] Gaussians per reference (0, 1, 3) */
+  const double *refq;         /* [n_ref_elem][7] reference charges for the weights */
+  const double *gam;          /* [n_elem] chemical hardness (before the gc factor) */
+  const int64_t *zeff;        /* [n_elem] effective nuclear charge */
+  const double *r4r2;         /* [n_elem] sqrt(0.5 * <r4>/<r2> * sqrt(Z)) */
+  const double *cov_d3;       /* [n_elem] D3 covalent radii (Bohr) */
+  const double *en;           /* [n_elem] Pauling electronegativities */
+  const double *eeq_chi;      /* [n_elem] EEQ electronegativity */
+  const double *eeq_eta;      /* [n_elem] EEQ chemical hardness */
+  const double *eeq_kcn;      /* [n_elem] EEQ CN scaling */
+  const double *eeq_rad;      /* [n_elem] EEQ charge width (Bohr) */
+  const double *wfpair;       /* [n_elem][n_elem] D4S weighting factors */
+  const double *freq_weights; /* [23] Casimir-Polder quadrature weights */
+} d4_tables_t;
+
+/* Charge-scaling and weighting constants of a model (model/base.py:57-59). */
+typedef struct d4_model_cfg {
+  int32_t kind; /* d4_model_kind */
+  double ga;    /* 3.0 */
+  double gc;    /* 2.0 */
+  double wf;    /* 6.0 (D4; D4S takes wfpair) */
+} d4_model_cfg_t;
+
+/* Damping parameters and cutoffs (damping/parameters/base.py:48-85, cutoff.py). */
+typedef struct d4_params {
+  double s6, s8, s10, a1, a2, s9, alp;
+  int32_t has_s8;  /* 0: no dipole-quadrupole term (reference gating, functions.py:144) */
+  int32_t has_s10; /* 1: add the s10 term (twobody.py:184-197) */
+  double cut_disp2;  /* two-body cutoff, inclusive (60) */
+  double cut_disp3;  /* three-body cutoff on r_ij and r_jk (40) */
+  double cut_cn;     /* D4 CN cutoff (30) */
+  double cut_cn_eeq; /* EEQ CN cutoff (25) */
+  double cn_eeq_max; /* smooth EEQ CN cap (8) */
+  double kcn, k4, k5, k6; /* CN counting constants (defaults.py:41-50) */
+} d4_params_t;
+
+/* A zero-padded batch (device pointers). */
+typedef struct d4_batch {
+  int32_t n_struct; /* B */
+  int32_t n_pad;    /* N, padded atoms per structure */
+  const int64_t *d_numbers;  /* [B][N] */
+  const double *d_positions; /* [B][N][3] */
+  const double *d_charge;    /* [B] total charges */
+  const double *d_charges_in; /* [B][N] atomic charges, read with D4_FLAG_CHARGES_IN */
+  const double *d_r4r2_in;    /* [B][N] per-atom r4r2 values, or NULL for the table */
+  const double *d_energy_weights; /* [B][N] weights w of the differentiated quantity
+                                     sum_i w_i E_i, or NULL for all ones */
+} d4_batch_t;
+
+/* Outputs (device pointers; optional ones may be NULL). */
+typedef struct d4_outputs {
+  double *d_energy;   /* [B][N] atom-resolved energy (required) */
+  double *d_gradient; /* [B][N][3] dE/dR, written with D4_FLAG_GRADIENT */
+  double *d_charges;  /* [B][N] EEQ charges (optional) */
+  double *d_cn;       /* [B][N] D4 coordination numbers (optional) */
+  double *d_param_grad; /* [B][8] dE_b/d(s6,s8,s10,a1,a2,s9,alp,-), D4_FLAG_PARAM_GRAD */
+} d4_outputs_t;
+
+/* Library ABI version (D4_ABI_VERSION). */
+int d4_abi_version(void);
+
+/* Human-readable text for a status code (static storage). */
+const char *d4_status_string(int status);
+
+/* Text of the last CUDA error seen by this thread ("" if none). */
+const char *d4_last_cuda_error(void);
+
+/*
+ * Reference polarisabilities alpha_{e,r}(i w) for every element, written to
+ * ``d_alpha_out`` [n_ref_elem][7][23].  Follows model/base.py:367-418: the
+ * secondary-system polarisability scaled by the charge-scaling function of
+ * its reference charge ``d_refh`` is subtracted from the free reference
+ * value, clipped at zero.  Replaces the per-call ``_get_alpha`` of
+ * BaseModel (called from model/base.py:151 and model/d4.py:306).
+ */
+int d4_prepare_alpha(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                     const double *d_refalpha,  /* [n_ref_elem][7][23] */
+                     const double *d_refascale, /* [n_ref_elem][7] */
+                     const double *d_refscount, /* [n_ref_elem][7] */
+                     const int64_t *d_refsys,   /* [n_ref_elem][7] */
+                     const double *d_secscale,  /* [n_sec] */
+                     const double *d_secalpha,  /* [n_sec][23] */
+                     int32_t n_sec,
+                     const double *d_refh,      /* [n_ref_elem][7] */
+                     double *d_alpha_out, void *stream);
+
+/*
+ * Bytes of workspace needed by d4_dispersion for B structures of N padded
+ * atoms.  ``n_slots`` is 1 for D4 and the largest number of distinct
+ * elements in one structure for D4S.
+ */
+size_t d4_workspace_size(int32_t n_struct, int32_t n_pad, int32_t n_slots, uint32_t flags);
+
+/*
+ * Atom-resolved DFT-D4 energy (and gradient) of a padded batch.  Replaces
+ * ``tad_dftd4.dftd4`` (disp.py:44-146) / ``Disp.calculate``
+ * (dispersion/base.py:285-431) with the terms registered by ``dftd4``:
+ * ``TwoBodyTerm`` with rational damping at the EEQ charges
+ * (dispersion/twobody.py:60-201) and ``D4ATMApprox`` at q = 0
+ * (dispersion/threebody.py:54-163, 210-256, 311-321).  The gradient is the
+ * derivative of the total energy, through CN, charges, weights, C6, damping
+ * and ATM, as autograd gives in the reference.
+ */
+int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                  const d4_batch_t *batch, const d4_params_t *params,
+                  uint32_t flags, int32_t n_slots, void *d_workspace,
+                  size_t workspace_bytes, const d4_outputs_t *out, void *stream);
+
+/*
+ * Copy the device status word of a workspace to the host (synchronous on
+ * ``stream``) and clear it.  Returns a d4_status.
+ */
+int d4_read_status(void *d_workspace, void *stream);
+
+#ifdef __cplusplus
+}
+#endif
+
+#endif /* TAD_DFTD4_GB300_H */

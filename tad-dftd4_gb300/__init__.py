@@ -1,0 +1,35 @@
+"""
+tad-dftd4 dispersion on GB300: the ``dftd4()`` path of tad-dftd4 rebuilt as
+hand-written CUDA kernels behind a C ABI (``include/tad_dftd4_gb300.h``).
+
+Import with ``importlib.import_module("tad-dftd4_gb300")`` (the directory
+name carries a hyphen).  Public API, mirroring ``tad_dftd4``:
+
+* ``dftd4(numbers, positions, charge, param, *, model=..., cutoff=...)``
+* ``Cutoff``, ``D4Model``, ``D4SModel``, ``Param``, ``RationalDamping``,
+  ``ZeroDamping``
+* ``dispersion_energy_gradient`` -- energies and forces in one fused call
+"""
+
+from __future__ import annotations
+
+from . import _lib, tables, workloads  # noqa: F401
+from .cutoff import Cutoff
+from .damping import Damping, Param, RationalDamping, ZeroDamping
+from .disp import dftd4, dispersion_energy_gradient
+from .model import D4Model, D4SModel
+
+__version__ = "0.1.0"
+
+__all__ = [
+    "Cutoff",
+    "D4Model",
+    "D4SModel",
+    "Damping",
+    "Param",
+    "RationalDamping",
+    "ZeroDamping",
+    "dftd4",
+    "dispersion_energy_gradient",
+    "__version__",
+]

@@ -1,0 +1,122 @@
+// C ABI entry points (include/tad_dftd4_gb300.h).
+#include <stdio.h>
+#include <string.h>
+
+#include "d4_common.cuh"
+#include "d4_kernels.cuh"
+
+namespace {
+thread_local char g_cuda_error[256] = "";
+
+int check_cuda(cudaError_t e) {
+  if (e == cudaSuccess) return D4_OK;
+  snprintf(g_cuda_error, sizeof(g_cuda_error), "%s: %s", cudaGetErrorName(e),
+           cudaGetErrorString(e));
+  return D4_ERR_CUDA;
+}
+
+bool tables_ok(const d4_tables_t *t) {
+  return t && t->alpha && t->refcovcn && t->refc && t->refq && t->gam && t->zeff &&
+         t->r4r2 && t->cov_d3 && t->en && t->eeq_chi && t->eeq_eta && t->eeq_kcn &&
+         t->eeq_rad && t->freq_weights && t->n_ref_elem > 0 && t->n_elem >= t->n_ref_elem &&
+         t->n_ref_elem <= d4::MAX_ELEM_ID;
+}
+}  // namespace
+
+extern "C" {
+
+int d4_abi_version(void) { return D4_ABI_VERSION; }
+
+const char *d4_status_string(int status) {
+  switch (status) {
+    case D4_OK: return "ok";
+    case D4_ERR_ARGUMENT: return "invalid argument";
+    case D4_ERR_WORKSPACE: return "workspace too small";
+    case D4_ERR_CUDA: return "CUDA error";
+    case D4_ERR_ELEMENT: return "atomic number outside the element tables";
+    case D4_ERR_EEQ_SINGULAR: return "EEQ matrix is not positive definite";
+    case D4_ERR_NONFINITE: return "non-finite position or charge";
+    case D4_ERR_TOO_MANY_ELEMENTS: return "more distinct elements than D4S slots";
+    default: return "unknown status";
+  }
+}
+
+const char *d4_last_cuda_error(void) { return g_cuda_error; }
+
+int d4_prepare_alpha(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                     const double *d_refalpha, const double *d_refascale,
+                     const double *d_refscount, const int64_t *d_refsys,
+                     const double *d_secscale, const double *d_secalpha, int32_t n_sec,
+                     const double *d_refh, double *d_alpha_out, void *stream) {
+  if (!tables || !cfg || !d_refalpha || !d_refascale || !d_refscount || !d_refsys ||
+      !d_secscale || !d_secalpha || !d_refh || !d_alpha_out || n_sec <= 0 ||
+      !tables->gam || !tables->zeff || tables->n_ref_elem <= 0)
+    return D4_ERR_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  d4::launch_prepare_alpha(*tables, *cfg, d_refalpha, d_refascale, d_refscount, d_refsys,
+                           d_secscale, d_secalpha, n_sec, d_refh, d_alpha_out, st);
+  return check_cuda(cudaGetLastError());
+}
+
+size_t d4_workspace_size(int32_t n_struct, int32_t n_pad, int32_t n_slots, uint32_t flags) {
+  if (n_struct <= 0 || n_pad <= 0 || n_slots <= 0) return 0;
+  return d4::carve_workspace(nullptr, n_struct, n_pad, n_slots, flags).bytes;
+}
+
+int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                  const d4_batch_t *batch, const d4_params_t *params, uint32_t flags,
+                  int32_t n_slots, void *d_workspace, size_t workspace_bytes,
+                  const d4_outputs_t *out, void *stream) {
+  if (!tables_ok(tables) || !cfg || !batch || !params || !out || !d_workspace)
+    return D4_ERR_ARGUMENT;
+  if (batch->n_struct <= 0 || batch->n_pad <= 0 || batch->n_struct > 65535 || n_slots <= 0)
+    return D4_ERR_ARGUMENT;
+  if (!batch->d_numbers || !batch->d_positions || !batch->d_charge || !out->d_energy)
+    return D4_ERR_ARGUMENT;
+  if ((flags & D4_FLAG_GRADIENT) && !out->d_gradient) return D4_ERR_ARGUMENT;
+  if ((flags & D4_FLAG_CHARGES_IN) && !batch->d_charges_in) return D4_ERR_ARGUMENT;
+  if ((flags & D4_FLAG_PARAM_GRAD) && (!out->d_param_grad || !(flags & D4_FLAG_GRADIENT)))
+    return D4_ERR_ARGUMENT;
+  if (cfg->kind != D4_MODEL_D4 && cfg->kind != D4_MODEL_D4S) return D4_ERR_ARGUMENT;
+  if (cfg->kind == D4_MODEL_D4S && !tables->wfpair) return D4_ERR_ARGUMENT;
+  if (cfg->kind == D4_MODEL_D4 && n_slots != 1) return D4_ERR_ARGUMENT;
+  if (flags & D4_FLAG_MIXED) return D4_ERR_ARGUMENT;  // precision form: separate library path
+  d4::Workspace w = d4::carve_workspace(d_workspace, batch->n_struct, batch->n_pad, n_slots,
+                                        flags);
+  if (workspace_bytes < w.bytes) return D4_ERR_WORKSPACE;
+  d4::Ctx c;
+  c.tab = *tables;
+  c.cfg = *cfg;
+  c.par = *params;
+  c.numbers = batch->d_numbers;
+  c.positions = batch->d_positions;
+  c.charge = batch->d_charge;
+  c.charges_in = batch->d_charges_in;
+  c.r4r2_in = batch->d_r4r2_in;
+  c.weights = batch->d_energy_weights;
+  c.B = batch->n_struct;
+  c.N = batch->n_pad;
+  c.S = n_slots;
+  c.flags = flags;
+  c.w = w;
+  c.out = *out;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  d4::launch_fp64(c, st);
+  return check_cuda(cudaGetLastError());
+}
+
+int d4_read_status(void *d_workspace, void *stream) {
+  if (!d_workspace) return D4_ERR_ARGUMENT;
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int status = 0;
+  d4::Workspace w = d4::carve_workspace(d_workspace, 1, 1, 1, 0);
+  int rc = check_cuda(cudaMemcpyAsync(&status, w.status, sizeof(int), cudaMemcpyDeviceToHost, st));
+  if (rc != D4_OK) return rc;
+  rc = check_cuda(cudaStreamSynchronize(st));
+  if (rc != D4_OK) return rc;
+  rc = check_cuda(cudaMemsetAsync(w.status, 0, sizeof(int), st));
+  if (rc != D4_OK) return rc;
+  return status;
+}
+
+}  // extern "C"

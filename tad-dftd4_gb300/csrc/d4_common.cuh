@@ -1,0 +1,189 @@
+// Shared device-side definitions for the DFT-D4 kernels.
+#pragma once
+
+#include <cuda_runtime.h>
+#include <stdint.h>
+
+#include "tad_dftd4_gb300.h"
+
+namespace d4 {
+
+constexpr int NREF = D4_NREF;
+constexpr int NFREQ = D4_NFREQ;
+constexpr int MAX_ELEM_ID = 128;  // element ids are < 128 in every table
+constexpr double THOPI = 3.0 / 3.141592653589793238462643383279502884197;  // utils.py:50
+constexpr double SQRT_2_OVER_PI = 0.79788456080286535587989211986876;
+constexpr double INV_SQRT_PI = 0.56418958354775628694807945156077;
+
+// Workspace carved out of one caller-provided buffer.  The same function
+// computes the layout for d4_workspace_size and d4_dispersion.
+struct Workspace {
+  int *status;      // [1]
+  int *n_eff;       // [B]   highest real atom index + 1
+  int *n_slots;     // [B]   distinct-element slots (D4S), 1 for D4
+  int *z;           // [B*N] validated atomic numbers (0: padding or invalid)
+  int *slot;        // [B*N] slot of each atom's element in its structure
+  int *slot_elem;   // [B*MAX_ELEM_ID] element of each slot
+  double *cn;       // [B*N] D4 coordination number
+  double *cnq;      // [B*N] capped EEQ coordination number
+  double *dcnq;     // [B*N] d(capped)/d(raw)
+  double *q;        // [B*N] atomic charges
+  double *eeq_y;    // [B*N] A^-1 1
+  double *eeq_w;    // [B*N] adjoint charges
+  double *eeq_sum;  // [B*2] (sum y, lambda)
+  double *dEdcn;    // [B*N]
+  double *dEdq;     // [B*N]
+  double *dEdcnq;   // [B*N] dE/d(raw EEQ CN)
+  double *e3;       // [B*N] ATM energy (accumulated atomically)
+  double *pgrad;    // [B*8] parameter gradients (atomics)
+  double *A;        // [B*N*S*23] weighted polarisabilities at q
+  double *A0;       // [B*N*S*23] at q = 0
+  double *dA_dcn;   // [B*N*S*23]
+  double *dA_dq;    // [B*N*S*23]
+  double *dA0_dcn;  // [B*N*S*23]
+  double *G;        // [B*N*S*23] dE/dA
+  double *G0;       // [B*N*S*23] dE/dA0
+  double *pr_r;     // [B*N*N] distance
+  double *pr_ir;    // [B*N*N] 1/distance
+  double *pr_L;     // [B*N*N] log(R0/r) of the ATM damping
+  double *pr_c;     // [B*N*N] sqrt(C6 at q = 0)
+  double *pr_S;     // [B*N*N] dE_ATM/d(r^2) (atomics)
+  double *pr_P;     // [B*N*N] sum of weighted triple energies (atomics)
+  double *pr_da1;   // [B*N*N] d log R0 / d a1 (parameter gradients only)
+  double *pr_da2;   // [B*N*N] d log R0 / d a2 (parameter gradients only)
+  double *eeq_L;    // [B*N*(N+1)/2] packed Cholesky factor
+  size_t bytes;
+};
+
+inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Layout of the workspace; ``base == nullptr`` only measures it.
+inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags) {
+  Workspace w{};
+  size_t off = 0;
+  char *p = static_cast<char *>(base);
+  auto take = [&](size_t bytes) -> void * {
+    off = align_up(off, 256);
+    void *r = p ? p + off : nullptr;
+    off += bytes;
+    return r;
+  };
+  const size_t BN = (size_t)B * N;
+  const size_t BNS23 = BN * S * NFREQ;
+  const size_t BNN = BN * N;
+  const bool grad = (flags & D4_FLAG_GRADIENT) != 0;
+  w.status = (int *)take(sizeof(int) * 4);
+  w.n_eff = (int *)take(sizeof(int) * B);
+  w.n_slots = (int *)take(sizeof(int) * B);
+  w.z = (int *)take(sizeof(int) * BN);
+  w.slot = (int *)take(sizeof(int) * BN);
+  w.slot_elem = (int *)take(sizeof(int) * B * MAX_ELEM_ID);
+  w.cn = (double *)take(8 * BN);
+  w.cnq = (double *)take(8 * BN);
+  w.dcnq = (double *)take(8 * BN);
+  w.q = (double *)take(8 * BN);
+  w.eeq_y = (double *)take(8 * BN);
+  w.eeq_w = (double *)take(8 * BN);
+  w.eeq_sum = (double *)take(8 * 2 * B);
+  w.dEdcn = (double *)take(8 * BN);
+  w.dEdq = (double *)take(8 * BN);
+  w.dEdcnq = (double *)take(8 * BN);
+  w.e3 = (double *)take(8 * BN);
+  w.pgrad = (double *)take(8 * 8 * B);
+  w.A = (double *)take(8 * BNS23);
+  w.A0 = (double *)take(8 * BNS23);
+  w.dA_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.dA_dq = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.dA0_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.G = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.G0 = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.pr_r = (double *)take(8 * BNN);
+  w.pr_ir = (double *)take(8 * BNN);
+  w.pr_L = (double *)take(8 * BNN);
+  w.pr_c = (double *)take(8 * BNN);
+  w.pr_S = grad ? (double *)take(8 * BNN) : nullptr;
+  w.pr_P = grad ? (double *)take(8 * BNN) : nullptr;
+  const bool pgrad = (flags & D4_FLAG_PARAM_GRAD) != 0;
+  w.pr_da1 = pgrad ? (double *)take(8 * BNN) : nullptr;
+  w.pr_da2 = pgrad ? (double *)take(8 * BNN) : nullptr;
+  w.eeq_L = (double *)take(8 * (size_t)B * ((size_t)N * (N + 1) / 2));
+  w.bytes = align_up(off, 256);
+  return w;
+}
+
+// Everything a kernel needs, passed by value.
+struct Ctx {
+  d4_tables_t tab;
+  d4_model_cfg_t cfg;
+  d4_params_t par;
+  const int64_t *numbers;
+  const double *positions;
+  const double *charge;
+  const double *charges_in;
+  const double *r4r2_in;
+  const double *weights;
+  int B, N, S;
+  uint32_t flags;
+  Workspace w;
+  d4_outputs_t out;
+};
+
+// ---------------------------------------------------------------- helpers
+
+__device__ __forceinline__ double atom_r4r2(const Ctx &c, size_t a, int64_t z) {
+  return c.r4r2_in ? c.r4r2_in[a] : c.tab.r4r2[z];
+}
+
+__device__ __forceinline__ double atom_weight(const Ctx &c, size_t a) {
+  return c.weights ? c.weights[a] : 1.0;
+}
+
+__device__ __forceinline__ double warp_sum(double v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ void set_status(int *status, int code) {
+  atomicCAS(status, 0, code);
+}
+
+// Error-function counting function of the CN: 1/2 (1 + erf(-k (r/r0 - 1))).
+__device__ __forceinline__ double erf_count(double r, double r0, double k) {
+  return 0.5 * (1.0 + erf(-k * (r / r0 - 1.0)));
+}
+
+// Its derivative with respect to r.
+__device__ __forceinline__ double erf_count_dr(double r, double r0, double k) {
+  const double x = k * (r / r0 - 1.0);
+  return -k / r0 * INV_SQRT_PI * exp(-x * x);
+}
+
+// EN weighting of the D4 CN: k4 exp(-(|en_i - en_j| + k5)^2 / k6).
+__device__ __forceinline__ double en_factor(double eni, double enj, double k4, double k5,
+                                            double k6) {
+  const double t = fabs(eni - enj) + k5;
+  return k4 * exp(-(t * t) / k6);
+}
+
+// Charge-scaling function zeta (model/base.py:308-335) and d zeta / d qmod.
+__device__ __forceinline__ void zeta_and_deriv(double gam, double qref, double qmod,
+                                               double ga, double eps, double *z,
+                                               double *dz) {
+  if (qmod > 0.0) {
+    const double den = qmod - eps;
+    const double scale = exp(gam * (1.0 - qref / den));
+    const double zz = exp(ga * (1.0 - scale));
+    *z = zz;
+    *dz = -ga * zz * scale * gam * qref / (den * den);
+  } else {
+    *z = exp(ga);
+    *dz = 0.0;
+  }
+}
+
+__host__ __device__ inline size_t tri_index(int i, int j) {  // packed lower, j <= i
+  return (size_t)i * (i + 1) / 2 + j;
+}
+
+}  // namespace d4

@@ -1,0 +1,279 @@
+"""
+Drop-in ``dftd4()`` (``tad_dftd4/disp.py:44-146``) on the CUDA library.
+
+The signature, the zero-padded batch convention (atomic number 0 marks
+padding), the result's shape, dtype and device, and the errors follow the
+reference.  Every number is computed by the compiled kernels through the C
+ABI; this module only validates, packs pointers and wires autograd.
+
+Gradients: when ``positions`` (or a damping parameter) requires grad, the
+forward call also runs the hand-written adjoint and keeps dE_b/dR per
+structure.  ``backward`` scales it by the incoming gradient when that is
+uniform within each structure (the case of ``energy.sum()`` or per-structure
+sums); any other weighting re-runs the adjoint with those per-atom weights.
+"""
+
+from __future__ import annotations
+
+import ctypes
+from dataclasses import dataclass
+
+import torch
+
+from . import _lib, tables as _tables
+from .cutoff import (D4_CN_CUTOFF, D4_CN_EEQ_MAX, D4_K4, D4_K5, D4_K6, D4_KCN, Cutoff)
+from .damping import PARAM_ORDER, Damping, Param, RationalDamping, ZeroDamping, resolve
+from .model import BaseModel, D4Model, D4SModel
+
+__all__ = ["dftd4", "dispersion_energy_gradient", "Runner"]
+
+_ALLOWED_MODELS = ("d3", "d4", "d4s", "d5")
+CHECK_STATUS = True
+
+
+def _as_tensor(x, device, dtype):
+    if isinstance(x, torch.Tensor):
+        return x.to(device=device, dtype=dtype)
+    return torch.tensor(x, device=device, dtype=dtype)
+
+
+def _resolve_model(model, numbers) -> BaseModel:
+    if isinstance(model, str):
+        key = model.casefold()
+        if key not in _ALLOWED_MODELS:
+            raise ValueError(
+                f"Unknown model '{key}'. Please use {', '.join(_ALLOWED_MODELS)}."
+            )
+        if key == "d4":
+            return D4Model(numbers)
+        if key == "d4s":
+            return D4SModel(numbers)
+        raise NotImplementedError(f"model '{key}' has no dispersion model in tad-dftd4")
+    if isinstance(model, BaseModel):
+        return model
+    raise TypeError(f"unsupported model object {type(model).__name__}")
+
+
+@dataclass
+class Runner:
+    """One configured call of the library on a padded batch (B, N)."""
+
+    numbers: torch.Tensor  # (B, N) int64, device
+    charge: torch.Tensor  # (B,) float64, device
+    tables: _tables.DeviceTables
+    model: BaseModel
+    params: dict
+    cut: dict
+    q: torch.Tensor | None = None
+    r4r2: torch.Tensor | None = None
+    n_slots: int = 1
+
+    def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
+            weights: torch.Tensor | None = None, charges_out: bool = False,
+            cn_out: bool = False):
+        lib = _lib.load()
+        device = positions.device
+        B, N = self.numbers.shape
+        pos = positions.detach().to(torch.float64).contiguous()
+        flags = 0
+        if gradient or param_grad:
+            flags |= _lib.FLAG_GRADIENT
+        if param_grad:
+            flags |= _lib.FLAG_PARAM_GRAD
+        if self.q is not None:
+            flags |= _lib.FLAG_CHARGES_IN
+        energy = torch.empty((B, N), dtype=torch.float64, device=device)
+        grad = (torch.empty((B, N, 3), dtype=torch.float64, device=device)
+                if flags & _lib.FLAG_GRADIENT else None)
+        pgrad = (torch.empty((B, 8), dtype=torch.float64, device=device)
+                 if param_grad else None)
+        qout = torch.empty((B, N), dtype=torch.float64, device=device) if charges_out else None
+        cnout = torch.empty((B, N), dtype=torch.float64, device=device) if cn_out else None
+        w = None if weights is None else weights.to(torch.float64).contiguous()
+        ws_bytes = lib.d4_workspace_size(B, N, self.n_slots, flags)
+        work = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        p = self.params
+        params = _lib.Params(
+            s6=p["s6"], s8=p["s8"], s10=p["s10"], a1=p["a1"], a2=p["a2"], s9=p["s9"],
+            alp=p["alp"], has_s8=int(p["has_s8"]), has_s10=int(p["has_s10"]),
+            cut_disp2=self.cut["disp2"], cut_disp3=self.cut["disp3"],
+            cut_cn=self.cut["cn"], cut_cn_eeq=self.cut["cn_eeq"],
+            cn_eeq_max=D4_CN_EEQ_MAX, kcn=D4_KCN, k4=D4_K4, k5=D4_K5, k6=D4_K6,
+        )
+        batch = _lib.Batch(
+            n_struct=B, n_pad=N, d_numbers=self.numbers.data_ptr(), d_positions=pos.data_ptr(),
+            d_charge=self.charge.data_ptr(),
+            d_charges_in=self.q.data_ptr() if self.q is not None else None,
+            d_r4r2_in=self.r4r2.data_ptr() if self.r4r2 is not None else None,
+            d_energy_weights=w.data_ptr() if w is not None else None,
+        )
+        outs = _lib.Outputs(
+            d_energy=energy.data_ptr(),
+            d_gradient=grad.data_ptr() if grad is not None else None,
+            d_charges=qout.data_ptr() if qout is not None else None,
+            d_cn=cnout.data_ptr() if cnout is not None else None,
+            d_param_grad=pgrad.data_ptr() if pgrad is not None else None,
+        )
+        cfg = _lib.ModelCfg(kind=_lib.MODEL_D4S if self.model.kind == "d4s" else _lib.MODEL_D4,
+                            ga=self.model.ga, gc=self.model.gc,
+                            wf=self.model.wf if self.model.wf is not None else 6.0)
+        stream = torch.cuda.current_stream(device).cuda_stream
+        with torch.cuda.device(device):
+            _lib.check(lib.d4_dispersion(self.tables.struct, cfg, batch, params, flags,
+                                         self.n_slots, work.data_ptr(), ws_bytes, outs, stream),
+                       "d4_dispersion")
+            if CHECK_STATUS:
+                status = lib.d4_read_status(work.data_ptr(), stream)
+                if status == 4:
+                    raise ValueError("atomic number outside the element tables")
+                if status == 6:
+                    raise ValueError("non-finite positions or charges")
+                _lib.check(status, "d4_dispersion (device status)")
+        return energy, grad, pgrad, qout, cnout
+
+
+class _D4Function(torch.autograd.Function):
+    @staticmethod
+    def forward(ctx, positions, pvec, runner: Runner):
+        need_pos = ctx.needs_input_grad[0]
+        need_par = ctx.needs_input_grad[1]
+        energy, grad, pgrad, _, _ = runner.run(positions, gradient=need_pos or need_par,
+                                               param_grad=need_par)
+        ctx.runner = runner
+        ctx.positions = positions.detach()
+        ctx.save_for_backward(grad if grad is not None else torch.empty(0),
+                              pgrad if pgrad is not None else torch.empty(0))
+        return energy.to(positions.dtype)
+
+    @staticmethod
+    def backward(ctx, go):
+        grad, pgrad = ctx.saved_tensors
+        runner: Runner = ctx.runner
+        go = go.to(torch.float64)
+        real = runner.numbers != 0
+        first = torch.argmax(real.to(torch.int8), dim=-1, keepdim=True)
+        w0 = torch.gather(go, -1, first)  # (B, 1)
+        uniform = bool((((go - w0) * real).abs().amax() == 0).item())
+        if not uniform:
+            _, grad, pgrad, _, _ = runner.run(ctx.positions, gradient=True,
+                                              param_grad=ctx.needs_input_grad[1],
+                                              weights=go * real)
+            w0 = torch.ones_like(w0)
+        gpos = gpar = None
+        if ctx.needs_input_grad[0]:
+            gpos = (w0.unsqueeze(-1) * grad).to(ctx.positions.dtype)
+        if ctx.needs_input_grad[1]:
+            gpar = (w0 * pgrad).sum(0)[: len(PARAM_ORDER)]
+        return gpos, gpar, None
+
+
+def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
+             cn_function, counting_function, damping_function):
+    device = positions.device
+    dtype = positions.dtype
+    charge = _as_tensor(charge, device, dtype)
+    if numbers.shape != positions.shape[:-1]:
+        raise ValueError(
+            f"Shape of positions ({positions.shape}) is not consistent with atomic "
+            f"numbers ({numbers.shape})."
+        )
+    if cutoff is None:
+        cutoff = Cutoff(device=device, dtype=dtype)
+    mdl = _resolve_model(model, numbers)
+    if rcov is not None and numbers.shape != rcov.shape:
+        raise ValueError(f"Shape of covalent radii ({rcov.shape}) is not consistent with "
+                         f"atomic numbers ({numbers.shape}).")
+    if r4r2 is not None and numbers.shape != r4r2.shape:
+        raise ValueError(f"Shape of expectation values r4r2 ({r4r2.shape}) is not "
+                         f"consistent with atomic numbers ({numbers.shape}).")
+    if rvdw is not None and numbers.shape != rvdw.shape[:-1]:
+        raise ValueError(f"Shape of van der Waals radii ({rvdw.shape}) is not consistent "
+                         f"with atomic numbers ({numbers.shape}).")
+    if q is not None and numbers.shape != q.shape:
+        raise ValueError(f"Shape of atomic charges ({q.shape}) is not consistent with "
+                         f"atomic numbers ({numbers.shape}).")
+    if cn_function is not None or counting_function is not None:
+        raise NotImplementedError(
+            "only the default D4 coordination number (cn_d4 with erf_count) is built in")
+    if damping_function is not None and not isinstance(damping_function, RationalDamping):
+        if isinstance(damping_function, Damping) and damping_function.radius_type != "r4r2":
+            raise ValueError("`rvdw` radius type is not used by the two-body term of dftd4")
+        raise NotImplementedError("only rational (BJ) damping is built in for dftd4")
+    resolved = resolve(param)
+    if device.type != "cuda":
+        raise RuntimeError("tad-dftd4_gb300 runs on CUDA devices; move the inputs to a GPU")
+
+    shape = numbers.shape
+    N = shape[-1]
+    nums = numbers.reshape(-1, N).to(device=device, dtype=torch.int64).contiguous()
+    B = nums.shape[0]
+    if charge.dim() == 0:
+        chg = charge.to(torch.float64).expand(B).contiguous()
+    else:
+        chg = charge.reshape(-1).to(torch.float64).contiguous()
+        if chg.numel() != B:
+            raise ValueError(f"charge of shape {tuple(charge.shape)} for {B} structures")
+    tab = _tables.device_tables(device, mdl.ref_charges, mdl.ga, mdl.gc)
+    n_slots = 1
+    if mdl.kind == "d4s":
+        present = torch.zeros((B, 128), dtype=torch.int32, device=device)
+        present.scatter_(1, nums.clamp(0, 127), 1)
+        present[:, 0] = 0
+        n_slots = max(1, int(present.sum(1).max().item()))
+    cut = {
+        "disp2": float(cutoff.disp2), "disp3": float(cutoff.disp3),
+        "cn": D4_CN_CUTOFF, "cn_eeq": float(cutoff.cn_eeq),
+    }
+    runner = Runner(
+        numbers=nums, charge=chg, tables=tab, model=mdl, params=resolved, cut=cut,
+        q=None if q is None else q.reshape(-1, N).to(torch.float64).contiguous(),
+        r4r2=None if r4r2 is None else r4r2.reshape(-1, N).to(torch.float64).contiguous(),
+        n_slots=n_slots,
+    )
+    pvec = []
+    for key in PARAM_ORDER:
+        v = param.get(key)
+        if isinstance(v, torch.Tensor):
+            pvec.append(v.reshape(()).to(device=device, dtype=torch.float64))
+        else:
+            pvec.append(torch.tensor(resolved[key], dtype=torch.float64, device=device))
+    return runner, torch.stack(pvec), shape
+
+
+def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, *,
+          model="d4", rcov=None, r4r2=None, rvdw=None, q=None, cutoff: Cutoff | None = None,
+          cn_function=None, counting_function=None,
+          damping_function: Damping | None = None) -> torch.Tensor:
+    """
+    Atom-resolved DFT-D4 dispersion energy of a structure or a padded batch.
+
+    Same arguments and result as ``tad_dftd4.dftd4``: ``numbers`` (..., N)
+    with 0 for padding, ``positions`` (..., N, 3) in Bohr on a CUDA device,
+    total ``charge`` (scalar or per structure), damping parameters ``param``.
+    Returns (..., N) energies in Hartree with the dtype of ``positions``.
+    ``cn_function`` / ``counting_function`` / ``damping_function`` accept
+    only the defaults (D4 CN with erf counting, rational damping).
+    """
+    runner, pvec, shape = _prepare(numbers, positions, charge, param, model, rcov, r4r2,
+                                   rvdw, q, cutoff, cn_function, counting_function,
+                                   damping_function)
+    pos = positions.reshape(-1, shape[-1], 3)
+    energy = _D4Function.apply(pos, pvec, runner)
+    return energy.reshape(shape)
+
+
+def dispersion_energy_gradient(numbers, positions, charge, param, **kw):
+    """
+    Energies (..., N) and the gradient d(sum E)/dR (..., N, 3) in one fused
+    call, without autograd bookkeeping.  Same arguments as ``dftd4``.
+    """
+    runner, _, shape = _prepare(numbers, positions, charge, param, kw.pop("model", "d4"),
+                                kw.pop("rcov", None), kw.pop("r4r2", None),
+                                kw.pop("rvdw", None), kw.pop("q", None),
+                                kw.pop("cutoff", None), None, None, None)
+    if kw:
+        raise TypeError(f"unexpected arguments {sorted(kw)}")
+    pos = positions.reshape(-1, shape[-1], 3)
+    energy, grad, _, _, _ = runner.run(pos, gradient=True)
+    return (energy.reshape(shape).to(positions.dtype),
+            grad.reshape(*shape, 3).to(positions.dtype))

@@ -1,0 +1,205 @@
+"""
+Parity of the CUDA path with tad-dftd4's own outputs and with the oracle.
+
+Tolerances (float64, plain method): atom energies 1e-12 relative with a
+1e-15 Eh absolute floor; gradients 1e-10 relative with a 1e-13 Eh/Bohr
+floor; charges and CN 1e-10 relative.  The golden fixtures are the
+reference's own values (``tests/golden/golden.npz``).
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import assert_close, golden_cases, package
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+E_RTOL, E_ATOL = 1e-12, 1e-15
+G_RTOL, G_ATOL = 1e-10, 1e-13
+
+
+@pytest.fixture(scope="module")
+def d4():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return package()
+
+
+def _model(d4, meta, numbers):
+    cls = d4.D4Model if meta["model"] == "d4" else d4.D4SModel
+    return cls(numbers, ref_charges=meta["ref_charges"])
+
+
+def _run(d4, arrays, meta, grad=True, param_grad=False):
+    dev = torch.device("cuda")
+    numbers = torch.from_numpy(arrays["numbers"]).to(dev)
+    positions = torch.from_numpy(arrays["positions"]).to(dev)
+    charge = torch.from_numpy(arrays["charge"]).to(dev)
+    cutoff = d4.Cutoff(**meta["cutoff"]) if meta["cutoff"] else None
+    keys = sorted(meta["param"])
+    param = {k: torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=param_grad)
+             for k, v in meta["param"].items()}
+    pos = positions.clone().requires_grad_(grad)
+    energy = d4.dftd4(numbers, pos, charge, param, model=_model(d4, meta, numbers),
+                      cutoff=cutoff)
+    out = {"energy": energy.detach().cpu().numpy()}
+    if grad or param_grad:
+        wrt = ([pos] if grad else []) + ([param[k] for k in keys] if param_grad else [])
+        gs = torch.autograd.grad(energy.sum(), wrt)
+        if grad:
+            out["grad"] = gs[0].cpu().numpy()
+        if param_grad:
+            out["param_grad"] = np.array([g.item() for g in gs[-len(keys):]])
+    return out
+
+
+@pytest.mark.parametrize("tag,arrays,meta", CASES, ids=[c[0] for c in CASES])
+def test_energy_matches_reference(d4, tag, arrays, meta):
+    out = _run(d4, arrays, meta, grad=False)
+    assert_close(out["energy"], arrays["energy"], E_RTOL, E_ATOL, "energy")
+
+
+@pytest.mark.parametrize("tag,arrays,meta",
+                         [c for c in CASES if not c[2]["energy_only"]],
+                         ids=[c[0] for c in CASES if not c[2]["energy_only"]])
+def test_gradient_matches_reference(d4, tag, arrays, meta):
+    out = _run(d4, arrays, meta, grad=True)
+    assert_close(out["energy"], arrays["energy"], E_RTOL, E_ATOL, "energy")
+    assert_close(out["grad"], arrays["grad"], G_RTOL, G_ATOL, "grad")
+
+
+@pytest.mark.parametrize("tag,arrays,meta",
+                         [c for c in CASES if not c[2]["energy_only"]],
+                         ids=[c[0] for c in CASES if not c[2]["energy_only"]])
+def test_param_gradient_matches_reference(d4, tag, arrays, meta):
+    out = _run(d4, arrays, meta, grad=False, param_grad=True)
+    assert_close(out["param_grad"], arrays["param_grad"], G_RTOL, G_ATOL, "param_grad")
+
+
+@pytest.mark.parametrize("tag,arrays,meta", CASES, ids=[c[0] for c in CASES])
+def test_charges_and_cn(d4, tag, arrays, meta):
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    dev = torch.device("cuda")
+    numbers = torch.from_numpy(arrays["numbers"]).to(dev)
+    positions = torch.from_numpy(arrays["positions"]).to(dev)
+    charge = torch.from_numpy(arrays["charge"]).to(dev)
+    cutoff = d4.Cutoff(**meta["cutoff"]) if meta["cutoff"] else None
+    runner, _, _ = disp._prepare(numbers, positions, charge, meta["param"],
+                                 _model(d4, meta, numbers), None, None, None, None, cutoff,
+                                 None, None, None)
+    _, _, _, q, cn = runner.run(positions, charges_out=True, cn_out=True)
+    assert_close(cn.cpu().numpy(), arrays["cn"], 1e-12, 1e-15, "cn")
+    assert_close(q.cpu().numpy(), arrays["q"], 1e-10, 1e-13, "q")
+
+
+def _batch(seed, nstruct, nmin, nmax, charged=True):
+    wl = package().workloads
+    return wl.batch_uniform(seed, nstruct, nmin, nmax, wl.ELEMENTS_12, charged, "t", nmax)
+
+
+@pytest.mark.parametrize("model", ["d4", "d4s"])
+def test_random_batch_vs_oracle(d4, model):
+    b = _batch(101, 6, 5, 60)
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    numbers = torch.from_numpy(b.numbers)
+    positions = torch.from_numpy(b.positions)
+    charge = torch.from_numpy(b.charge)
+    e_ref, g_ref = oracle.dftd4_energy_and_grad(numbers, positions, charge, param, model=model)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(numbers.to(dev), positions.to(dev), charge.to(dev),
+                                         param, model=model)
+    assert_close(e.cpu().numpy(), e_ref.numpy(), E_RTOL, E_ATOL, "energy")
+    assert_close(g.cpu().numpy(), g_ref.numpy(), G_RTOL, G_ATOL, "grad")
+
+
+def test_nonuniform_backward_weights(d4):
+    """autograd with per-atom weights (not a plain sum) re-runs the adjoint."""
+    b = _batch(102, 3, 4, 20)
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    numbers = torch.from_numpy(b.numbers)
+    positions = torch.from_numpy(b.positions)
+    charge = torch.from_numpy(b.charge)
+    wts = torch.linspace(0.2, 1.7, numbers.numel(), dtype=torch.float64).reshape(numbers.shape)
+    pos_ref = positions.clone().requires_grad_(True)
+    e_ref = oracle.dftd4(numbers, pos_ref, charge, param)
+    (g_ref,) = torch.autograd.grad((e_ref * wts).sum(), pos_ref)
+    dev = torch.device("cuda")
+    pos = positions.to(dev).requires_grad_(True)
+    e = d4.dftd4(numbers.to(dev), pos, charge.to(dev), param)
+    (g,) = torch.autograd.grad((e * wts.to(dev)).sum(), pos)
+    assert_close(g.cpu().numpy(), g_ref.numpy(), G_RTOL, G_ATOL, "weighted grad")
+
+
+def test_padding_in_the_middle_and_empty_structure(d4):
+    b = _batch(103, 3, 6, 12)
+    numbers = b.numbers.copy()
+    positions = b.positions.copy()
+    numbers[0, 2] = 0  # a hole inside structure 0
+    numbers[2, :] = 0  # an all-padding structure
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    nt, pt, ct = map(torch.from_numpy, (numbers, positions, b.charge * 0))
+    # the oracle's dense EEQ system is singular for an all-padding structure,
+    # so it sees only the first two
+    e_ref, g_ref = oracle.dftd4_energy_and_grad(nt[:2], pt[:2], ct[:2], param)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(nt.to(dev), pt.to(dev), ct.to(dev), param)
+    assert_close(e.cpu().numpy()[:2], e_ref.numpy(), E_RTOL, E_ATOL, "energy")
+    assert_close(g.cpu().numpy()[:2], g_ref.numpy(), G_RTOL, G_ATOL, "grad")
+    assert (e.cpu().numpy()[2] == 0).all() and (g.cpu().numpy()[2] == 0).all()
+
+
+def test_single_and_two_atoms(d4):
+    dev = torch.device("cuda")
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    for z, r in (([6], [[0.0, 0.0, 0.0]]), ([1, 8], [[0.0, 0.0, 0.0], [0.0, 0.0, 1.8]])):
+        nt = torch.tensor(z)
+        pt = torch.tensor(r, dtype=torch.float64)
+        e_ref, g_ref = oracle.dftd4_energy_and_grad(nt, pt, torch.tensor(0.0), param)
+        e, g = d4.dispersion_energy_gradient(nt.to(dev), pt.to(dev), 0.0, param)
+        assert e.shape == nt.shape
+        assert_close(e.cpu().numpy(), e_ref.numpy(), E_RTOL, E_ATOL, "energy")
+        assert_close(g.cpu().numpy(), g_ref.numpy(), G_RTOL, G_ATOL, "grad")
+
+
+def test_given_charges_and_r4r2(d4):
+    b = _batch(104, 2, 8, 16, charged=False)
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    nt, pt, ct = map(torch.from_numpy, (b.numbers, b.positions, b.charge))
+    q = torch.linspace(-0.3, 0.3, nt.numel(), dtype=torch.float64).reshape(nt.shape)
+    q = torch.where(nt != 0, q, torch.zeros_like(q))
+    e_ref = oracle.dftd4(nt, pt, ct, param, q=q)
+    dev = torch.device("cuda")
+    e = d4.dftd4(nt.to(dev), pt.to(dev), ct.to(dev), param, q=q.to(dev))
+    assert_close(e.cpu().numpy(), e_ref.numpy(), E_RTOL, E_ATOL, "energy with q")
+
+
+def test_float32_positions_follow_dtype(d4):
+    b = _batch(105, 2, 8, 16)
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    dev = torch.device("cuda")
+    pos = torch.from_numpy(b.positions).to(dev, torch.float32)
+    e = d4.dftd4(torch.from_numpy(b.numbers).to(dev), pos, torch.from_numpy(b.charge).to(dev),
+                 param)
+    assert e.dtype == torch.float32 and e.device == pos.device
+
+
+def test_bad_element_raises(d4):
+    dev = torch.device("cuda")
+    nt = torch.tensor([1, 104], device=dev)
+    pt = torch.tensor([[0.0, 0, 0], [0, 0, 2.0]], dtype=torch.float64, device=dev)
+    with pytest.raises(ValueError):
+        d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})
+
+
+def test_nonfinite_positions_raise(d4):
+    dev = torch.device("cuda")
+    nt = torch.tensor([1, 1], device=dev)
+    pt = torch.tensor([[0.0, 0, 0], [0, 0, float("nan")]], dtype=torch.float64, device=dev)
+    with pytest.raises(ValueError):
+        d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})

@@ -1,0 +1,80 @@
+"""
+Host-side behaviour of the drop-in ``dftd4()`` that needs no GPU: the
+reference's argument checks and error types (``dispersion/base.py:354-414``,
+``damping/functions.py:68-114``) and the refusal to compute on the CPU.
+"""
+
+from __future__ import annotations
+
+import pytest
+import torch
+
+from conftest import package
+
+PARAM = {"s6": 1.0, "s8": 1.0, "a1": 0.4, "a2": 5.0}
+
+
+@pytest.fixture
+def d4():
+    return package()
+
+
+def test_shape_errors(d4):
+    numbers = torch.tensor([1, 1])
+    positions = torch.tensor([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    with pytest.raises(ValueError):
+        d4.dftd4(numbers, positions, 0.0, PARAM, rcov=torch.tensor([1.0]))
+    with pytest.raises(ValueError):
+        d4.dftd4(numbers, positions, 0.0, PARAM, r4r2=torch.tensor([1.0]))
+    with pytest.raises(ValueError):
+        d4.dftd4(numbers, positions, 0.0, PARAM, rvdw=torch.tensor([1.0]))
+    with pytest.raises(ValueError):
+        d4.dftd4(numbers, positions, 0.0, PARAM, q=torch.tensor([1.0]))
+    with pytest.raises(ValueError):
+        d4.dftd4(torch.tensor([1]), positions, 0.0, PARAM, q=torch.tensor([0.5, -0.5]))
+
+
+def test_missing_damping_parameters_raise_type_error(d4):
+    numbers = torch.tensor([1, 1])
+    positions = torch.tensor([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    with pytest.raises(TypeError):
+        d4.dftd4(numbers, positions, 0.0, {"s6": 1.0})
+
+
+def test_unknown_model(d4):
+    numbers = torch.tensor([1, 1])
+    positions = torch.tensor([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]])
+    with pytest.raises(ValueError):
+        d4.dftd4(numbers, positions, 0.0, PARAM, model="d9")
+
+
+def test_cpu_inputs_are_refused(d4):
+    numbers = torch.tensor([1, 1])
+    positions = torch.tensor([[0.0, 0.0, 0.0], [0.0, 0.0, 1.0]], dtype=torch.float64)
+    with pytest.raises(RuntimeError, match="CUDA"):
+        d4.dftd4(numbers, positions, 0.0, PARAM)
+
+
+def test_param_resolution_follows_reference_gating(d4):
+    from importlib import import_module
+    damping = import_module("tad-dftd4_gb300.damping")
+    r = damping.resolve({"a1": 0.5, "a2": 4.0})
+    assert r["s6"] == 1.0 and not r["has_s8"] and not r["has_s10"]
+    assert r["s9"] == 1.0 and r["alp"] == 16.0
+    r = damping.resolve({"a1": torch.tensor(0.5), "a2": 4.0, "s8": 2.0, "s10": 0.0})
+    assert r["has_s8"] and r["s8"] == 2.0 and r["has_s10"]
+
+
+def test_cutoff_defaults(d4):
+    c = d4.Cutoff()
+    assert float(c.disp2) == 60.0 and float(c.disp3) == 40.0
+    assert float(c.cn) == 30.0 and float(c.cn_eeq) == 25.0
+
+
+def test_model_descriptors(d4):
+    z = torch.tensor([6, 1])
+    assert d4.D4Model(z).wf == 6.0
+    with pytest.raises(ValueError):
+        d4.D4Model(z, ref_charges="xyz")
+    with pytest.raises(NotImplementedError):
+        d4.D4SModel(z, wf=3.0)
