@@ -1011,6 +1011,7 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   const dim3 atoms((N + 7) / 8, B);
   const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
+  cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
   prep_kernel<<<B, 256, 0, st>>>(c);
   cn_kernel<<<atoms, 256, 0, st>>>(c);
   const size_t vec_bytes = (size_t)8 * ((N + 1) / 2 + 1 + 2 * N);
