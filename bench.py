@@ -1,0 +1,427 @@
+#!/usr/bin/env python
+"""
+Benchmark of the DFT-D4 dispersion path: energy + forces, structures/s.
+
+Workload (N = 1): ``batch512`` -- 512 structures, N ~ U[8, 200] atoms padded
+to 200, 12 elements (H 0.45, C 0.30, others 0.025), density 0.01 atoms/Bohr^3,
+total charges in {-1, 0, +1}, BJ parameters s6=1, s8=1.2, a1=0.4, a2=5,
+s9=1, float64, seed 1.  One step = energies and forces of the whole batch.
+
+Lines printed by rank 0 (one JSON line):
+
+* ``value``: structures/s with inputs resident in HBM (device-timed fused
+  energy + gradient call, L2 flushed between steps);
+* ``e2e``: the same metric through the public API ``dftd4()`` + autograd,
+  with pinned host inputs copied in and energies / forces copied out every
+  step;
+* ``roofline``: the dominant kernel (ATM), algorithmic flops per launch
+  divided by its CUDA-event duration in the timed steps, against the
+  FP64 / FP32 FMA peak measured in this run;
+* ``cpu_baseline``: the float64 CPU oracle on a bounded sample.
+
+``--impl reference`` times the CPU restatement of tad-dftd4 (the oracle) on
+the host cores for the same workload and metric.
+"""
+
+from __future__ import annotations
+
+import argparse
+import ctypes
+import importlib
+import json
+import os
+import subprocess
+import sys
+import threading
+import time
+from pathlib import Path
+
+import numpy as np
+
+REPO = Path(__file__).resolve().parent
+sys.path.insert(0, str(REPO))
+
+METRIC = "energy+force structures/s"
+UNIT = "structures/s"
+ATM_FLOPS_PER_TRIPLE = 180.0  # forward 60 + backward 120 (flop convention of the path)
+PAIR_FLOPS = 92.0 + 30.0
+
+
+def parse_args():
+    ap = argparse.ArgumentParser(description=__doc__.split("\n\n")[0])
+    ap.add_argument("--gpus", type=int, default=1)
+    ap.add_argument("--steps", type=int, default=20)
+    ap.add_argument("--warmup", type=int, default=3)
+    ap.add_argument("--impl", choices=("ours", "reference"), default="ours")
+    ap.add_argument("--nstruct", type=int, default=512)
+    ap.add_argument("--e2e-steps", type=int, default=None)
+    ap.add_argument("--cpu-seconds", type=float, default=15.0)
+    ap.add_argument("--no-cpu-baseline", action="store_true")
+    return ap.parse_args()
+
+
+def dist_setup(ngpus: int):
+    import torch
+
+    world = int(os.environ.get("WORLD_SIZE", "1"))
+    rank = int(os.environ.get("RANK", "0"))
+    local = int(os.environ.get("LOCAL_RANK", "0"))
+    if world > 1:
+        import torch.distributed as dist
+
+        backend = "nccl" if torch.cuda.is_available() else "gloo"
+        dist.init_process_group(backend=backend)
+    if torch.cuda.is_available():
+        torch.cuda.set_device(local)
+    return world, rank, local
+
+
+def barrier(world):
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.barrier()
+
+
+def max_over_ranks(x: float, world: int) -> float:
+    if world == 1:
+        return x
+    import torch
+    import torch.distributed as dist
+
+    t = torch.tensor([x], dtype=torch.float64,
+                     device="cuda" if torch.cuda.is_available() else "cpu")
+    dist.all_reduce(t, op=dist.ReduceOp.MAX)
+    return float(t.item())
+
+
+def structure_counts(numbers: np.ndarray, positions: np.ndarray, cut2: float, cut3: float):
+    """Unordered pairs within cut2 and triples with >= 2 sides within cut3."""
+    pairs = 0
+    triples = 0
+    for z, r in zip(numbers, positions):
+        real = z != 0
+        rr = r[real]
+        n = len(rr)
+        if n < 2:
+            continue
+        d = np.sqrt(((rr[:, None, :] - rr[None, :, :]) ** 2).sum(-1))
+        np.fill_diagonal(d, np.inf)
+        pairs += int((d <= cut2).sum()) // 2
+        m = (d <= cut3).astype(np.float64)
+        deg = m.sum(1)
+        tri = np.trace(m @ m @ m) / 6.0
+        triples += int(round((deg * (deg - 1) / 2).sum() - 2 * tri))
+    return pairs, triples
+
+
+class ClockSampler:
+    """nvidia-smi clock / throttle samples while the timed region runs."""
+
+    QUERY = ("index,clocks.sm,clocks.max.sm,power.draw,clocks_event_reasons.active,"
+             "clocks_event_reasons.hw_slowdown,clocks_event_reasons.hw_thermal_slowdown,"
+             "clocks_event_reasons.sw_thermal_slowdown,clocks_event_reasons.sw_power_cap")
+
+    def __init__(self, index: int):
+        self.index = index
+        self.proc = None
+        self.lines: list[str] = []
+
+    def __enter__(self):
+        try:
+            self.proc = subprocess.Popen(
+                ["nvidia-smi", f"--id={self.index}", f"--query-gpu={self.QUERY}",
+                 "--format=csv,noheader,nounits", "-lms", "100"],
+                stdout=subprocess.PIPE, stderr=subprocess.DEVNULL, text=True)
+            self.thread = threading.Thread(target=self._read, daemon=True)
+            self.thread.start()
+        except (FileNotFoundError, OSError):
+            self.proc = None
+        return self
+
+    def _read(self):
+        for line in self.proc.stdout:
+            self.lines.append(line.strip())
+
+    def __exit__(self, *exc):
+        if self.proc is not None:
+            self.proc.terminate()
+            try:
+                self.proc.wait(timeout=5)
+            except subprocess.TimeoutExpired:
+                self.proc.kill()
+
+    def summary(self):
+        sm, mx, reasons = [], None, set()
+        names = ["hw_slowdown", "hw_thermal_slowdown", "sw_thermal_slowdown", "sw_power_cap"]
+        for line in self.lines:
+            parts = [p.strip() for p in line.split(",")]
+            if len(parts) < 9:
+                continue
+            try:
+                sm.append(float(parts[1]))
+                mx = float(parts[2])
+            except ValueError:
+                continue
+            for name, flag in zip(names, parts[5:9]):
+                if flag.lower().startswith("active"):
+                    reasons.add(name)
+        return {"sm_mhz": float(np.median(sm)) if sm else None, "sm_max_mhz": mx,
+                "reasons": sorted(reasons), "samples": len(sm)}
+
+
+def cpu_oracle_rate(batch, param, seconds: float, threads: int):
+    """Structures/s of the float64 CPU oracle (energy + autograd forces)."""
+    import torch
+
+    import oracle
+
+    torch.set_num_threads(threads)
+    order = np.random.default_rng(0).permutation(len(batch.numbers))
+    done, t0, sizes = 0, time.perf_counter(), []
+    for k in order:
+        z = batch.numbers[k]
+        n = int((z != 0).sum())
+        nt = torch.from_numpy(z[:n])
+        pt = torch.from_numpy(batch.positions[k, :n])
+        oracle.dftd4_energy_and_grad(nt, pt, torch.tensor(float(batch.charge[k])), param)
+        done += 1
+        sizes.append(n)
+        if time.perf_counter() - t0 >= seconds and done >= 3:
+            break
+    dt = time.perf_counter() - t0
+    return done / dt, done, dt, sizes
+
+
+def oracle_errors(batch, param, energy: np.ndarray, grad: np.ndarray, count: int = 3):
+    """Max |dE| per structure and max |dF| against the oracle on a few structures."""
+    import torch
+
+    import oracle
+
+    sizes = (batch.numbers != 0).sum(-1)
+    order = np.argsort(sizes)
+    pick = sorted(set(order[: count - 1].tolist() + [int(order[-1])]))
+    de, df = 0.0, 0.0
+    for k in pick:
+        n = int(sizes[k])
+        nt = torch.from_numpy(batch.numbers[k, :n])
+        pt = torch.from_numpy(batch.positions[k, :n])
+        e_ref, g_ref = oracle.dftd4_energy_and_grad(nt, pt, torch.tensor(float(batch.charge[k])),
+                                                    param)
+        de = max(de, abs(float(energy[k, :n].sum() - e_ref.sum())))
+        df = max(df, float(np.abs(grad[k, :n] - g_ref.numpy()).max()))
+    return {"structures_checked": [int(k) for k in pick], "max_abs_dE_eh": de,
+            "max_abs_dF_eh_bohr": df}
+
+
+def run_reference(args, world, rank):
+    """--impl reference: the CPU restatement on the host cores."""
+    if rank != 0:
+        return
+    pkg = importlib.import_module("tad-dftd4_gb300")
+    batch = pkg.workloads.batch512(1, args.nstruct)
+    param = dict(pkg.workloads.BJ_PARAMS)
+    threads = os.cpu_count() or 1
+    per_step = max(1.0, args.cpu_seconds / max(1, args.steps))
+    for _ in range(args.warmup):
+        cpu_oracle_rate(batch, param, 0.0, threads)
+    rates, total_n, total_t = [], 0, 0.0
+    for _ in range(args.steps):
+        rate, n, dt, _ = cpu_oracle_rate(batch, param, per_step, threads)
+        rates.append(rate)
+        total_n += n
+        total_t += dt
+    value = total_n / total_t
+    line = {
+        "impl": "reference", "metric": METRIC, "value": value, "unit": UNIT,
+        "n_gpus": args.gpus, "steps": args.steps, "warmup": args.warmup,
+        "ms_per_step": 1e3 * total_t / args.steps, "higher_is_better": True,
+        "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+        "config": {"workload": "batch512: 512 structures, N~U[8,200] padded to 200, "
+                               "12 elements, density 0.01/Bohr^3, charges {-1,0,1}, seed 1",
+                   "model": "D4", "step": "bounded sample of the batch per step"},
+        "cpu_baseline": {"value": value, "unit": UNIT, "cores": threads, "kind": "port",
+                         "sample": f"{total_n} structures drawn from the batch, "
+                                   f"energy + autograd forces, torch float64 CPU"},
+        "e2e": {"value": value, "unit": UNIT, "h2d_bytes_per_step": 0,
+                "d2h_bytes_per_step": 0},
+    }
+    print(json.dumps(line), flush=True)
+
+
+def run_ours(args, world, rank, local):
+    import torch
+
+    pkg = importlib.import_module("tad-dftd4_gb300")
+    disp = importlib.import_module("tad-dftd4_gb300.disp")
+    lib = pkg._lib.load()
+    dev = torch.device("cuda", local)
+    batch = pkg.workloads.batch512(1, args.nstruct)
+    param = dict(pkg.workloads.BJ_PARAMS)
+    B, N = batch.numbers.shape
+    numbers = torch.from_numpy(batch.numbers).to(dev)
+    positions = torch.from_numpy(batch.positions).to(dev)
+    charge = torch.from_numpy(batch.charge).to(dev)
+    runner, _, _ = disp._prepare(numbers, positions, charge, param, "d4", None, None, None,
+                                 None, None, None, None, None)
+    flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
+    disp.CHECK_STATUS = False
+    for _ in range(args.warmup):
+        runner.run(positions, gradient=True)
+    torch.cuda.synchronize()
+
+    # ---- device-resident timed region
+    nstage = lib.d4_stage_count()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    barrier(world)
+    torch.cuda.synchronize()
+    with ClockSampler(local) as clocks:
+        pkg._lib.check(lib.d4_timing_begin(args.steps), "timing")
+        for k in range(args.steps):
+            flush.zero_()
+            starts[k].record()
+            runner.run(positions, gradient=True)
+            ends[k].record()
+        torch.cuda.synchronize()
+        ms_stage = (ctypes.c_float * nstage)()
+        ncalls = ctypes.c_int32(0)
+        pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
+    barrier(world)
+    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
+    total_s = max_over_ranks(sum(step_ms) / 1e3, world)
+    value = world * B * args.steps / total_s
+    stages = {lib.d4_stage_name(i).decode(): ms_stage[i] / max(1, ncalls.value)
+              for i in range(nstage)}
+
+    # error of the timed configuration against the float64 oracle
+    disp.CHECK_STATUS = True
+    e_dev, g_dev, _, _, _ = runner.run(positions, gradient=True)
+    err = oracle_errors(batch, param, e_dev.cpu().numpy(), g_dev.cpu().numpy())
+
+    # ---- end to end through the public API, host buffers
+    e2e_steps = args.e2e_steps or max(3, args.steps // 2)
+    h_num = torch.from_numpy(batch.numbers).pin_memory()
+    h_pos = torch.from_numpy(batch.positions).pin_memory()
+    h_chg = torch.from_numpy(batch.charge).pin_memory()
+    h_e = torch.empty((B, N), dtype=torch.float64).pin_memory()
+    h_g = torch.empty((B, N, 3), dtype=torch.float64).pin_memory()
+
+    def e2e_step():
+        d_num = h_num.to(dev, non_blocking=True)
+        d_pos = h_pos.to(dev, non_blocking=True).requires_grad_(True)
+        d_chg = h_chg.to(dev, non_blocking=True)
+        energy = pkg.dftd4(d_num, d_pos, d_chg, param)
+        (grad,) = torch.autograd.grad(energy.sum(), d_pos)
+        h_e.copy_(energy.detach(), non_blocking=True)
+        h_g.copy_(grad, non_blocking=True)
+        torch.cuda.synchronize()
+
+    for _ in range(2):
+        e2e_step()
+    lat = []
+    barrier(world)
+    for _ in range(e2e_steps):
+        flush.zero_()
+        torch.cuda.synchronize()
+        t0 = time.perf_counter()
+        e2e_step()
+        lat.append(time.perf_counter() - t0)
+    e2e_total = max_over_ranks(sum(lat), world)
+    e2e_value = world * B * e2e_steps / e2e_total
+    h2d = h_num.numel() * 8 + h_pos.numel() * 8 + h_chg.numel() * 8
+    d2h = h_e.numel() * 8 + h_g.numel() * 8
+
+    # ---- roofline of the dominant kernel
+    pairs, triples = structure_counts(batch.numbers, batch.positions, 60.0, 40.0)
+    sink = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
+    ms = ctypes.c_float(0.0)
+    best = 0.0
+    for _ in range(3):
+        pkg._lib.check(lib.d4_probe_fma(1, 152 * 8, 4096, sink.data_ptr(), ms,
+                                        torch.cuda.current_stream(dev).cuda_stream), "probe")
+        best = max(best, 152 * 8 * 256 * 4096 * 8 * 2 / (ms.value * 1e-3) / 1e12)
+    fp64_peak = best
+    top = max(stages, key=stages.get)
+    atm_ms = stages["atm"]
+    achieved = ATM_FLOPS_PER_TRIPLE * triples / (atm_ms * 1e-3) / 1e12
+    traffic = None
+    tfile = REPO / "profiles" / "traffic.txt"
+    if tfile.exists():
+        for line in tfile.read_text().splitlines():
+            parts = line.split()
+            if len(parts) >= 2 and parts[0] == "atm_fp64_batch512":
+                traffic = float(parts[1])
+    peaks = {}
+    pfile = REPO / "MEASURED_PEAKS.json"
+    if pfile.exists():
+        peaks = json.loads(pfile.read_text())
+
+    # ---- CPU baseline (rank 0, bounded sample)
+    cpu = None
+    if rank == 0 and world == 1 and not args.no_cpu_baseline:
+        threads = os.cpu_count() or 1
+        rate, n, dt, sizes = cpu_oracle_rate(batch, param, args.cpu_seconds, threads)
+        cpu = {"value": rate, "unit": UNIT, "cores": threads, "kind": "port",
+               "sample": f"{n} structures of the batch (mean N {np.mean(sizes):.0f}), "
+                         f"energy + autograd forces, float64 torch CPU oracle, {dt:.1f} s"}
+
+    clk = clocks.summary()
+    if rank == 0:
+        line = {
+            "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
+            "steps": args.steps, "warmup": args.warmup,
+            "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
+            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "config": {
+                "workload": "batch512: 512 structures, N~U[8,200] padded to 200, 12 elements, "
+                            "density 0.01/Bohr^3, charges {-1,0,1}, seed 1",
+                "model": "D4", "method": "plain FP64", "global_batch": B, "n_pad": N,
+                "params": param, "cutoffs": {"disp2": 60.0, "disp3": 40.0, "cn_eeq": 25.0},
+                "l2": "flushed between steps (256 MiB write); working set > L2",
+                "parallelism": f"replicas x{world}",
+            },
+            "atom_pairs_per_s": world * pairs * args.steps / total_s,
+            "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
+                           "p99": float(np.percentile(step_ms, 99))},
+            "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
+                    "d2h_bytes_per_step": d2h,
+                    "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
+                                   "p99": 1e3 * float(np.percentile(lat, 99))},
+                    "api": "dftd4() + torch.autograd.grad, pinned host buffers"},
+            "roofline": {
+                "kernel": "atm_kernel<GRAD> (FP64)", "bound": "fp64",
+                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp64_peak if fp64_peak else None,
+                "traffic": traffic,
+                "peak_source": "FP64 FMA-chain probe (d4_probe_fma) measured in this run; "
+                               "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
+                "algorithmic": f"{ATM_FLOPS_PER_TRIPLE:.0f} flop x {triples} triples per launch",
+                "avg_launch_ms": atm_ms,
+                "hbm_peak_gbs": peaks.get("hbm_gbs"),
+            },
+            "error_vs_fp64_oracle": err,
+            "stage_ms": stages, "top_stage": top,
+            "gpu_launches": 10 * args.steps,
+            "clocks": {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
+            "cpu_baseline": cpu,
+        }
+        print(json.dumps(line), flush=True)
+
+
+def main():
+    args = parse_args()
+    world, rank, local = dist_setup(args.gpus)
+    if args.impl == "reference":
+        run_reference(args, world, rank)
+    else:
+        run_ours(args, world, rank, local)
+    if world > 1:
+        import torch.distributed as dist
+
+        dist.destroy_process_group()
+
+
+if __name__ == "__main__":
+    main()

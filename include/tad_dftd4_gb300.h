@@ -185,6 +185,32 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
  */
 int d4_read_status(void *d_workspace, void *stream);
 
+/*
+ * Kernel timing.  Between d4_timing_begin and d4_timing_end, every
+ * d4_dispersion call on this host thread records a pair of CUDA events
+ * around each of its kernels, on the stream it launches them on (at most
+ * ``max_calls`` calls are recorded).  d4_timing_end waits for the last event
+ * and writes the summed milliseconds of each stage to ``ms_per_stage``
+ * (``n_stage`` entries, see d4_stage_name) and the number of recorded calls
+ * to ``n_calls``.
+ */
+int d4_timing_begin(int32_t max_calls);
+int d4_timing_end(float *ms_per_stage, int32_t n_stage, int32_t *n_calls);
+int32_t d4_stage_count(void);
+const char *d4_stage_name(int32_t stage);
+
+/*
+ * Arithmetic-throughput probe: ``n_blocks`` CTAs of 256 threads run
+ * ``iters`` dependent-chain FMA iterations on 8 independent accumulators in
+ * FP64 (``fp64`` != 0) or FP32 and write one value per thread to
+ * ``d_sink`` (n_blocks * 256 doubles).  The elapsed time of the launch (CUDA
+ * events) goes to ``ms_out``; the flop count is
+ * n_blocks * 256 * iters * 8 * 2.  Used to measure the FP32 / FP64 peak
+ * that bounds the pair and triple kernels.
+ */
+int d4_probe_fma(int32_t fp64, int32_t n_blocks, int32_t iters, double *d_sink,
+                 float *ms_out, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

@@ -129,6 +129,13 @@ SIGNATURES = {
          ctypes.POINTER(Outputs), c_void_p],
     ),
     "d4_read_status": (c_int, [c_void_p, c_void_p]),
+    "d4_timing_begin": (c_int, [c_int32]),
+    "d4_timing_end": (c_int, [ctypes.POINTER(ctypes.c_float), c_int32,
+                              ctypes.POINTER(c_int32)]),
+    "d4_stage_count": (c_int32, []),
+    "d4_stage_name": (c_char_p, [c_int32]),
+    "d4_probe_fma": (c_int, [c_int32, c_int32, c_int32, c_void_p,
+                             ctypes.POINTER(ctypes.c_float), c_void_p]),
 }
 
 _LIB: ctypes.CDLL | None = None

@@ -1011,11 +1011,17 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   const dim3 atoms((N + 7) / 8, B);
   const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
+  timing_next_call();
   cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
+  stage_begin(ST_PREP, st);
   prep_kernel<<<B, 256, 0, st>>>(c);
+  stage_end(ST_PREP, st);
+  stage_begin(ST_CN, st);
   cn_kernel<<<atoms, 256, 0, st>>>(c);
+  stage_end(ST_CN, st);
   const size_t vec_bytes = (size_t)8 * ((N + 1) / 2 + 1 + 2 * N);
   const size_t tri_bytes = (size_t)8 * ((size_t)N * (N + 1) / 2);
+  stage_begin(ST_EEQ, st);
   if (eeq) {
     if (vec_bytes + tri_bytes <= 220 * 1024) {
       cudaFuncSetAttribute(eeq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
@@ -1030,27 +1036,45 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
     const size_t total = (size_t)B * N;
     charges_in_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
   }
+  stage_end(ST_EEQ, st);
+  stage_begin(ST_WEIGHTS, st);
   weights_kernel<<<atoms, 256, 0, st>>>(c);
+  stage_end(ST_WEIGHTS, st);
+  stage_begin(ST_PAIR_FWD, st);
   pair_fwd_kernel<<<atoms, 256, 0, st>>>(c);
+  stage_end(ST_PAIR_FWD, st);
   const dim3 tiles(((N + 7) / 8) * ((N + 31) / 32), B);
+  stage_begin(ST_ATM, st);
   if (grad) {
     if (c.flags & D4_FLAG_PARAM_GRAD)
       atm_kernel<true, true><<<tiles, 256, 0, st>>>(c);
     else
       atm_kernel<true, false><<<tiles, 256, 0, st>>>(c);
-    pair_atm_bwd_kernel<<<atoms, 256, 0, st>>>(c);
-    if (eeq) {
-      cudaFuncSetAttribute(eeq_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)vec_bytes);
-      eeq_adjoint_kernel<<<B, 256, vec_bytes, st>>>(c);
-    }
-    pair_cn_bwd_kernel<<<atoms, 256, 0, st>>>(c);
   } else {
     atm_kernel<false, false><<<tiles, 256, 0, st>>>(c);
   }
+  stage_end(ST_ATM, st);
+  if (grad) {
+    stage_begin(ST_PAIR_ATM_BWD, st);
+    pair_atm_bwd_kernel<<<atoms, 256, 0, st>>>(c);
+    stage_end(ST_PAIR_ATM_BWD, st);
+    if (eeq) {
+      stage_begin(ST_EEQ_ADJ, st);
+      cudaFuncSetAttribute(eeq_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)vec_bytes);
+      eeq_adjoint_kernel<<<B, 256, vec_bytes, st>>>(c);
+      stage_end(ST_EEQ_ADJ, st);
+    }
+    stage_begin(ST_PAIR_CN_BWD, st);
+    pair_cn_bwd_kernel<<<atoms, 256, 0, st>>>(c);
+    stage_end(ST_PAIR_CN_BWD, st);
+  }
+  stage_begin(ST_FINISH, st);
   const size_t total = (size_t)B * N;
   finish_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
-  if (c.flags & D4_FLAG_PARAM_GRAD) param_grad_finish_kernel<<<(8 * B + 255) / 256, 256, 0, st>>>(c);
+  if (c.flags & D4_FLAG_PARAM_GRAD)
+    param_grad_finish_kernel<<<(8 * B + 255) / 256, 256, 0, st>>>(c);
+  stage_end(ST_FINISH, st);
   return 0;
 }
 

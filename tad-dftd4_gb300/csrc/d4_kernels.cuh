@@ -5,6 +5,25 @@
 
 namespace d4 {
 
+enum Stage {
+  ST_PREP = 0,
+  ST_CN,
+  ST_EEQ,
+  ST_WEIGHTS,
+  ST_PAIR_FWD,
+  ST_ATM,
+  ST_PAIR_ATM_BWD,
+  ST_EEQ_ADJ,
+  ST_PAIR_CN_BWD,
+  ST_FINISH,
+  ST_COUNT
+};
+
+// Stage timing hooks (no-ops unless d4_timing_begin was called).
+void stage_begin(int stage, cudaStream_t st);
+void stage_end(int stage, cudaStream_t st);
+void timing_next_call();
+
 int launch_fp64(const Ctx &c, cudaStream_t st);
 int launch_prepare_alpha(const d4_tables_t &tab, const d4_model_cfg_t &cfg,
                          const double *refalpha, const double *refascale,
