@@ -211,6 +211,42 @@ const char *d4_stage_name(int32_t stage);
 int d4_probe_fma(int32_t fp64, int32_t n_blocks, int32_t iters, double *d_sink,
                  float *ms_out, void *stream);
 
+/*
+ * Allocation-free variant of d4_dispersion.  This entry point has no
+ * counterpart in the reference (tad-dftd4 allocates tensors on every call).
+ *
+ * It is meant for callers that cannot call cudaMalloc: code running where
+ * device allocation is forbidden or unsafe, such as inside a host callback
+ * or a real-time loop with a fixed memory budget, a plugin that must not
+ * touch its host application's allocator, or a process whose memory pool is
+ * managed by someone else.  Instead of a caller-provided workspace it uses
+ * one file-scope device array of D4_NOALLOC_SCRATCH_BYTES (32 MiB) that is
+ * part of the library image: every GPU that loads the library holds it until
+ * the process exits.  The caller still provides all inputs and outputs.
+ *
+ * Limits and rules:
+ *  - the problem must fit: d4_workspace_size(B, N, n_slots, flags) must not
+ *    exceed D4_NOALLOC_SCRATCH_BYTES (with gradients that is, e.g., 12
+ *    structures of 200 atoms or one structure of about 700 atoms); larger
+ *    problems are rejected with D4_ERR_WORKSPACE before any work is queued;
+ *  - all calls share the one array, and it keeps the last call's contents
+ *    (everything a call needs zeroed it clears itself): calls whose work
+ *    overlaps on the GPU -- different streams without ordering, or
+ *    different host threads on one device -- race and corrupt each other;
+ *  - the first call on each device looks up the array's device address
+ *    (cudaGetSymbolAddress) with that device current; make that first call
+ *    before any stream capture starts;
+ *  - with ``check_status`` != 0 the call waits for ``stream`` and returns the
+ *    device status (as d4_read_status would); otherwise it returns without
+ *    waiting and device-side input errors are not reported.
+ * No cudaMalloc, cudaFree or allocating library routine is called.
+ */
+#define D4_NOALLOC_SCRATCH_BYTES (32u * 1024u * 1024u)
+int d4_dispersion_noalloc(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                          const d4_batch_t *batch, const d4_params_t *params,
+                          uint32_t flags, int32_t n_slots, const d4_outputs_t *out,
+                          int32_t check_status, void *stream);
+
 #ifdef __cplusplus
 }
 #endif

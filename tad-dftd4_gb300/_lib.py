@@ -136,6 +136,12 @@ SIGNATURES = {
     "d4_stage_name": (c_char_p, [c_int32]),
     "d4_probe_fma": (c_int, [c_int32, c_int32, c_int32, c_void_p,
                              ctypes.POINTER(ctypes.c_float), c_void_p]),
+    "d4_dispersion_noalloc": (
+        c_int,
+        [ctypes.POINTER(Tables), ctypes.POINTER(ModelCfg), ctypes.POINTER(Batch),
+         ctypes.POINTER(Params), c_uint32, c_int32, ctypes.POINTER(Outputs), c_int32,
+         c_void_p],
+    ),
 }
 
 _LIB: ctypes.CDLL | None = None
