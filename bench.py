@@ -9,14 +9,16 @@ s9=1, float64, seed 1.  One step = energies and forces of the whole batch.
 
 Lines printed by rank 0 (one JSON line):
 
-* ``value``: structures/s with inputs resident in HBM (device-timed fused
-  energy + gradient call, L2 flushed between steps);
+* ``value``: structures/s of the precision form with inputs resident in HBM
+  (device-timed fused energy + gradient call, L2 flushed between steps);
+  the plain FP64 kernels are timed on the same workload beside it
+  (``plain_fp64``), and both are compared with the float64 oracle;
 * ``e2e``: the same metric through the public API ``dftd4()`` + autograd,
   with pinned host inputs copied in and energies / forces copied out every
   step;
 * ``roofline``: the dominant kernel (ATM), algorithmic flops per launch
-  divided by its CUDA-event duration in the timed steps, against the
-  FP64 / FP32 FMA peak measured in this run;
+  divided by its CUDA-event duration in the timed steps, against the FP32
+  FMA peak measured in this run;
 * ``cpu_baseline``: the float64 CPU oracle on a bounded sample.
 
 ``--impl reference`` times the CPU restatement of tad-dftd4 (the oracle) on
@@ -250,6 +252,46 @@ def run_reference(args, world, rank):
     print(json.dumps(line), flush=True)
 
 
+def time_steps(lib, pkg, runner, positions, steps, flush, timing: bool):
+    """Per-step CUDA-event times of the fused energy + gradient call."""
+    import torch
+
+    nstage = lib.d4_stage_count()
+    starts = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    ends = [torch.cuda.Event(enable_timing=True) for _ in range(steps)]
+    if timing:
+        pkg._lib.check(lib.d4_timing_begin(steps), "timing")
+    for k in range(steps):
+        flush.zero_()
+        starts[k].record()
+        runner.run(positions, gradient=True)
+        ends[k].record()
+    torch.cuda.synchronize()
+    stages = None
+    if timing:
+        ms_stage = (ctypes.c_float * nstage)()
+        ncalls = ctypes.c_int32(0)
+        pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
+        stages = {lib.d4_stage_name(i).decode(): ms_stage[i] / max(1, ncalls.value)
+                  for i in range(nstage)}
+    return [s.elapsed_time(e) for s, e in zip(starts, ends)], stages
+
+
+def probe_peak(lib, pkg, dev, fp64: bool) -> float:
+    """Best of three FMA-chain probes, TFLOP/s."""
+    import torch
+
+    blocks, iters = 152 * 8, (4096 if fp64 else 65536)
+    sink = torch.empty(blocks * 256, dtype=torch.float64, device=dev)
+    ms = ctypes.c_float(0.0)
+    best = 0.0
+    for _ in range(3):
+        pkg._lib.check(lib.d4_probe_fma(int(fp64), blocks, iters, sink.data_ptr(), ms,
+                                        torch.cuda.current_stream(dev).cuda_stream), "probe")
+        best = max(best, blocks * 256 * iters * 8 * 2 / (ms.value * 1e-3) / 1e12)
+    return best
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -263,42 +305,44 @@ def run_ours(args, world, rank, local):
     numbers = torch.from_numpy(batch.numbers).to(dev)
     positions = torch.from_numpy(batch.positions).to(dev)
     charge = torch.from_numpy(batch.charge).to(dev)
-    runner, _, _ = disp._prepare(numbers, positions, charge, param, "d4", None, None, None,
-                                 None, None, None, None, None)
+
+    def make_runner(precision):
+        r, _, _ = disp._prepare(numbers, positions, charge, param, "d4", None, None, None,
+                                None, None, None, None, None, precision)
+        return r
+
+    mixed = make_runner("mixed")
+    plain = make_runner("fp64")
     flush = torch.empty(256 * 1024 * 1024, dtype=torch.uint8, device=dev)
     disp.CHECK_STATUS = False
     for _ in range(args.warmup):
-        runner.run(positions, gradient=True)
+        mixed.run(positions, gradient=True)
+        plain.run(positions, gradient=True)
     torch.cuda.synchronize()
 
-    # ---- device-resident timed region
-    nstage = lib.d4_stage_count()
-    starts = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
-    ends = [torch.cuda.Event(enable_timing=True) for _ in range(args.steps)]
+    # ---- device-resident timed region: the precision form (headline)
     barrier(world)
     torch.cuda.synchronize()
     with ClockSampler(local) as clocks:
-        pkg._lib.check(lib.d4_timing_begin(args.steps), "timing")
-        for k in range(args.steps):
-            flush.zero_()
-            starts[k].record()
-            runner.run(positions, gradient=True)
-            ends[k].record()
-        torch.cuda.synchronize()
-        ms_stage = (ctypes.c_float * nstage)()
-        ncalls = ctypes.c_int32(0)
-        pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
+        step_ms, stages = time_steps(lib, pkg, mixed, positions, args.steps, flush, True)
     barrier(world)
-    step_ms = [s.elapsed_time(e) for s, e in zip(starts, ends)]
     total_s = max_over_ranks(sum(step_ms) / 1e3, world)
     value = world * B * args.steps / total_s
-    stages = {lib.d4_stage_name(i).decode(): ms_stage[i] / max(1, ncalls.value)
-              for i in range(nstage)}
 
-    # error of the timed configuration against the float64 oracle
+    # ---- the plain FP64 kernels on the same workload (comparison point)
+    plain_steps = max(3, min(args.steps, 10))
+    plain_ms, plain_stages = time_steps(lib, pkg, plain, positions, plain_steps, flush, True)
+    plain_total = max_over_ranks(sum(plain_ms) / 1e3, world)
+    plain_value = world * B * plain_steps / plain_total
+
+    # ---- error of both forms against the float64 oracle
     disp.CHECK_STATUS = True
-    e_dev, g_dev, _, _, _ = runner.run(positions, gradient=True)
-    err = oracle_errors(batch, param, e_dev.cpu().numpy(), g_dev.cpu().numpy())
+    e_m, g_m, _, _, _ = mixed.run(positions, gradient=True)
+    e_p, g_p, _, _, _ = plain.run(positions, gradient=True)
+    err_m = oracle_errors(batch, param, e_m.cpu().numpy(), g_m.cpu().numpy())
+    err_p = oracle_errors(batch, param, e_p.cpu().numpy(), g_p.cpu().numpy())
+    e_all = (e_m.sum(-1) - e_p.sum(-1)).abs().max().item()
+    f_all = (g_m - g_p).abs().max().item()
 
     # ---- end to end through the public API, host buffers
     e2e_steps = args.e2e_steps or max(3, args.steps // 2)
@@ -312,7 +356,7 @@ def run_ours(args, world, rank, local):
         d_num = h_num.to(dev, non_blocking=True)
         d_pos = h_pos.to(dev, non_blocking=True).requires_grad_(True)
         d_chg = h_chg.to(dev, non_blocking=True)
-        energy = pkg.dftd4(d_num, d_pos, d_chg, param)
+        energy = pkg.dftd4(d_num, d_pos, d_chg, param, precision="mixed")
         (grad,) = torch.autograd.grad(energy.sum(), d_pos)
         h_e.copy_(energy.detach(), non_blocking=True)
         h_g.copy_(grad, non_blocking=True)
@@ -333,26 +377,21 @@ def run_ours(args, world, rank, local):
     h2d = h_num.numel() * 8 + h_pos.numel() * 8 + h_chg.numel() * 8
     d2h = h_e.numel() * 8 + h_g.numel() * 8
 
-    # ---- roofline of the dominant kernel
+    # ---- roofline of the dominant kernel (ATM, FP32 arithmetic)
     pairs, triples = structure_counts(batch.numbers, batch.positions, 60.0, 40.0)
-    sink = torch.empty(152 * 8 * 256, dtype=torch.float64, device=dev)
-    ms = ctypes.c_float(0.0)
-    best = 0.0
-    for _ in range(3):
-        pkg._lib.check(lib.d4_probe_fma(1, 152 * 8, 4096, sink.data_ptr(), ms,
-                                        torch.cuda.current_stream(dev).cuda_stream), "probe")
-        best = max(best, 152 * 8 * 256 * 4096 * 8 * 2 / (ms.value * 1e-3) / 1e12)
-    fp64_peak = best
+    fp32_peak = probe_peak(lib, pkg, dev, fp64=False)
+    fp64_peak = probe_peak(lib, pkg, dev, fp64=True)
     top = max(stages, key=stages.get)
     atm_ms = stages["atm"]
     achieved = ATM_FLOPS_PER_TRIPLE * triples / (atm_ms * 1e-3) / 1e12
-    traffic = None
+    plain_achieved = ATM_FLOPS_PER_TRIPLE * triples / (plain_stages["atm"] * 1e-3) / 1e12
+    traffic = {}
     tfile = REPO / "profiles" / "traffic.txt"
     if tfile.exists():
         for line in tfile.read_text().splitlines():
             parts = line.split()
-            if len(parts) >= 2 and parts[0] == "atm_fp64_batch512":
-                traffic = float(parts[1])
+            if len(parts) >= 2 and not line.startswith("#"):
+                traffic[parts[0]] = float(parts[1])
     peaks = {}
     pfile = REPO / "MEASURED_PEAKS.json"
     if pfile.exists():
@@ -373,37 +412,47 @@ def run_ours(args, world, rank, local):
             "metric": METRIC, "value": value, "unit": UNIT, "n_gpus": world,
             "steps": args.steps, "warmup": args.warmup,
             "ms_per_step": total_s * 1e3 / args.steps, "higher_is_better": True,
-            "scaling": "weak", "vs_baseline": None, "dtype": "f64", "data": "synthetic",
+            "scaling": "weak", "vs_baseline": None, "dtype": "f32+f64", "data": "synthetic",
             "config": {
                 "workload": "batch512: 512 structures, N~U[8,200] padded to 200, 12 elements, "
                             "density 0.01/Bohr^3, charges {-1,0,1}, seed 1",
-                "model": "D4", "method": "plain FP64", "global_batch": B, "n_pad": N,
+                "model": "D4", "method": "precision form (FP32 pair/triple maths, "
+                                         "compensated sums, FP32 EEQ + FP64 refinement)",
+                "global_batch": B, "n_pad": N,
                 "params": param, "cutoffs": {"disp2": 60.0, "disp3": 40.0, "cn_eeq": 25.0},
-                "l2": "flushed between steps (256 MiB write); working set > L2",
+                "l2": "flushed between steps (256 MiB write)",
                 "parallelism": f"replicas x{world}",
             },
             "atom_pairs_per_s": world * pairs * args.steps / total_s,
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
                            "p99": float(np.percentile(step_ms, 99))},
+            "plain_fp64": {"value": plain_value, "unit": UNIT,
+                           "ms_per_step": plain_total * 1e3 / plain_steps,
+                           "speedup_of_precision_form": value / plain_value,
+                           "stage_ms": plain_stages,
+                           "atm_achieved_tflops": plain_achieved, "fp64_peak_tflops": fp64_peak},
+            "error_vs_fp64_oracle": err_m,
+            "error_plain_fp64_vs_oracle": err_p,
+            "error_precision_vs_plain_all_structures": {"max_abs_dE_eh": e_all,
+                                                        "max_abs_dF_eh_bohr": f_all},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
                                    "p99": 1e3 * float(np.percentile(lat, 99))},
-                    "api": "dftd4() + torch.autograd.grad, pinned host buffers"},
+                    "api": "dftd4(precision='mixed') + torch.autograd.grad, pinned host buffers"},
             "roofline": {
-                "kernel": "atm_kernel<GRAD> (FP64)", "bound": "fp64",
-                "achieved": achieved, "peak": fp64_peak, "unit": "TFLOP/s",
-                "frac": achieved / fp64_peak if fp64_peak else None,
-                "traffic": traffic,
-                "peak_source": "FP64 FMA-chain probe (d4_probe_fma) measured in this run; "
+                "kernel": "atm_mixed_kernel<SMEM,GRAD> (FP32 arithmetic)", "bound": "fp32",
+                "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
+                "frac": achieved / fp32_peak if fp32_peak else None,
+                "traffic": traffic.get("atm_mixed_batch512"),
+                "peak_source": "FP32 FMA-chain probe (d4_probe_fma) measured in this run; "
                                "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
                 "algorithmic": f"{ATM_FLOPS_PER_TRIPLE:.0f} flop x {triples} triples per launch",
                 "avg_launch_ms": atm_ms,
                 "hbm_peak_gbs": peaks.get("hbm_gbs"),
             },
-            "error_vs_fp64_oracle": err,
             "stage_ms": stages, "top_stage": top,
-            "gpu_launches": 10 * args.steps,
+            "gpu_launches": 11 * args.steps,
             "clocks": {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
             "cpu_baseline": cpu,
         }

@@ -80,7 +80,6 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   if (cfg->kind != D4_MODEL_D4 && cfg->kind != D4_MODEL_D4S) return D4_ERR_ARGUMENT;
   if (cfg->kind == D4_MODEL_D4S && !tables->wfpair) return D4_ERR_ARGUMENT;
   if (cfg->kind == D4_MODEL_D4 && n_slots != 1) return D4_ERR_ARGUMENT;
-  if (flags & D4_FLAG_MIXED) return D4_ERR_ARGUMENT;  // precision form: separate library path
   d4::Workspace w = d4::carve_workspace(d_workspace, batch->n_struct, batch->n_pad, n_slots,
                                         flags);
   if (workspace_bytes < w.bytes) return D4_ERR_WORKSPACE;
@@ -101,7 +100,10 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   c.w = w;
   c.out = *out;
   cudaStream_t st = static_cast<cudaStream_t>(stream);
-  d4::launch_fp64(c, st);
+  if (flags & D4_FLAG_MIXED)
+    d4::launch_mixed(c, st);
+  else
+    d4::launch_fp64(c, st);
   return check_cuda(cudaGetLastError());
 }
 

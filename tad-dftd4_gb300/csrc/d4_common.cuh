@@ -51,7 +51,15 @@ struct Workspace {
   double *pr_P;     // [B*N*N] sum of weighted triple energies (atomics)
   double *pr_da1;   // [B*N*N] d log R0 / d a1 (parameter gradients only)
   double *pr_da2;   // [B*N*N] d log R0 / d a2 (parameter gradients only)
-  double *eeq_L;    // [B*N*(N+1)/2] packed Cholesky factor
+  double *eeq_L;    // [B*N*(N+1)/2] packed Cholesky factor (FP64 method) or
+                    // packed FP64 EEQ matrix (precision form)
+  // precision form only
+  float4 *pos32;    // [B*N] positions in FP32 (x, y, z, sqrt(r4r2))
+  float *A32;       // [B*N*S*23]
+  float *A032;      // [B*N*S*23]
+  float4 *ptf;      // [B*N*N] (r, 1/r, log(R0/r), sqrt(C6(q=0)))
+  float2 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2)
+  float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor
   size_t bytes;
 };
 
@@ -97,16 +105,25 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.dA0_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
   w.G = grad ? (double *)take(8 * BNS23) : nullptr;
   w.G0 = grad ? (double *)take(8 * BNS23) : nullptr;
-  w.pr_r = (double *)take(8 * BNN);
-  w.pr_ir = (double *)take(8 * BNN);
-  w.pr_L = (double *)take(8 * BNN);
-  w.pr_c = (double *)take(8 * BNN);
+  const bool mixed = (flags & D4_FLAG_MIXED) != 0;
+  w.pr_r = mixed ? nullptr : (double *)take(8 * BNN);
+  w.pr_ir = mixed ? nullptr : (double *)take(8 * BNN);
+  w.pr_L = mixed ? nullptr : (double *)take(8 * BNN);
+  w.pr_c = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_S = grad ? (double *)take(8 * BNN) : nullptr;
   w.pr_P = grad ? (double *)take(8 * BNN) : nullptr;
   const bool pgrad = (flags & D4_FLAG_PARAM_GRAD) != 0;
-  w.pr_da1 = pgrad ? (double *)take(8 * BNN) : nullptr;
-  w.pr_da2 = pgrad ? (double *)take(8 * BNN) : nullptr;
+  w.pr_da1 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
+  w.pr_da2 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
   w.eeq_L = (double *)take(8 * (size_t)B * ((size_t)N * (N + 1) / 2));
+  if (mixed) {
+    w.pos32 = (float4 *)take(16 * BN);
+    w.A32 = (float *)take(4 * BNS23);
+    w.A032 = (float *)take(4 * BNS23);
+    w.ptf = (float4 *)take(16 * BNN);
+    w.ptf_da = pgrad ? (float2 *)take(8 * BNN) : nullptr;
+    w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
+  }
   w.bytes = align_up(off, 256);
   return w;
 }
@@ -184,6 +201,42 @@ __device__ __forceinline__ void zeta_and_deriv(double gam, double qref, double q
 
 __host__ __device__ inline size_t tri_index(int i, int j) {  // packed lower, j <= i
   return (size_t)i * (i + 1) / 2 + j;
+}
+
+__device__ __forceinline__ float warp_sumf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+// Compensated FP32 accumulator (Knuth two-sum): value = hi + lo.
+struct Acc32 {
+  float hi = 0.0f, lo = 0.0f;
+  __device__ __forceinline__ void add(float x) {
+    const float t = hi + x;
+    const float bp = t - hi;
+    lo += (hi - (t - bp)) + (x - bp);
+    hi = t;
+  }
+  __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
+};
+
+// Real atoms of structure b compacted into s_idx[0..m).  Returns m.
+__device__ inline int compact_real_atoms(const Ctx &c, int b, int n, int *s_idx, int *s_tmp) {
+  // serial prefix by warp 0 is enough for n <= a few thousand
+  if (threadIdx.x < 32) {
+    int base = 0;
+    for (int i0 = 0; i0 < n; i0 += 32) {
+      const int i = i0 + threadIdx.x;
+      const bool real = i < n && c.w.z[(size_t)b * c.N + i] != 0;
+      const unsigned mask = __ballot_sync(0xffffffffu, real);
+      if (real) s_idx[base + __popc(mask & ((1u << threadIdx.x) - 1u))] = i;
+      base += __popc(mask);
+    }
+    if (threadIdx.x == 0) *s_tmp = base;
+  }
+  __syncthreads();
+  return *s_tmp;
 }
 
 }  // namespace d4

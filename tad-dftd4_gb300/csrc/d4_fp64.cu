@@ -115,6 +115,9 @@ __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
     const double dx = xi - P[3 * j], dy = yi - P[3 * j + 1], dz = zi3 - P[3 * j + 2];
     const double r = sqrt(dx * dx + dy * dy + dz * dz);
     const double r0 = rci + c.tab.cov_d3[zj];
+    // 1/2 (1 + erf(-x)) is exactly 0.0 in FP64 for x > 6; skip those pairs
+    // (bitwise the same sums) after a cheap FP32 test.
+    if (c.par.kcn * ((float)r / (float)r0 - 1.0f) > 7.0f) continue;
     const double cf = erf_count(r, r0, c.par.kcn);
     if (r <= c.par.cut_cn) s_d4 += en_factor(eni, c.tab.en[zj], c.par.k4, c.par.k5, c.par.k6) * cf;
     if (r <= c.par.cut_cn_eeq) s_q += cf;
@@ -131,24 +134,6 @@ __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
 }
 
 // ---------------------------------------------------------------- EEQ
-
-// Real atoms of structure b compacted into s_idx[0..m).  Returns m.
-__device__ int compact_real_atoms(const Ctx &c, int b, int n, int *s_idx, int *s_tmp) {
-  // serial prefix by warp 0 is enough for n <= a few thousand
-  if (threadIdx.x < 32) {
-    int base = 0;
-    for (int i0 = 0; i0 < n; i0 += 32) {
-      const int i = i0 + threadIdx.x;
-      const bool real = i < n && c.w.z[(size_t)b * c.N + i] != 0;
-      const unsigned mask = __ballot_sync(0xffffffffu, real);
-      if (real) s_idx[base + __popc(mask & ((1u << threadIdx.x) - 1u))] = i;
-      base += __popc(mask);
-    }
-    if (threadIdx.x == 0) *s_tmp = base;
-  }
-  __syncthreads();
-  return *s_tmp;
-}
 
 // Row-oriented triangular solves with one warp.  L is packed lower.
 // forward: L z = v (in place); backward: L^T x = z (in place).
@@ -356,127 +341,134 @@ __global__ void __launch_bounds__(256) eeq_adjoint_kernel(Ctx c) {
 
 // ---------------------------------------------------------------- weights
 
+constexpr int WU = 4;  // (atom, slot) units per warp of weights_kernel
+
 // Charge-scaled Gaussian weights of every reference and the weighted
 // polarisabilities A_i(w) = sum_r gw_ir alpha_{Z_i r}(w), at the charges q
-// and at q = 0, with their derivatives.  One warp per (atom, slot): lanes
-// 0..6 hold the references, lanes 0..22 the frequencies.
+// and at q = 0, with their derivatives.  A warp handles four units (atom,
+// D4S slot): in phase 1 lane 8u + r computes reference r of unit u (lanes
+// 8u + 7 idle), in phase 2 the lanes cover the 4 x 23 (unit, frequency)
+// outputs, reading the per-reference values from shared memory.
 __global__ void __launch_bounds__(256) weights_kernel(Ctx c) {
   const int b = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
-  const int i = blockIdx.x * 8 + warp;
   const int N = c.N;
-  if (i >= N) return;
-  const size_t ai = (size_t)b * N + i;
-  const int zi = c.w.z[ai];
-  const int n = c.w.n_eff[b];
-  const int nslot = c.w.n_slots[b];
+  const int S = c.S;
+  __shared__ double s_w[8][WU][5][NREF];
+  const int u = lane >> 3, r = lane & 7;
+  const int unit = (blockIdx.x * 8 + warp) * WU + u;  // = atom * S + slot
+  const int i = unit / S, s = unit % S;
   const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
   const bool d4s = c.cfg.kind == D4_MODEL_D4S;
-  for (int s = 0; s < c.S; ++s) {
-    const size_t o = (ai * c.S + s) * NFREQ;
-    if (i >= n || zi == 0 || s >= nslot) {
-      if (lane < NFREQ) {
-        c.w.A[o + lane] = 0.0;
-        c.w.A0[o + lane] = 0.0;
-        if (grad) {
-          c.w.dA_dcn[o + lane] = 0.0;
-          c.w.dA_dq[o + lane] = 0.0;
-          c.w.dA0_dcn[o + lane] = 0.0;
-        }
-      }
-      continue;
-    }
+  const int n = c.w.n_eff[b];
+  const int nslot = c.w.n_slots[b];
+  const size_t ai = (size_t)b * N + (i < N ? i : 0);
+  const int zi = (i < N) ? c.w.z[ai] : 0;
+  const bool live = i < N && i < n && zi != 0 && s < nslot;
+  // ---- phase 1: references
+  double e = 0.0, de = 0.0, refcn = -1e300;
+  int refc = 0;
+  double z = 0.0, dz = 0.0, z0 = 0.0;
+  if (live && r < NREF) {
     const double cn = c.w.cn[ai];
-    const double q = c.w.q[ai];
     const double wf = d4s ? c.tab.wfpair[zi * c.tab.n_elem + c.w.slot_elem[b * MAX_ELEM_ID + s]]
                           : c.cfg.wf;
-    // per reference (lanes 0..6)
-    double e = 0.0, de = 0.0, refcn = -1e300;
-    int refc = 0;
-    if (lane < NREF) {
-      refc = (int)c.tab.refc[zi * NREF + lane];
-      refcn = c.tab.refcovcn[zi * NREF + lane];
-      const double dcn = cn - refcn;
-      if (refc > 0) {
-        if (!d4s) {  // model/d4.py:177-194
-          const double tmp = exp(-dcn * dcn);
-          if (refc == 1) {
-            const double p1 = pow(tmp, wf);
-            e = p1;
-            de = -2.0 * wf * dcn * p1;
-          } else if (refc == 3) {
-            const double p1 = pow(tmp, wf), p2 = pow(tmp, 2.0 * wf), p3 = pow(tmp, 3.0 * wf);
-            e = p1 + p2 + p3;
-            de = -2.0 * wf * dcn * (p1 + 2.0 * p2 + 3.0 * p3);
-          } else {
-            e = tmp;
-            de = -2.0 * dcn * tmp;
-          }
-        } else {  // model/d4s.py:191-213
-          const double tmp = exp(-dcn * dcn * wf);
-          const double dtmp = -2.0 * wf * dcn * tmp;
-          if (refc == 3) {
-            const double t2 = pow(tmp, 2.0), t3 = pow(tmp, 3.0);
-            e = tmp + t2 + t3;
-            de = dtmp * (1.0 + 2.0 * tmp + 3.0 * t2);
-          } else {
-            e = tmp;
-            de = dtmp;
-          }
+    refc = (int)c.tab.refc[zi * NREF + r];
+    refcn = c.tab.refcovcn[zi * NREF + r];
+    const double dcn = cn - refcn;
+    if (refc > 0) {
+      if (!d4s) {  // model/d4.py:177-194
+        const double tmp = exp(-dcn * dcn);
+        if (refc == 1) {
+          const double p1 = pow(tmp, wf);
+          e = p1;
+          de = -2.0 * wf * dcn * p1;
+        } else if (refc == 3) {
+          const double p1 = pow(tmp, wf), p2 = pow(tmp, 2.0 * wf), p3 = pow(tmp, 3.0 * wf);
+          e = p1 + p2 + p3;
+          de = -2.0 * wf * dcn * (p1 + 2.0 * p2 + 3.0 * p3);
+        } else {
+          e = tmp;
+          de = -2.0 * dcn * tmp;
+        }
+      } else {  // model/d4s.py:191-213
+        const double tmp = exp(-dcn * dcn * wf);
+        const double dtmp = -2.0 * wf * dcn * tmp;
+        if (refc == 3) {
+          const double t2 = pow(tmp, 2.0), t3 = pow(tmp, 3.0);
+          e = tmp + t2 + t3;
+          de = dtmp * (1.0 + 2.0 * tmp + 3.0 * t2);
+        } else {
+          e = tmp;
+          de = dtmp;
         }
       }
+      const double zeff = (double)c.tab.zeff[zi];
+      const double gam = c.tab.gam[zi] * c.cfg.gc;
+      const double qref = c.tab.refq[zi * NREF + r] + zeff;
+      double dz0;
+      zeta_and_deriv(gam, qref, c.w.q[ai] + zeff, c.cfg.ga, DBL_EPSILON, &z, &dz);
+      zeta_and_deriv(gam, qref, 0.0 + zeff, c.cfg.ga, DBL_EPSILON, &z0, &dz0);
     }
-    double maxcn = refcn;
+  }
+  // sums over the 8-lane group of this unit
+  double norm = e, dnorm = de, maxcn = refcn;
 #pragma unroll
-    for (int o2 = 16; o2 > 0; o2 >>= 1) maxcn = fmax(maxcn, __shfl_xor_sync(0xffffffffu, maxcn, o2));
-    const double norm = warp_sum(e);
-    const double dnorm = warp_sum(de);
+  for (int o = 1; o < 8; o <<= 1) {
+    norm += __shfl_xor_sync(0xffffffffu, norm, o);
+    dnorm += __shfl_xor_sync(0xffffffffu, dnorm, o);
+    maxcn = fmax(maxcn, __shfl_xor_sync(0xffffffffu, maxcn, o));
+  }
+  if (r < NREF) {
     double gq = 0.0, g0 = 0.0, dgq_dcn = 0.0, dgq_dq = 0.0, dg0_dcn = 0.0;
-    if (lane < NREF && refc > 0) {
+    if (live && refc > 0) {
       double gw = e / norm;
       double dgw = (de - gw * dnorm) / norm;
       if (isnan(gw) || gw > DBL_MAX) {  // utils.py:208-224, model/d4.py:209-217
         gw = (refcn == maxcn) ? 1.0 : 0.0;
         dgw = 0.0;
       }
-      const double zeff = (double)c.tab.zeff[zi];
-      const double gam = c.tab.gam[zi] * c.cfg.gc;
-      const double qref = c.tab.refq[zi * NREF + lane] + zeff;
-      double z, dz, z0, dz0;
-      zeta_and_deriv(gam, qref, q + zeff, c.cfg.ga, DBL_EPSILON, &z, &dz);
-      zeta_and_deriv(gam, qref, 0.0 + zeff, c.cfg.ga, DBL_EPSILON, &z0, &dz0);
       gq = z * gw;
       g0 = z0 * gw;
       dgq_dcn = z * dgw;
       dgq_dq = dz * gw;
       dg0_dcn = z0 * dgw;
     }
+    s_w[warp][u][0][r] = gq;
+    s_w[warp][u][1][r] = g0;
+    s_w[warp][u][2][r] = dgq_dcn;
+    s_w[warp][u][3][r] = dgq_dq;
+    s_w[warp][u][4][r] = dg0_dcn;
+  }
+  __syncwarp();
+  // ---- phase 2: frequencies
+  for (int o = lane; o < WU * NFREQ; o += 32) {
+    const int uu = o / NFREQ, w = o % NFREQ;
+    const int unit2 = (blockIdx.x * 8 + warp) * WU + uu;
+    const int i2 = unit2 / S, s2 = unit2 % S;
+    if (i2 >= N) continue;
+    const size_t a2 = (size_t)b * N + i2;
+    const int z2 = c.w.z[a2];
+    const size_t off = (a2 * S + s2) * NFREQ + w;
     double a = 0.0, a0 = 0.0, da_dcn = 0.0, da_dq = 0.0, da0_dcn = 0.0;
-    const double *alpha = c.tab.alpha + (size_t)zi * NREF * NFREQ;
+    if (z2 != 0) {
+      const double *alpha = c.tab.alpha + (size_t)z2 * NREF * NFREQ + w;
 #pragma unroll
-    for (int r = 0; r < NREF; ++r) {
-      const double wq = __shfl_sync(0xffffffffu, gq, r);
-      const double w0 = __shfl_sync(0xffffffffu, g0, r);
-      const double w1 = __shfl_sync(0xffffffffu, dgq_dcn, r);
-      const double w2 = __shfl_sync(0xffffffffu, dgq_dq, r);
-      const double w3 = __shfl_sync(0xffffffffu, dg0_dcn, r);
-      if (lane < NFREQ) {
-        const double al = alpha[r * NFREQ + lane];
-        a += wq * al;
-        a0 += w0 * al;
-        da_dcn += w1 * al;
-        da_dq += w2 * al;
-        da0_dcn += w3 * al;
+      for (int rr = 0; rr < NREF; ++rr) {
+        const double al = alpha[rr * NFREQ];
+        a += s_w[warp][uu][0][rr] * al;
+        a0 += s_w[warp][uu][1][rr] * al;
+        da_dcn += s_w[warp][uu][2][rr] * al;
+        da_dq += s_w[warp][uu][3][rr] * al;
+        da0_dcn += s_w[warp][uu][4][rr] * al;
       }
     }
-    if (lane < NFREQ) {
-      c.w.A[o + lane] = a;
-      c.w.A0[o + lane] = a0;
-      if (grad) {
-        c.w.dA_dcn[o + lane] = da_dcn;
-        c.w.dA_dq[o + lane] = da_dq;
-        c.w.dA0_dcn[o + lane] = da0_dcn;
-      }
+    c.w.A[off] = a;
+    c.w.A0[off] = a0;
+    if (grad) {
+      c.w.dA_dcn[off] = da_dcn;
+      c.w.dA_dq[off] = da_dq;
+      c.w.dA0_dcn[off] = da0_dcn;
     }
   }
 }
@@ -1038,7 +1030,8 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   }
   stage_end(ST_EEQ, st);
   stage_begin(ST_WEIGHTS, st);
-  weights_kernel<<<atoms, 256, 0, st>>>(c);
+  const dim3 units(((size_t)N * c.S + 8 * WU - 1) / (8 * WU), B);
+  weights_kernel<<<units, 256, 0, st>>>(c);
   stage_end(ST_WEIGHTS, st);
   stage_begin(ST_PAIR_FWD, st);
   pair_fwd_kernel<<<atoms, 256, 0, st>>>(c);
@@ -1076,6 +1069,32 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
     param_grad_finish_kernel<<<(8 * B + 255) / 256, 256, 0, st>>>(c);
   stage_end(ST_FINISH, st);
   return 0;
+}
+
+void launch_prep(const Ctx &c, cudaStream_t st) {
+  cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
+  prep_kernel<<<c.B, 256, 0, st>>>(c);
+}
+
+void launch_cn(const Ctx &c, cudaStream_t st) {
+  cn_kernel<<<dim3((c.N + 7) / 8, c.B), 256, 0, st>>>(c);
+}
+
+void launch_weights(const Ctx &c, cudaStream_t st) {
+  const dim3 units(((size_t)c.N * c.S + 8 * WU - 1) / (8 * WU), c.B);
+  weights_kernel<<<units, 256, 0, st>>>(c);
+}
+
+void launch_charges_in(const Ctx &c, cudaStream_t st) {
+  const size_t total = (size_t)c.B * c.N;
+  charges_in_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
+}
+
+void launch_finish(const Ctx &c, cudaStream_t st) {
+  const size_t total = (size_t)c.B * c.N;
+  finish_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
+  if (c.flags & D4_FLAG_PARAM_GRAD)
+    param_grad_finish_kernel<<<(8 * c.B + 255) / 256, 256, 0, st>>>(c);
 }
 
 int launch_prepare_alpha(const d4_tables_t &tab, const d4_model_cfg_t &cfg,

@@ -25,6 +25,14 @@ void stage_end(int stage, cudaStream_t st);
 void timing_next_call();
 
 int launch_fp64(const Ctx &c, cudaStream_t st);
+int launch_mixed(const Ctx &c, cudaStream_t st);
+
+// stages shared by the FP64 method and the precision form (d4_fp64.cu)
+void launch_prep(const Ctx &c, cudaStream_t st);
+void launch_cn(const Ctx &c, cudaStream_t st);
+void launch_weights(const Ctx &c, cudaStream_t st);
+void launch_charges_in(const Ctx &c, cudaStream_t st);
+void launch_finish(const Ctx &c, cudaStream_t st);
 int launch_prepare_alpha(const d4_tables_t &tab, const d4_model_cfg_t &cfg,
                          const double *refalpha, const double *refascale,
                          const double *refscount, const int64_t *refsys,

@@ -1,0 +1,935 @@
+// Precision form of the D4 path: FP32 pair and triple arithmetic with
+// compensated accumulation, FP32 Cholesky of the EEQ matrix recovered by FP64
+// iterative refinement, FP64 for coordination numbers, reference weights,
+// residuals and the final per-atom / per-structure reductions.
+//
+// Shared stages (prep, CN, weights, finish) are the FP64 ones.  The CN kernel
+// skips pairs whose counting function is exactly zero in FP64, so it costs
+// little; the weights are per atom.
+#include <float.h>
+
+#include "d4_common.cuh"
+#include "d4_kernels.cuh"
+
+namespace d4 {
+
+constexpr float INV_SQRT_PI_F = 0.564189583547756f;
+constexpr float SQRT3_F = 1.7320508075688772f;
+constexpr double ATM_CTA_TRIPLES = 300000.0;  // target triples per ATM CTA
+constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
+constexpr int ATM_THREADS = 512;
+
+// ---------------------------------------------------------------- convert
+
+// FP32 copies: positions relative to the structure's first slot (so the
+// FP32 differences keep their precision) with sqrt(r4r2) in .w, and the
+// weighted polarisabilities.
+__global__ void mixed_convert_kernel(Ctx c) {
+  const size_t BN = (size_t)c.B * c.N;
+  const size_t nA = BN * c.S * NFREQ;
+  const size_t stride = (size_t)gridDim.x * blockDim.x;
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < BN; t += stride) {
+    const size_t b = t / c.N;
+    const int z = c.w.z[t];
+    const double *p = c.positions + 3 * t;
+    const double *p0 = c.positions + 3 * b * c.N;
+    const double r4 = z ? atom_r4r2(c, t, z) : 0.0;
+    c.w.pos32[t] = z ? make_float4((float)(p[0] - p0[0]), (float)(p[1] - p0[1]),
+                                   (float)(p[2] - p0[2]), (float)sqrt(r4))
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+  }
+  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nA; t += stride) {
+    c.w.A32[t] = (float)c.w.A[t];
+    c.w.A032[t] = (float)c.w.A0[t];
+  }
+}
+
+// ---------------------------------------------------------------- pairs
+
+// Fused C6 + BJ two-body term in FP32, the per-pair ATM table (float4:
+// r, 1/r, log(R0/r), sqrt(C6(q=0))), the direct gradient and the C6
+// adjoint.  One warp per atom i, lanes over partners j.
+template <bool GRAD, bool PGRAD>
+__global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  __shared__ float s_wa[8][NFREQ];
+  __shared__ float s_wa0[8][NFREQ];
+  if (i >= N) return;
+  const size_t ai = (size_t)b * N + i;
+  const int zi = c.w.z[ai];
+  const int n = c.w.n_eff[b];
+  if (i >= n || zi == 0) {
+    if (lane == 0) {
+      c.out.d_energy[ai] = 0.0;
+      if (GRAD) {
+        c.out.d_gradient[3 * ai] = 0.0;
+        c.out.d_gradient[3 * ai + 1] = 0.0;
+        c.out.d_gradient[3 * ai + 2] = 0.0;
+      }
+    }
+    if (GRAD && lane < NFREQ)
+      for (int s = 0; s < c.S; ++s) c.w.G[(ai * c.S + s) * NFREQ + lane] = 0.0;
+    return;
+  }
+  const d4_params_t &p = c.par;
+  const float s6 = (float)p.s6, s8 = (float)p.s8, s10 = (float)p.s10;
+  const float a1 = (float)p.a1, a2 = (float)p.a2, cut2 = (float)p.cut_disp2;
+  const float4 *P = c.w.pos32 + (size_t)b * N;
+  const float4 pi = P[i];
+  const float wi = (float)atom_weight(c, ai);
+  const int nslot = c.w.n_slots[b];
+  const int slot_i = c.w.slot[ai];
+  const double *fw = c.tab.freq_weights;
+  float4 *T = c.w.ptf + (size_t)ai * N;
+  float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
+  Acc32 e_acc, gx, gy, gz;
+  float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  for (int s = 0; s < nslot; ++s) {
+    if (lane < NFREQ) {
+      const size_t o = (ai * c.S + s) * NFREQ + lane;
+      const float f = (float)(THOPI * fw[lane]);
+      s_wa[warp][lane] = f * c.w.A32[o];
+      s_wa0[warp][lane] = f * c.w.A032[o];
+    }
+    __syncwarp();
+    float gacc[NFREQ];
+#pragma unroll
+    for (int w = 0; w < NFREQ; ++w) gacc[w] = 0.f;
+    for (int j = lane; j < n; j += 32) {
+      const size_t aj = (size_t)b * N + j;
+      const int zj = c.w.z[aj];
+      if (j == i || zj == 0 || c.w.slot[aj] != s) continue;
+      const float4 pj = P[j];
+      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float r2 = dx * dx + dy * dy + dz * dz;
+      const float ir = rsqrtf(r2);
+      const float r = r2 * ir;
+      const float *Aj = c.w.A32 + (aj * c.S + slot_i) * NFREQ;
+      const float *A0j = c.w.A032 + (aj * c.S + slot_i) * NFREQ;
+      float c6 = 0.f, c60 = 0.f;
+#pragma unroll
+      for (int w = 0; w < NFREQ; ++w) {
+        c6 = fmaf(s_wa[warp][w], Aj[w], c6);
+        c60 = fmaf(s_wa0[warp][w], A0j[w], c60);
+      }
+      const float sqq = SQRT3_F * pi.w * pj.w;  // sqrt(3 r4r2_i r4r2_j)
+      const float qq = sqq * sqq;
+      const float R0 = fmaf(a1, sqq, a2);
+      T[j] = make_float4(r, ir, logf(R0 * ir), sqrtf(c60));
+      if (PGRAD) Tda[j] = make_float2(sqq / R0, 1.0f / R0);
+      if (r <= cut2) {
+        const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R02 * R02 * R02;
+        const float t6 = 1.0f / (r6 + R06);
+        float e = s6 * c6 * t6;
+        float dEdr = 6.0f * s6 * c6 * (r6 * ir) * t6 * t6;
+        float K = -s6 * t6;
+        float dE_dR0 = 6.0f * s6 * c6 * (R06 / R0) * t6 * t6;
+        pg[0] -= wi * c6 * t6;
+        if (p.has_s8) {
+          const float r8 = r6 * r2, R08 = R06 * R02;
+          const float t8 = 1.0f / (r8 + R08);
+          const float c8 = c6 * qq;
+          e += s8 * c8 * t8;
+          dEdr += 8.0f * s8 * c8 * (r8 * ir) * t8 * t8;
+          K -= s8 * qq * t8;
+          dE_dR0 += 8.0f * s8 * c8 * (R08 / R0) * t8 * t8;
+          pg[1] -= wi * c8 * t8;
+        }
+        if (p.has_s10) {
+          const float r10 = r6 * r2 * r2, R010 = R06 * R02 * R02;
+          const float t10 = 1.0f / (r10 + R010);
+          const float q2 = qq * qq * (49.0f / 40.0f);
+          const float c10 = c6 * q2;
+          e += s10 * c10 * t10;
+          dEdr += 10.0f * s10 * c10 * (r10 * ir) * t10 * t10;
+          K -= s10 * q2 * t10;
+          dE_dR0 += 10.0f * s10 * c10 * (R010 / R0) * t10 * t10;
+          pg[2] -= wi * c10 * t10;
+        }
+        e_acc.add(-0.5f * e);
+        const float phi = 0.5f * (wi + (float)atom_weight(c, aj));
+        dEdr *= phi;
+        K *= phi;
+        pg[3] += wi * 0.5f * dE_dR0 * sqq;
+        pg[4] += wi * 0.5f * dE_dR0;
+        const float f = dEdr * ir;
+        gx.add(f * dx);
+        gy.add(f * dy);
+        gz.add(f * dz);
+        if (GRAD) {
+#pragma unroll
+          for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(K, Aj[w], gacc[w]);
+        }
+      }
+    }
+    if (GRAD) {
+#pragma unroll
+      for (int w = 0; w < NFREQ; ++w) {
+        const float g = warp_sumf(gacc[w]);
+        if (lane == w) c.w.G[(ai * c.S + s) * NFREQ + w] = THOPI * fw[w] * (double)g;
+      }
+    }
+    __syncwarp();
+  }
+  if (GRAD && lane < NFREQ)
+    for (int s = nslot; s < c.S; ++s) c.w.G[(ai * c.S + s) * NFREQ + lane] = 0.0;
+  const double e = warp_sum(e_acc.value());
+  if (PGRAD) {
+    double v[5];
+#pragma unroll
+    for (int k = 0; k < 5; ++k) v[k] = warp_sum((double)pg[k]);
+    if (lane == 0) {
+      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * v[0]);
+      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * v[1]);
+      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * v[2]);
+      atomicAdd(&c.w.pgrad[b * 8 + 3], v[3]);
+      atomicAdd(&c.w.pgrad[b * 8 + 4], v[4]);
+    }
+  }
+  if (GRAD) {
+    const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
+    if (lane == 0) {
+      c.out.d_gradient[3 * ai] = g0;
+      c.out.d_gradient[3 * ai + 1] = g1;
+      c.out.d_gradient[3 * ai + 2] = g2;
+    }
+  }
+  if (lane == 0) c.out.d_energy[ai] = e;
+}
+
+// ---------------------------------------------------------------- ATM
+
+__device__ __forceinline__ int tri_u(int j, int k, int n) {  // j < k, upper triangle
+  return j * n - j * (j + 1) / 2 + (k - j - 1);
+}
+
+// Number of CTAs that share one structure's triples.
+__device__ __forceinline__ int atm_ctas(int n) {
+  const double work = (double)n * n * n / 6.0;
+  int K = (int)ceil(work / ATM_CTA_TRIPLES);
+  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
+}
+
+// Accumulation target of the per-pair / per-atom ATM adjoints.
+template <bool SMEM>
+struct AtmAcc {
+  float *sS, *sP, *sE;  // shared (SMEM)
+  double *gS, *gP, *gE; // global pair blocks [N][N] and atom energies
+  int n, N;
+  __device__ __forceinline__ void pair(int j, int k, float S, float P) const {
+    if (SMEM) {
+      const int t = tri_u(j, k, n);
+      atomicAdd(&sS[t], S);
+      atomicAdd(&sP[t], P);
+    } else {
+      const size_t o = (size_t)j * N + k;
+      atomicAdd(&gS[o], (double)S);
+      atomicAdd(&gP[o], (double)P);
+    }
+  }
+  __device__ __forceinline__ void energy(int x, float e) const {
+    if (SMEM)
+      atomicAdd(&sE[x], e);
+    else
+      atomicAdd(&gE[x], (double)e);
+  }
+};
+
+// ATM energy and adjoint over triples i < j < k of one structure.  K CTAs
+// share a structure (the third atom i is interleaved over them).  A warp
+// takes a task (j, 32 consecutive k > j) and loops over i: lanes hold the
+// (j, k) pair in registers and read the (i, j) (broadcast) and (i, k)
+// (coalesced 128-bit) pair records.  Per-pair dE/dr^2 and mask-weighted
+// triple energies accumulate in shared memory (SMEM, n <= 234) and are
+// flushed once per CTA with FP64 atomics; larger structures accumulate
+// straight into global memory.
+template <bool SMEM, bool GRAD, bool PGRAD>
+__global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
+  extern __shared__ float s_acc[];
+  const int b = blockIdx.y;
+  const int cta = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  if (n < 3) return;
+  const int K = atm_ctas(n);
+  if (cta >= K) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int P = n * (n - 1) / 2;
+  AtmAcc<SMEM> acc;
+  acc.n = n;
+  acc.N = N;
+  acc.sS = s_acc;
+  acc.sP = s_acc + P;
+  acc.sE = s_acc + 2 * P;
+  acc.gS = GRAD ? c.w.pr_S + (size_t)b * N * N : nullptr;
+  acc.gP = GRAD ? c.w.pr_P + (size_t)b * N * N : nullptr;
+  acc.gE = c.w.e3 + (size_t)b * N;
+  if (SMEM) {
+    for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
+    __syncthreads();
+  }
+  const int *Zb = c.w.z + (size_t)b * N;
+  const float4 *T = c.w.ptf + (size_t)b * N * N;
+  const float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
+  const float cut = (float)c.par.cut_disp3;
+  const float alp3 = (float)(c.par.alp / 3.0);
+  const float s9 = (float)c.par.s9;
+  const bool weighted = c.weights != nullptr;
+  const double *W = c.weights ? c.weights + (size_t)b * N : nullptr;
+  float g_s9 = 0.f, g_alp = 0.f, g_a1 = 0.f, g_a2 = 0.f;
+  int task = 0;
+  for (int j = 1; j < n - 1; ++j) {
+    for (int kc = j + 1; kc < n; kc += 32, ++task) {
+      if (task % nwarps != warp || Zb[j] == 0) continue;
+      const int k = kc + lane;
+      const bool kok = k < n && Zb[k] != 0;
+      const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(1e30f, 0.f, 0.f, 0.f);
+      const float rjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
+      const float zjk = rjk * rjk;
+      const int mjk = rjk <= cut;
+      float2 dajk = make_float2(0.f, 0.f);
+      if (PGRAD && kok) dajk = Tda[(size_t)j * N + k];
+      const float wj = weighted ? (float)W[j] : 1.f;
+      const float wk = (weighted && kok) ? (float)W[k] : 1.f;
+      Acc32 Sjk, Pjk, Ej, Ek;
+      for (int i = cta; i < j; i += K) {
+        if (Zb[i] == 0) continue;
+        const float4 pij = T[(size_t)i * N + j];
+        float sij = 0.f, pij_e = 0.f, ei = 0.f;
+        if (kok) {
+          const float4 pik = T[(size_t)i * N + k];
+          const int mij = pij.x <= cut, mik = pik.x <= cut;
+          const int wcount = (mij & mik) + (mij & mjk) + (mik & mjk);
+          if (wcount > 0) {
+            const float x = pij.x * pij.x, y = pik.x * pik.x, z = zjk;
+            const float ir1 = pij.y * pik.y * irjk;
+            const float ir2 = ir1 * ir1;
+            const float ir3 = ir1 * ir2;
+            const float A = x + z - y, Bv = x - z + y, Cv = -x + z + y;
+            const float sfac = A * Bv * Cv;
+            const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
+            const float Lsum = pij.z + pik.z + Ljk;
+            const float ta = __expf(alp3 * Lsum);
+            const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
+            const float c9 = pij.w * pik.w * cjk;
+            const float e = s9 * c9 * fd * ang;
+            const float sixth = e * (1.0f / 6.0f);
+            const float mi = (float)(mjk * (mij + mik));
+            const float mj = (float)(mik * (mij + mjk));
+            const float mk = (float)(mij * (mik + mjk));
+            ei = sixth * mi;
+            Ej.add(sixth * mj);
+            Ek.add(sixth * mk);
+            if (GRAD) {
+              const float wi = weighted ? (float)W[i] : 1.f;
+              const float wgt = (wi * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
+              const float Kc = s9 * c9;
+              const float dfl = 6.0f * alp3 * ta * fd * fd;
+              const float Q = -(5.0f * ang - 2.0f * ir3);
+              const float U = Kc * fd * 0.375f * ir2 * ir3;
+              const float V = 0.5f * Kc * (fd * Q + ang * dfl);
+              const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
+              const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
+              const float dey = fmaf(U, -BC + AC + AB, V * pik.y * pik.y);
+              const float dez = fmaf(U, BC - AC + AB, V * irjk * irjk);
+              sij = wgt * dex;
+              Sjk.add(wgt * dez);
+              const float we = wgt * e;
+              pij_e = we;
+              Pjk.add(we);
+              acc.pair(i, k, wgt * dey, we);
+              if (PGRAD) {
+                const float dfdL = -6.0f * fd * fd * ta;
+                g_s9 += wgt * c9 * fd * ang;
+                g_alp += wgt * s9 * c9 * ang * dfdL * Lsum * (1.0f / 3.0f);
+                const float dfa = wgt * s9 * c9 * ang * dfdL * alp3;
+                const float2 daij = Tda[(size_t)i * N + j];
+                const float2 daik = Tda[(size_t)i * N + k];
+                g_a1 += dfa * (daij.x + daik.x + dajk.x);
+                g_a2 += dfa * (daij.y + daik.y + dajk.y);
+              }
+            }
+          }
+        }
+        // (i, j) and E_i: one value per warp
+        if (GRAD) {
+          sij = warp_sumf(sij);
+          pij_e = warp_sumf(pij_e);
+        }
+        ei = warp_sumf(ei);
+        if (lane == 0) {
+          if (ei != 0.f) acc.energy(i, ei);
+          if (GRAD && (sij != 0.f || pij_e != 0.f)) acc.pair(i, j, sij, pij_e);
+        }
+      }
+      if (GRAD && kok) {
+        const float sv = (float)Sjk.value(), pv = (float)Pjk.value();
+        if (sv != 0.f || pv != 0.f) acc.pair(j, k, sv, pv);
+      }
+      const float ej = warp_sumf((float)Ej.value());
+      if (lane == 0 && ej != 0.f) acc.energy(j, ej);
+      const float ek = (float)Ek.value();
+      if (kok && ek != 0.f) acc.energy(k, ek);
+    }
+  }
+  if (PGRAD) {
+    g_s9 = warp_sumf(g_s9);
+    g_alp = warp_sumf(g_alp);
+    g_a1 = warp_sumf(g_a1);
+    g_a2 = warp_sumf(g_a2);
+    if (lane == 0) {
+      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)g_a1);
+      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)g_a2);
+      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)g_s9);
+      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)g_alp);
+    }
+  }
+  if (SMEM) {
+    __syncthreads();
+    for (int j = warp; j < n; j += nwarps) {
+      for (int k = j + 1 + lane; k < n; k += 32) {
+        const int t = tri_u(j, k, n);
+        if (GRAD) {
+          const float sv = acc.sS[t], pv = acc.sP[t];
+          if (sv != 0.f || pv != 0.f) {
+            const size_t o = ((size_t)b * N + j) * N + k;
+            atomicAdd(&c.w.pr_S[o], (double)sv);
+            atomicAdd(&c.w.pr_P[o], (double)pv);
+          }
+        }
+      }
+    }
+    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+      const float ev = acc.sE[x];
+      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);
+    }
+  }
+}
+
+// ATM forces, C6(q=0) adjoint, chain rule to dE/dCN and dE/dq, E2 + E3.
+__global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int x = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  if (x >= N) return;
+  const size_t ax = (size_t)b * N + x;
+  const int zx = c.w.z[ax];
+  const int n = c.w.n_eff[b];
+  if (x >= n || zx == 0) {
+    if (lane == 0) {
+      c.w.dEdcn[ax] = 0.0;
+      c.w.dEdq[ax] = 0.0;
+    }
+    if (lane < NFREQ)
+      for (int s = 0; s < c.S; ++s) c.w.G0[(ax * c.S + s) * NFREQ + lane] = 0.0;
+    return;
+  }
+  const float4 *P = c.w.pos32 + (size_t)b * N;
+  const float4 px = P[x];
+  const int nslot = c.w.n_slots[b];
+  const int slot_x = c.w.slot[ax];
+  const size_t base = (size_t)b * N * N;
+  const float4 *T = c.w.ptf + base + (size_t)x * N;
+  const double *fw = c.tab.freq_weights;
+  Acc32 gx, gy, gz;
+  for (int s = 0; s < nslot; ++s) {
+    float gacc[NFREQ];
+#pragma unroll
+    for (int w = 0; w < NFREQ; ++w) gacc[w] = 0.f;
+    for (int y = lane; y < n; y += 32) {
+      const size_t ay = (size_t)b * N + y;
+      if (y == x || c.w.z[ay] == 0 || c.w.slot[ay] != s) continue;
+      const int lo = min(x, y), hi = max(x, y);
+      const size_t o = base + (size_t)lo * N + hi;
+      const float S = (float)c.w.pr_S[o];
+      const double Pv = c.w.pr_P[o];
+      const float4 py = P[y];
+      gx.add(2.0f * S * (px.x - py.x));
+      gy.add(2.0f * S * (px.y - py.y));
+      gz.add(2.0f * S * (px.z - py.z));
+      if (Pv != 0.0) {
+        const float cc = T[y].w;
+        const float D = (float)Pv / (2.0f * cc * cc);
+        const float *A0y = c.w.A032 + (ay * c.S + slot_x) * NFREQ;
+#pragma unroll
+        for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[w], gacc[w]);
+      }
+    }
+#pragma unroll
+    for (int w = 0; w < NFREQ; ++w) {
+      const float g = warp_sumf(gacc[w]);
+      if (lane == w) c.w.G0[(ax * c.S + s) * NFREQ + w] = THOPI * fw[w] * (double)g;
+    }
+  }
+  if (lane < NFREQ)
+    for (int s = nslot; s < c.S; ++s) c.w.G0[(ax * c.S + s) * NFREQ + lane] = 0.0;
+  const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
+  __syncwarp();
+  double dcn = 0.0, dq = 0.0;
+  for (int s = 0; s < nslot; ++s) {
+    if (lane < NFREQ) {
+      const size_t o = (ax * c.S + s) * NFREQ + lane;
+      dcn += c.w.G[o] * c.w.dA_dcn[o] + c.w.G0[o] * c.w.dA0_dcn[o];
+      dq += c.w.G[o] * c.w.dA_dq[o];
+    }
+  }
+  dcn = warp_sum(dcn);
+  dq = warp_sum(dq);
+  if (lane == 0) {
+    c.w.dEdcn[ax] = dcn;
+    c.w.dEdq[ax] = dq;
+    c.out.d_gradient[3 * ax] += g0;
+    c.out.d_gradient[3 * ax + 1] += g1;
+    c.out.d_gradient[3 * ax + 2] += g2;
+    c.out.d_energy[ax] += c.w.e3[ax];
+  }
+}
+
+// Forces through the D4 CN, the EEQ CN and the EEQ Coulomb matrix (FP32).
+__global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  if (i >= N) return;
+  const size_t ai = (size_t)b * N + i;
+  const int zi = c.w.z[ai];
+  const int n = c.w.n_eff[b];
+  if (i >= n || zi == 0) return;
+  const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
+  const d4_params_t &p = c.par;
+  const float kcn = (float)p.kcn, k4 = (float)p.k4, k5 = (float)p.k5, k6 = (float)p.k6;
+  const float cut_cn = (float)p.cut_cn, cut_q = (float)p.cut_cn_eeq;
+  const float4 *P = c.w.pos32 + (size_t)b * N;
+  const float4 pi = P[i];
+  const float rci = (float)c.tab.cov_d3[zi], eni = (float)c.tab.en[zi];
+  const float radi = (float)c.tab.eeq_rad[zi];
+  const float gcn_i = (float)c.w.dEdcn[ai];
+  const float gq_i = eeq ? (float)c.w.dEdcnq[ai] : 0.f;
+  const float wi = eeq ? (float)c.w.eeq_w[ai] : 0.f, qi = (float)c.w.q[ai];
+  Acc32 gx, gy, gz;
+  for (int j = lane; j < n; j += 32) {
+    const size_t aj = (size_t)b * N + j;
+    const int zj = c.w.z[aj];
+    if (j == i || zj == 0) continue;
+    const float4 pj = P[j];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r2 = dx * dx + dy * dy + dz * dz;
+    const float ir = rsqrtf(r2);
+    const float r = r2 * ir;
+    float dEdr = 0.f;
+    const float r0 = rci + (float)c.tab.cov_d3[zj];
+    const float xx = kcn * (r / r0 - 1.0f);
+    if (xx < 9.0f) {
+      const float dcf = -kcn / r0 * INV_SQRT_PI_F * __expf(-xx * xx);
+      if (r <= cut_cn) {
+        const float t = fabsf(eni - (float)c.tab.en[zj]) + k5;
+        dEdr += (gcn_i + (float)c.w.dEdcn[aj]) * k4 * __expf(-(t * t) / k6) * dcf;
+      }
+      if (eeq && r <= cut_q) dEdr += (gq_i + (float)c.w.dEdcnq[aj]) * dcf;
+    }
+    if (eeq) {
+      const float radj = (float)c.tab.eeq_rad[zj];
+      const float g = rsqrtf(radi * radi + radj * radj);
+      const float gr = g * r;
+      const float dA = (2.0f * g * INV_SQRT_PI_F * __expf(-gr * gr) * r - erff(gr)) * ir * ir;
+      dEdr -= (wi * (float)c.w.q[aj] + (float)c.w.eeq_w[aj] * qi) * dA;
+    }
+    const float f = dEdr * ir;
+    gx.add(f * dx);
+    gy.add(f * dy);
+    gz.add(f * dz);
+  }
+  const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
+  if (lane == 0) {
+    c.out.d_gradient[3 * ai] += g0;
+    c.out.d_gradient[3 * ai + 1] += g1;
+    c.out.d_gradient[3 * ai + 2] += g2;
+  }
+}
+
+// ---------------------------------------------------------------- EEQ
+
+// One-warp FP32 triangular solves on a packed lower factor.
+template <int NRHS>
+__device__ void warp_forward_solve_f(const float *L, float *v, int ldv, int m) {
+  const int lane = threadIdx.x & 31;
+  for (int i = 0; i < m; ++i) {
+    const float *row = L + tri_index(i, 0);
+    float s[NRHS];
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) s[r] = 0.f;
+    for (int k = lane; k < i; k += 32) {
+      const float l = row[k];
+#pragma unroll
+      for (int r = 0; r < NRHS; ++r) s[r] = fmaf(l, v[r * ldv + k], s[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) s[r] = warp_sumf(s[r]);
+    if (lane == 0) {
+      const float inv = 1.0f / row[i];
+#pragma unroll
+      for (int r = 0; r < NRHS; ++r) v[r * ldv + i] = (v[r * ldv + i] - s[r]) * inv;
+    }
+    __syncwarp();
+  }
+}
+
+template <int NRHS>
+__device__ void warp_backward_solve_f(const float *L, float *v, int ldv, int m) {
+  const int lane = threadIdx.x & 31;
+  for (int i = m - 1; i >= 0; --i) {
+    float s[NRHS];
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) s[r] = 0.f;
+    for (int k = i + 1 + lane; k < m; k += 32) {
+      const float l = L[tri_index(k, i)];
+#pragma unroll
+      for (int r = 0; r < NRHS; ++r) s[r] = fmaf(l, v[r * ldv + k], s[r]);
+    }
+#pragma unroll
+    for (int r = 0; r < NRHS; ++r) s[r] = warp_sumf(s[r]);
+    if (lane == 0) {
+      const float inv = 1.0f / L[tri_index(i, i)];
+#pragma unroll
+      for (int r = 0; r < NRHS; ++r) v[r * ldv + i] = (v[r * ldv + i] - s[r]) * inv;
+    }
+    __syncwarp();
+  }
+}
+
+// Shared-memory layout of the mixed EEQ kernels (in doubles):
+//   idx      int[N]               (N/2 + 1 doubles)
+//   x,y      double[2N]           solution
+//   rx,ry    double[2N]           FP64 residual / right-hand sides
+//   bb       double[2N]           right-hand sides (b, 1) in FP64
+//   vf       float[2N]            FP32 correction (N doubles)
+//   L        float[N(N+1)/2]      FP32 factor (SMEM only)
+__host__ __device__ inline size_t eeq_mixed_vec_doubles(int N) {
+  return (size_t)(N + 1) / 2 + 1 + 6 * (size_t)N + (size_t)N;
+}
+
+constexpr int EEQ_REFINE_MAX = 8;
+constexpr double EEQ_RESIDUAL_TOL = 1e-10;
+
+// max |b - A x| over ``nr`` right-hand sides (FP64 packed symmetric A)
+__device__ double eeq_residual(const double *A64, const double *x, const double *bb, double *rx,
+                               int m, int N, int nr, double *s_red) {
+  double mx = 0.0;
+  for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
+    const int r = t / m, k = t % m;
+    const double *xv = x + r * N;
+    double acc = bb[r * N + k];
+    const double *rowk = A64 + tri_index(k, 0);
+    for (int l = 0; l <= k; ++l) acc -= rowk[l] * xv[l];
+    for (int l = k + 1; l < m; ++l) acc -= A64[tri_index(l, k)] * xv[l];
+    rx[r * N + k] = acc;
+    mx = fmax(mx, fabs(acc));
+  }
+  // block max
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
+  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = mx;
+  __syncthreads();
+  if (threadIdx.x == 0) {
+    double v = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, s_red[w]);
+    s_red[32] = v;
+  }
+  __syncthreads();
+  const double out = s_red[32];
+  __syncthreads();
+  return out;
+}
+
+// FP32 factor + FP64 refinement: x (nr columns) <- A^-1 bb.
+__device__ void eeq_refined_solve(const float *L, const double *A64, double *x, double *rx,
+                                  const double *bb, float *vf, int m, int N, int nr,
+                                  double *s_red) {
+  for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
+    const int r = t / m, k = t % m;
+    x[r * N + k] = 0.0;
+    rx[r * N + k] = bb[r * N + k];
+  }
+  __syncthreads();
+  for (int it = 0; it < EEQ_REFINE_MAX; ++it) {
+    for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
+      const int r = t / m, k = t % m;
+      vf[r * N + k] = (float)rx[r * N + k];
+    }
+    __syncthreads();
+    if (threadIdx.x < 32) {
+      if (nr == 2) {
+        warp_forward_solve_f<2>(L, vf, N, m);
+        warp_backward_solve_f<2>(L, vf, N, m);
+      } else {
+        warp_forward_solve_f<1>(L, vf, N, m);
+        warp_backward_solve_f<1>(L, vf, N, m);
+      }
+    }
+    __syncthreads();
+    for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
+      const int r = t / m, k = t % m;
+      x[r * N + k] += (double)vf[r * N + k];
+    }
+    __syncthreads();
+    if (eeq_residual(A64, x, bb, rx, m, N, nr, s_red) < EEQ_RESIDUAL_TOL) break;
+  }
+}
+
+template <bool SMEM>
+__global__ void __launch_bounds__(256) eeq_mixed_kernel(Ctx c) {
+  extern __shared__ double s_dyn[];
+  const int b = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  __shared__ int s_m;
+  __shared__ float s_inv;
+  __shared__ double s_red[33];
+  int *s_idx = reinterpret_cast<int *>(s_dyn);
+  double *x = s_dyn + (N + 1) / 2 + 1;
+  double *rx = x + 2 * N;
+  double *bb = rx + 2 * N;
+  float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  const size_t NN2 = (size_t)N * (N + 1) / 2;
+  float *L = SMEM ? vf + 2 * N : c.w.eeq_L32 + (size_t)b * NN2;
+  double *A64 = c.w.eeq_L + (size_t)b * NN2;
+  const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
+  const double *P = c.positions + (size_t)b * N * 3;
+  const int *Zb = c.w.z + (size_t)b * N;
+  const size_t tri_m = (size_t)m * (m + 1) / 2;
+  for (size_t t = threadIdx.x; t < tri_m; t += blockDim.x) {
+    int ii = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
+    while (tri_index(ii + 1, 0) <= t) ++ii;
+    while (tri_index(ii, 0) > t) --ii;
+    const int jj = (int)(t - tri_index(ii, 0));
+    const int ia = s_idx[ii], ja = s_idx[jj];
+    const int za = Zb[ia], zb = Zb[ja];
+    double v;
+    if (ii == jj) {
+      v = c.tab.eeq_eta[za] + SQRT_2_OVER_PI / c.tab.eeq_rad[za];
+    } else {
+      const double dx = P[3 * ia] - P[3 * ja], dy = P[3 * ia + 1] - P[3 * ja + 1],
+                   dz = P[3 * ia + 2] - P[3 * ja + 2];
+      const double r = sqrt(dx * dx + dy * dy + dz * dz);
+      const double ra = c.tab.eeq_rad[za], rb = c.tab.eeq_rad[zb];
+      const double g = 1.0 / sqrt(ra * ra + rb * rb);
+      v = erf(g * r) / r;
+    }
+    A64[t] = v;
+    L[t] = (float)v;
+  }
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    const int ia = s_idx[k];
+    const int z = Zb[ia];
+    const double cq = c.w.cnq[(size_t)b * N + ia];
+    const double sq = cq > 0.0 ? sqrt(cq) : 0.0;
+    bb[k] = -c.tab.eeq_chi[z] + c.tab.eeq_kcn[z] * sq;
+    bb[N + k] = 1.0;
+  }
+  __syncthreads();
+  // FP32 right-looking Cholesky
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  for (int k = 0; k < m; ++k) {
+    if (threadIdx.x == 0) {
+      float d = L[tri_index(k, k)];
+      if (!(d > 0.f)) {
+        set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
+        d = 1.f;
+      }
+      d = sqrtf(d);
+      L[tri_index(k, k)] = d;
+      s_inv = 1.0f / d;
+    }
+    __syncthreads();
+    const float inv = s_inv;
+    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) L[tri_index(i, k)] *= inv;
+    __syncthreads();
+    for (int i = k + 1 + warp; i < m; i += nw) {
+      const float lik = L[tri_index(i, k)];
+      float *row = L + tri_index(i, 0);
+      for (int j = k + 1 + lane; j <= i; j += 32) row[j] = fmaf(-lik, L[tri_index(j, k)], row[j]);
+    }
+    __syncthreads();
+  }
+  eeq_refined_solve(L, A64, x, rx, bb, vf, m, N, 2, s_red);
+  if (warp == 0) {
+    double sx = 0.0, sy = 0.0;
+    for (int k = lane; k < m; k += 32) {
+      sx += x[k];
+      sy += x[N + k];
+    }
+    sx = warp_sum(sx);
+    sy = warp_sum(sy);
+    if (lane == 0) {
+      const double lam = m > 0 ? (sx - c.charge[b]) / sy : 0.0;
+      c.w.eeq_sum[2 * b] = sy;
+      c.w.eeq_sum[2 * b + 1] = lam;
+      s_red[32] = lam;
+    }
+  }
+  __syncthreads();
+  const double lam = s_red[32];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    c.w.q[(size_t)b * N + i] = 0.0;
+    c.w.eeq_y[(size_t)b * N + i] = 0.0;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    const size_t a = (size_t)b * N + s_idx[k];
+    c.w.q[a] = x[k] - lam * x[N + k];
+    c.w.eeq_y[a] = x[N + k];
+  }
+  if (SMEM) {
+    float *G = c.w.eeq_L32 + (size_t)b * NN2;
+    for (size_t t = threadIdx.x; t < tri_m; t += blockDim.x) G[t] = L[t];
+  }
+}
+
+// Adjoint: A u = dE/dq by the FP32 factor + FP64 refinement, w = u - nu y.
+__global__ void __launch_bounds__(256) eeq_adjoint_mixed_kernel(Ctx c) {
+  extern __shared__ double s_dyn[];
+  const int b = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  __shared__ int s_m;
+  __shared__ double s_red[33];
+  int *s_idx = reinterpret_cast<int *>(s_dyn);
+  double *x = s_dyn + (N + 1) / 2 + 1;
+  double *rx = x + 2 * N;
+  double *bb = rx + 2 * N;
+  float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  const size_t NN2 = (size_t)N * (N + 1) / 2;
+  const float *L = c.w.eeq_L32 + (size_t)b * NN2;
+  const double *A64 = c.w.eeq_L + (size_t)b * NN2;
+  const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
+  for (int k = threadIdx.x; k < m; k += blockDim.x) bb[k] = c.w.dEdq[(size_t)b * N + s_idx[k]];
+  __syncthreads();
+  eeq_refined_solve(L, A64, x, rx, bb, vf, m, N, 1, s_red);
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  if (warp == 0) {
+    double su = 0.0;
+    for (int k = lane; k < m; k += 32) su += x[k];
+    su = warp_sum(su);
+    if (lane == 0) s_red[32] = m > 0 ? su / c.w.eeq_sum[2 * b] : 0.0;
+  }
+  __syncthreads();
+  const double nu = s_red[32];
+  for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    c.w.eeq_w[(size_t)b * N + i] = 0.0;
+    c.w.dEdcnq[(size_t)b * N + i] = 0.0;
+  }
+  __syncthreads();
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    const size_t a = (size_t)b * N + s_idx[k];
+    const double w = x[k] - nu * c.w.eeq_y[a];
+    c.w.eeq_w[a] = w;
+    const double cq = c.w.cnq[a];
+    const int z = c.w.z[a];
+    c.w.dEdcnq[a] = cq > 0.0 ? w * c.tab.eeq_kcn[z] * 0.5 / sqrt(cq) * c.w.dcnq[a] : 0.0;
+  }
+}
+
+// ---------------------------------------------------------------- launch
+
+template <bool SMEM, bool GRAD, bool PGRAD>
+static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
+  if (SMEM)
+    cudaFuncSetAttribute(atm_mixed_kernel<SMEM, GRAD, PGRAD>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+  atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(ATM_KMAX, c.B), ATM_THREADS, smem, st>>>(c);
+}
+
+int launch_mixed(const Ctx &c, cudaStream_t st) {
+  const int B = c.B, N = c.N;
+  const dim3 atoms((N + 7) / 8, B);
+  const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
+  const bool pgrad = (c.flags & D4_FLAG_PARAM_GRAD) != 0;
+  const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
+  timing_next_call();
+  stage_begin(ST_PREP, st);
+  launch_prep(c, st);
+  stage_end(ST_PREP, st);
+  stage_begin(ST_CN, st);
+  launch_cn(c, st);
+  stage_end(ST_CN, st);
+  const size_t vec_bytes = 8 * eeq_mixed_vec_doubles(N);
+  const size_t tri_bytes = (size_t)4 * ((size_t)N * (N + 1) / 2);
+  const bool eeq_smem = vec_bytes + tri_bytes <= 220 * 1024;
+  stage_begin(ST_EEQ, st);
+  if (eeq) {
+    if (eeq_smem) {
+      cudaFuncSetAttribute(eeq_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)(vec_bytes + tri_bytes));
+      eeq_mixed_kernel<true><<<B, 256, vec_bytes + tri_bytes, st>>>(c);
+    } else {
+      cudaFuncSetAttribute(eeq_mixed_kernel<false>,
+                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
+      eeq_mixed_kernel<false><<<B, 256, vec_bytes, st>>>(c);
+    }
+  } else {
+    launch_charges_in(c, st);
+  }
+  stage_end(ST_EEQ, st);
+  stage_begin(ST_WEIGHTS, st);
+  launch_weights(c, st);
+  const size_t BN = (size_t)B * N;
+  size_t conv_blocks = (BN * c.S * NFREQ + 255) / 256;
+  if (conv_blocks > 65535) conv_blocks = 65535;
+  mixed_convert_kernel<<<(unsigned)conv_blocks, 256, 0, st>>>(c);
+  stage_end(ST_WEIGHTS, st);
+  stage_begin(ST_PAIR_FWD, st);
+  if (pgrad)
+    pair_fwd_mixed_kernel<true, true><<<atoms, 256, 0, st>>>(c);
+  else if (grad)
+    pair_fwd_mixed_kernel<true, false><<<atoms, 256, 0, st>>>(c);
+  else
+    pair_fwd_mixed_kernel<false, false><<<atoms, 256, 0, st>>>(c);
+  stage_end(ST_PAIR_FWD, st);
+  // ATM: shared-memory accumulation when the largest structure fits
+  const size_t atm_smem = (size_t)4 * ((size_t)N * (N - 1) + N);
+  const bool atm_sm = atm_smem <= 220 * 1024;
+  stage_begin(ST_ATM, st);
+  if (atm_sm) {
+    if (pgrad)
+      launch_atm<true, true, true>(c, st, atm_smem);
+    else if (grad)
+      launch_atm<true, true, false>(c, st, atm_smem);
+    else
+      launch_atm<true, false, false>(c, st, atm_smem);
+  } else {
+    if (pgrad)
+      launch_atm<false, true, true>(c, st, 0);
+    else if (grad)
+      launch_atm<false, true, false>(c, st, 0);
+    else
+      launch_atm<false, false, false>(c, st, 0);
+  }
+  stage_end(ST_ATM, st);
+  if (grad) {
+    stage_begin(ST_PAIR_ATM_BWD, st);
+    pair_atm_bwd_mixed_kernel<<<atoms, 256, 0, st>>>(c);
+    stage_end(ST_PAIR_ATM_BWD, st);
+    if (eeq) {
+      stage_begin(ST_EEQ_ADJ, st);
+      cudaFuncSetAttribute(eeq_adjoint_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)vec_bytes);
+      eeq_adjoint_mixed_kernel<<<B, 256, vec_bytes, st>>>(c);
+      stage_end(ST_EEQ_ADJ, st);
+    }
+    stage_begin(ST_PAIR_CN_BWD, st);
+    pair_cn_bwd_mixed_kernel<<<atoms, 256, 0, st>>>(c);
+    stage_end(ST_PAIR_CN_BWD, st);
+  }
+  stage_begin(ST_FINISH, st);
+  launch_finish(c, st);
+  stage_end(ST_FINISH, st);
+  return 0;
+}
+
+}  // namespace d4

@@ -67,6 +67,7 @@ class Runner:
     q: torch.Tensor | None = None
     r4r2: torch.Tensor | None = None
     n_slots: int = 1
+    mixed: bool = False
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
@@ -82,6 +83,8 @@ class Runner:
             flags |= _lib.FLAG_PARAM_GRAD
         if self.q is not None:
             flags |= _lib.FLAG_CHARGES_IN
+        if self.mixed:
+            flags |= _lib.FLAG_MIXED
         energy = torch.empty((B, N), dtype=torch.float64, device=device)
         grad = (torch.empty((B, N, 3), dtype=torch.float64, device=device)
                 if flags & _lib.FLAG_GRADIENT else None)
@@ -167,8 +170,11 @@ class _D4Function(torch.autograd.Function):
         return gpos, gpar, None
 
 
+PRECISIONS = ("fp64", "mixed")
+
+
 def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
-             cn_function, counting_function, damping_function):
+             cn_function, counting_function, damping_function, precision=None):
     device = positions.device
     dtype = positions.dtype
     charge = _as_tensor(charge, device, dtype)
@@ -200,6 +206,10 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
             raise ValueError("`rvdw` radius type is not used by the two-body term of dftd4")
         raise NotImplementedError("only rational (BJ) damping is built in for dftd4")
     resolved = resolve(param)
+    if precision is None:
+        precision = "mixed" if dtype == torch.float32 else "fp64"
+    if precision not in PRECISIONS:
+        raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
     if device.type != "cuda":
         raise RuntimeError("tad-dftd4_gb300 runs on CUDA devices; move the inputs to a GPU")
 
@@ -228,7 +238,7 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
         numbers=nums, charge=chg, tables=tab, model=mdl, params=resolved, cut=cut,
         q=None if q is None else q.reshape(-1, N).to(torch.float64).contiguous(),
         r4r2=None if r4r2 is None else r4r2.reshape(-1, N).to(torch.float64).contiguous(),
-        n_slots=n_slots,
+        n_slots=n_slots, mixed=precision == "mixed",
     )
     pvec = []
     for key in PARAM_ORDER:
@@ -243,7 +253,8 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
 def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, *,
           model="d4", rcov=None, r4r2=None, rvdw=None, q=None, cutoff: Cutoff | None = None,
           cn_function=None, counting_function=None,
-          damping_function: Damping | None = None) -> torch.Tensor:
+          damping_function: Damping | None = None, precision: str | None = None
+          ) -> torch.Tensor:
     """
     Atom-resolved DFT-D4 dispersion energy of a structure or a padded batch.
 
@@ -253,10 +264,16 @@ def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, 
     Returns (..., N) energies in Hartree with the dtype of ``positions``.
     ``cn_function`` / ``counting_function`` / ``damping_function`` accept
     only the defaults (D4 CN with erf counting, rational damping).
+
+    ``precision`` (an addition to the reference signature): ``"fp64"`` runs
+    the plain method in double precision (default for float64 positions);
+    ``"mixed"`` the precision form -- FP32 pair and triple arithmetic with
+    compensated sums, FP32 EEQ factorisation refined in FP64, FP64 CN,
+    weights and final reductions (default for float32 positions).
     """
     runner, pvec, shape = _prepare(numbers, positions, charge, param, model, rcov, r4r2,
                                    rvdw, q, cutoff, cn_function, counting_function,
-                                   damping_function)
+                                   damping_function, precision)
     pos = positions.reshape(-1, shape[-1], 3)
     energy = _D4Function.apply(pos, pvec, runner)
     return energy.reshape(shape)
@@ -270,7 +287,8 @@ def dispersion_energy_gradient(numbers, positions, charge, param, **kw):
     runner, _, shape = _prepare(numbers, positions, charge, param, kw.pop("model", "d4"),
                                 kw.pop("rcov", None), kw.pop("r4r2", None),
                                 kw.pop("rvdw", None), kw.pop("q", None),
-                                kw.pop("cutoff", None), None, None, None)
+                                kw.pop("cutoff", None), None, None, None,
+                                kw.pop("precision", None))
     if kw:
         raise TypeError(f"unexpected arguments {sorted(kw)}")
     pos = positions.reshape(-1, shape[-1], 3)

@@ -1,0 +1,121 @@
+"""
+The precision form (``precision="mixed"``) against the FP64 oracle and the
+reference's own outputs.  Bar (the precision form's contract): per-structure
+energy error <= 1e-7 Eh and force error <= 1e-6 Eh/Bohr; charges from the
+FP32 factorisation refined in FP64 agree with the FP64 solve to 1e-10.
+"""
+
+from __future__ import annotations
+
+import numpy as np
+import pytest
+import torch
+
+import oracle
+from conftest import golden_cases, package
+
+pytestmark = pytest.mark.gpu
+
+CASES = golden_cases()
+E_TOL = 1e-7   # Eh per structure
+F_TOL = 1e-6   # Eh/Bohr per component
+PARAM = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+
+
+@pytest.fixture(scope="module")
+def d4():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    return package()
+
+
+def _check(e, g, e_ref, g_ref):
+    e = np.asarray(e).reshape(-1, np.asarray(e).shape[-1])
+    e_ref = np.asarray(e_ref).reshape(e.shape)
+    de = np.abs(e.sum(-1) - e_ref.sum(-1)).max()
+    df = np.abs(np.asarray(g) - np.asarray(g_ref)).max()
+    assert de <= E_TOL, f"max per-structure |dE| = {de:.3e} Eh"
+    assert df <= F_TOL, f"max |dF| = {df:.3e} Eh/Bohr"
+    return de, df
+
+
+@pytest.mark.parametrize("tag,arrays,meta",
+                         [c for c in CASES if not c[2]["energy_only"]],
+                         ids=[c[0] for c in CASES if not c[2]["energy_only"]])
+def test_golden_within_precision_bar(d4, tag, arrays, meta):
+    dev = torch.device("cuda")
+    numbers = torch.from_numpy(arrays["numbers"]).to(dev)
+    positions = torch.from_numpy(arrays["positions"]).to(dev)
+    charge = torch.from_numpy(arrays["charge"]).to(dev)
+    cutoff = d4.Cutoff(**meta["cutoff"]) if meta["cutoff"] else None
+    cls = d4.D4Model if meta["model"] == "d4" else d4.D4SModel
+    e, g = d4.dispersion_energy_gradient(numbers, positions, charge, meta["param"],
+                                         model=cls(numbers, ref_charges=meta["ref_charges"]),
+                                         cutoff=cutoff, precision="mixed")
+    _check(e.cpu().numpy(), g.cpu().numpy(), arrays["energy"], arrays["grad"])
+
+
+@pytest.mark.parametrize("model", ["d4", "d4s"])
+def test_random_batch_within_precision_bar(d4, model):
+    wl = package().workloads
+    b = wl.batch_uniform(301, 8, 5, 120, wl.ELEMENTS_12, True, "t", 120)
+    nt, pt, ct = map(torch.from_numpy, (b.numbers, b.positions, b.charge))
+    e_ref, g_ref = oracle.dftd4_energy_and_grad(nt, pt, ct, PARAM, model=model)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(nt.to(dev), pt.to(dev), ct.to(dev), PARAM,
+                                         model=model, precision="mixed")
+    _check(e.cpu().numpy(), g.cpu().numpy(), e_ref.numpy(), g_ref.numpy())
+
+
+def test_charges_refined_to_fp64(d4):
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    b = wl.batch_uniform(302, 4, 20, 150, wl.ELEMENTS_12, True, "t", 150)
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (b.numbers, b.positions, b.charge))
+    qs = []
+    for prec in ("fp64", "mixed"):
+        runner, _, _ = disp._prepare(nt, pt, ct, PARAM, "d4", None, None, None, None, None,
+                                     None, None, None, prec)
+        qs.append(runner.run(pt, charges_out=True)[3].cpu().numpy())
+    assert np.abs(qs[0] - qs[1]).max() < 1e-10
+
+
+def test_large_structure_global_accumulation(d4):
+    """n > 234 switches the ATM kernel to global accumulation."""
+    wl = package().workloads
+    z, r = wl.structure(303, 240)
+    nt, pt = torch.from_numpy(z), torch.from_numpy(r)
+    e_ref, g_ref = oracle.dftd4_energy_and_grad(nt, pt, torch.tensor(0.0), PARAM)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(nt.to(dev), pt.to(dev), 0.0, PARAM, precision="mixed")
+    _check(e.cpu().numpy()[None], g.cpu().numpy(), e_ref.numpy()[None], g_ref.numpy())
+
+
+def test_param_gradients_mixed(d4):
+    wl = package().workloads
+    b = wl.batch_uniform(304, 3, 10, 40, wl.ELEMENTS_12, False, "t", 40)
+    dev = torch.device("cuda")
+    nt, pt, ct = map(torch.from_numpy, (b.numbers, b.positions, b.charge))
+    keys = ["s6", "s8", "a1", "a2", "s9"]
+    pref = {k: torch.tensor(PARAM[k], dtype=torch.float64, requires_grad=True) for k in keys}
+    e_ref = oracle.dftd4(nt, pt, ct, pref)
+    g_ref = torch.autograd.grad(e_ref.sum(), [pref[k] for k in keys])
+    pd = {k: torch.tensor(PARAM[k], dtype=torch.float64, device=dev, requires_grad=True)
+          for k in keys}
+    e = d4.dftd4(nt.to(dev), pt.to(dev), ct.to(dev), pd, precision="mixed")
+    g = torch.autograd.grad(e.sum(), [pd[k] for k in keys])
+    for k, a, r in zip(keys, g, g_ref):
+        assert abs(a.item() - r.item()) <= 1e-6 * max(1.0, abs(r.item())), (k, a.item(), r.item())
+
+
+def test_float32_inputs_use_precision_form(d4):
+    wl = package().workloads
+    b = wl.batch_uniform(305, 2, 8, 30, wl.ELEMENTS_12, False, "t", 30)
+    dev = torch.device("cuda")
+    nt, pt, ct = map(torch.from_numpy, (b.numbers, b.positions, b.charge))
+    e_ref = oracle.dftd4(nt, pt, ct, PARAM)
+    e = d4.dftd4(nt.to(dev), pt.to(dev, torch.float32), ct.to(dev), PARAM)
+    assert e.dtype == torch.float32
+    assert np.abs(e.double().cpu().numpy().sum(-1) - e_ref.numpy().sum(-1)).max() <= 1e-6
