@@ -53,8 +53,15 @@ struct Workspace {
   double *pr_da2;   // [B*N*N] d log R0 / d a2 (parameter gradients only)
   double *eeq_L;    // [B*N*(N+1)/2] packed Cholesky factor (FP64 method) or
                     // packed FP64 EEQ matrix (precision form)
+  float4 *pos32;    // [B*N] positions relative to the structure's first slot, FP32,
+                    // with sqrt(r4r2) in .w (both methods)
+  float4 *aux32;    // [B*N] (cov_d3, en, eeq_rad, 0) in FP32 (both methods)
+  int *cidx;        // [B*N] index among the real atoms of the structure, -1 padding
   // precision form only
-  float4 *pos32;    // [B*N] positions in FP32 (x, y, z, sqrt(r4r2))
+  float4 *adj32;    // [B*N] (dE/dCN, dE/dCN_EEQ, q, EEQ adjoint w) in FP32
+  float *prS32;     // [B*N*N] ATM dE/d(r^2), FP32 accumulation
+  float *prP32;     // [B*N*N] ATM weighted triple energies, FP32 accumulation
+  double *eeq_A64;  // [B*N*N] dense FP64 EEQ matrix of the real atoms
   float *A32;       // [B*N*S*23]
   float *A032;      // [B*N*S*23]
   float4 *ptf;      // [B*N*N] (r, 1/r, log(R0/r), sqrt(C6(q=0)))
@@ -80,6 +87,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   const size_t BNS23 = BN * S * NFREQ;
   const size_t BNN = BN * N;
   const bool grad = (flags & D4_FLAG_GRADIENT) != 0;
+  const bool mixed = (flags & D4_FLAG_MIXED) != 0;
   w.status = (int *)take(sizeof(int) * 4);
   w.n_eff = (int *)take(sizeof(int) * B);
   w.n_slots = (int *)take(sizeof(int) * B);
@@ -105,19 +113,24 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.dA0_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
   w.G = grad ? (double *)take(8 * BNS23) : nullptr;
   w.G0 = grad ? (double *)take(8 * BNS23) : nullptr;
-  const bool mixed = (flags & D4_FLAG_MIXED) != 0;
   w.pr_r = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_ir = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_L = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_c = mixed ? nullptr : (double *)take(8 * BNN);
-  w.pr_S = grad ? (double *)take(8 * BNN) : nullptr;
-  w.pr_P = grad ? (double *)take(8 * BNN) : nullptr;
+  w.pr_S = (grad && !mixed) ? (double *)take(8 * BNN) : nullptr;
+  w.pr_P = (grad && !mixed) ? (double *)take(8 * BNN) : nullptr;
   const bool pgrad = (flags & D4_FLAG_PARAM_GRAD) != 0;
   w.pr_da1 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
   w.pr_da2 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
-  w.eeq_L = (double *)take(8 * (size_t)B * ((size_t)N * (N + 1) / 2));
+  w.eeq_L = mixed ? nullptr : (double *)take(8 * (size_t)B * ((size_t)N * (N + 1) / 2));
+  w.pos32 = (float4 *)take(16 * BN);
+  w.aux32 = (float4 *)take(16 * BN);
+  w.cidx = (int *)take(sizeof(int) * BN);
   if (mixed) {
-    w.pos32 = (float4 *)take(16 * BN);
+    w.adj32 = (float4 *)take(16 * BN);
+    w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
+    w.prP32 = grad ? (float *)take(4 * BNN) : nullptr;
+    w.eeq_A64 = (double *)take(8 * BNN);
     w.A32 = (float *)take(4 * BNS23);
     w.A032 = (float *)take(4 * BNS23);
     w.ptf = (float4 *)take(16 * BNN);

@@ -21,10 +21,13 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
   const int b = blockIdx.x;
   const int N = c.N;
   const int64_t *Z = c.numbers + (size_t)b * N;
-  __shared__ int s_neff;
+  __shared__ int s_neff, s_first;
   __shared__ int s_present[MAX_ELEM_ID];
   __shared__ int s_slot_of[MAX_ELEM_ID];
-  if (threadIdx.x == 0) s_neff = 0;
+  if (threadIdx.x == 0) {
+    s_neff = 0;
+    s_first = N;
+  }
   for (int e = threadIdx.x; e < MAX_ELEM_ID; e += blockDim.x) s_present[e] = 0;
   __syncthreads();
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
@@ -35,6 +38,7 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
       continue;
     }
     atomicMax(&s_neff, i + 1);
+    atomicMin(&s_first, i);
     s_present[z] = 1;
     const double *r = c.positions + ((size_t)b * N + i) * 3;
     if (!isfinite(r[0]) || !isfinite(r[1]) || !isfinite(r[2]))
@@ -64,13 +68,39 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
   }
   __syncthreads();
   const int n = s_neff;
+  // FP32 positions are taken relative to the first real atom
+  const double *p0 = c.positions + ((size_t)b * N + (s_first < N ? s_first : 0)) * 3;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
+    const size_t a = (size_t)b * N + i;
     const int64_t z = Z[i];
     const bool ok = z > 0 && z < c.tab.n_ref_elem && z < MAX_ELEM_ID;
     int s = ok ? s_slot_of[z] : 0;
-    c.w.z[(size_t)b * N + i] = ok ? (int)z : 0;
-    c.w.slot[(size_t)b * N + i] = s < c.S ? s : c.S - 1;
-    c.w.e3[(size_t)b * N + i] = 0.0;
+    c.w.z[a] = ok ? (int)z : 0;
+    c.w.slot[a] = s < c.S ? s : c.S - 1;
+    c.w.e3[a] = 0.0;
+    if (ok) {
+      const double *p = c.positions + 3 * a;
+      c.w.pos32[a] = make_float4((float)(p[0] - p0[0]), (float)(p[1] - p0[1]),
+                                 (float)(p[2] - p0[2]), (float)sqrt(atom_r4r2(c, a, z)));
+      c.w.aux32[a] = make_float4((float)c.tab.cov_d3[z], (float)c.tab.en[z],
+                                 (float)c.tab.eeq_rad[z], 0.f);
+    } else {
+      c.w.pos32[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+      c.w.aux32[a] = make_float4(1.f, 0.f, 1.f, 0.f);
+    }
+  }
+  // index of every real atom among the real atoms (EEQ matrix rows)
+  if (threadIdx.x < 32) {
+    int base = 0;
+    for (int i0 = 0; i0 < N; i0 += 32) {
+      const int i = i0 + threadIdx.x;
+      const int64_t z = i < N ? Z[i] : 0;
+      const bool real = i < N && z > 0 && z < c.tab.n_ref_elem && z < MAX_ELEM_ID;
+      const unsigned mask = __ballot_sync(0xffffffffu, real);
+      if (i < N) c.w.cidx[(size_t)b * N + i] =
+          real ? base + __popc(mask & ((1u << threadIdx.x) - 1u)) : -1;
+      base += __popc(mask);
+    }
   }
   if (threadIdx.x < 8) c.w.pgrad[b * 8 + threadIdx.x] = 0.0;
   if (c.w.pr_S) {
@@ -81,18 +111,32 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
       c.w.pr_P[o] = 0.0;
     }
   }
+  if (c.w.prS32) {
+    for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
+      const int i = t / n, j = t % n;
+      const size_t o = ((size_t)b * N + i) * N + j;
+      c.w.prS32[o] = 0.f;
+      c.w.prP32[o] = 0.f;
+    }
+  }
 }
 
 // ---------------------------------------------------------------- CN
 
 // D4 coordination number (EN weighted, cut_cn) and the EEQ coordination
 // number (plain count, cut_cn_eeq, smooth cap) in one pass over the pairs.
+// 1/2 (1 + erf(-x)) is exactly 0.0 in FP64 for x > 6, so a pair whose FP32
+// estimate of x exceeds 7 adds nothing and is dropped before any FP64 work
+// (the sums stay bitwise the same).  The surviving partners of the warp's
+// atom are queued in shared memory and evaluated 32 at a time, so the FP64
+// instructions run with full warps.
 __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
   const int b = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + warp;
   const int N = c.N;
   const int n = c.w.n_eff[b];
+  __shared__ int s_q[8][64];
   if (i >= N) return;
   const size_t ai = (size_t)b * N + i;
   const int zi = c.w.z[ai];
@@ -108,27 +152,50 @@ __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
   const double *P = c.positions + (size_t)b * N * 3;
   const double xi = P[3 * i], yi = P[3 * i + 1], zi3 = P[3 * i + 2];
   const double rci = c.tab.cov_d3[zi], eni = c.tab.en[zi];
-  double s_d4 = 0.0, s_q = 0.0;
-  for (int j = lane; j < n; j += 32) {
+  const float4 *P32 = c.w.pos32 + (size_t)b * N;
+  const float4 *X32 = c.w.aux32 + (size_t)b * N;
+  const float4 pi32 = P32[i];
+  const float rci32 = X32[i].x, kcn32 = (float)c.par.kcn;
+  double s_d4 = 0.0, s_q4 = 0.0;
+  int queued = 0;
+  auto evaluate = [&](int j) {
     const int zj = c.w.z[(size_t)b * N + j];
-    if (j == i || zj == 0) continue;
     const double dx = xi - P[3 * j], dy = yi - P[3 * j + 1], dz = zi3 - P[3 * j + 2];
     const double r = sqrt(dx * dx + dy * dy + dz * dz);
     const double r0 = rci + c.tab.cov_d3[zj];
-    // 1/2 (1 + erf(-x)) is exactly 0.0 in FP64 for x > 6; skip those pairs
-    // (bitwise the same sums) after a cheap FP32 test.
-    if (c.par.kcn * ((float)r / (float)r0 - 1.0f) > 7.0f) continue;
     const double cf = erf_count(r, r0, c.par.kcn);
     if (r <= c.par.cut_cn) s_d4 += en_factor(eni, c.tab.en[zj], c.par.k4, c.par.k5, c.par.k6) * cf;
-    if (r <= c.par.cut_cn_eeq) s_q += cf;
+    if (r <= c.par.cut_cn_eeq) s_q4 += cf;
+  };
+  for (int j0 = 0; j0 < n; j0 += 32) {
+    const int j = j0 + lane;
+    bool keep = false;
+    if (j < n && j != i && c.w.z[(size_t)b * N + j] != 0) {
+      const float4 pj32 = P32[j];
+      const float ex = pi32.x - pj32.x, ey = pi32.y - pj32.y, ez = pi32.z - pj32.z;
+      const float r32 = sqrtf(ex * ex + ey * ey + ez * ez);
+      keep = kcn32 * (r32 / (rci32 + X32[j].x) - 1.0f) <= 7.0f;
+    }
+    const unsigned m = __ballot_sync(0xffffffffu, keep);
+    if (keep) s_q[warp][queued + __popc(m & ((1u << lane) - 1u))] = j;
+    queued += __popc(m);
+    __syncwarp();
+    if (queued >= 32) {
+      evaluate(s_q[warp][lane]);
+      queued -= 32;
+      __syncwarp();
+      if (lane < queued) s_q[warp][lane] = s_q[warp][32 + lane];
+      __syncwarp();
+    }
   }
+  if (lane < queued) evaluate(s_q[warp][lane]);
   s_d4 = warp_sum(s_d4);
-  s_q = warp_sum(s_q);
+  s_q4 = warp_sum(s_q4);
   if (lane == 0) {
     c.w.cn[ai] = s_d4;
     const double m = c.par.cn_eeq_max;
-    c.w.cnq[ai] = log1p(exp(m)) - log1p(exp(m - s_q));
-    c.w.dcnq[ai] = 1.0 / (1.0 + exp(s_q - m));
+    c.w.cnq[ai] = log1p(exp(m)) - log1p(exp(m - s_q4));
+    c.w.dcnq[ai] = 1.0 / (1.0 + exp(s_q4 - m));
     if (c.out.d_cn) c.out.d_cn[ai] = s_d4;
   }
 }
@@ -379,12 +446,21 @@ __global__ void __launch_bounds__(256) weights_kernel(Ctx c) {
     if (refc > 0) {
       if (!d4s) {  // model/d4.py:177-194
         const double tmp = exp(-dcn * dcn);
+        // tmp^wf: the default wf = 6 by products (within a few ulp of pow)
+        const bool six = wf == 6.0;
+        double p1;
+        if (six) {
+          const double t2 = tmp * tmp;
+          p1 = t2 * t2 * t2;
+        } else {
+          p1 = pow(tmp, wf);
+        }
         if (refc == 1) {
-          const double p1 = pow(tmp, wf);
           e = p1;
           de = -2.0 * wf * dcn * p1;
         } else if (refc == 3) {
-          const double p1 = pow(tmp, wf), p2 = pow(tmp, 2.0 * wf), p3 = pow(tmp, 3.0 * wf);
+          const double p2 = six ? p1 * p1 : pow(tmp, 2.0 * wf);
+          const double p3 = six ? p2 * p1 : pow(tmp, 3.0 * wf);
           e = p1 + p2 + p3;
           de = -2.0 * wf * dcn * (p1 + 2.0 * p2 + 3.0 * p3);
         } else {
@@ -395,7 +471,7 @@ __global__ void __launch_bounds__(256) weights_kernel(Ctx c) {
         const double tmp = exp(-dcn * dcn * wf);
         const double dtmp = -2.0 * wf * dcn * tmp;
         if (refc == 3) {
-          const double t2 = pow(tmp, 2.0), t3 = pow(tmp, 3.0);
+          const double t2 = tmp * tmp, t3 = t2 * tmp;
           e = tmp + t2 + t3;
           de = dtmp * (1.0 + 2.0 * tmp + 3.0 * t2);
         } else {

@@ -17,27 +17,15 @@ constexpr float INV_SQRT_PI_F = 0.564189583547756f;
 constexpr float SQRT3_F = 1.7320508075688772f;
 constexpr double ATM_CTA_TRIPLES = 300000.0;  // target triples per ATM CTA
 constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
-constexpr int ATM_THREADS = 512;
+constexpr int ATM_THREADS = 1024;       // 32 warps: one CTA per SM (shared memory)
+constexpr int ATM_THREADS_PGRAD = 512;  // the parameter-gradient variant needs more registers
 
 // ---------------------------------------------------------------- convert
 
-// FP32 copies: positions relative to the structure's first slot (so the
-// FP32 differences keep their precision) with sqrt(r4r2) in .w, and the
-// weighted polarisabilities.
+// FP32 copies of the weighted polarisabilities.
 __global__ void mixed_convert_kernel(Ctx c) {
-  const size_t BN = (size_t)c.B * c.N;
-  const size_t nA = BN * c.S * NFREQ;
+  const size_t nA = (size_t)c.B * c.N * c.S * NFREQ;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < BN; t += stride) {
-    const size_t b = t / c.N;
-    const int z = c.w.z[t];
-    const double *p = c.positions + 3 * t;
-    const double *p0 = c.positions + 3 * b * c.N;
-    const double r4 = z ? atom_r4r2(c, t, z) : 0.0;
-    c.w.pos32[t] = z ? make_float4((float)(p[0] - p0[0]), (float)(p[1] - p0[1]),
-                                   (float)(p[2] - p0[2]), (float)sqrt(r4))
-                     : make_float4(0.f, 0.f, 0.f, 0.f);
-  }
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nA; t += stride) {
     c.w.A32[t] = (float)c.w.A[t];
     c.w.A032[t] = (float)c.w.A0[t];
@@ -217,7 +205,8 @@ __device__ __forceinline__ int atm_ctas(int n) {
 template <bool SMEM>
 struct AtmAcc {
   float *sS, *sP, *sE;  // shared (SMEM)
-  double *gS, *gP, *gE; // global pair blocks [N][N] and atom energies
+  float *gS, *gP;       // global pair blocks [N][N]
+  double *gE;           // atom energies
   int n, N;
   __device__ __forceinline__ void pair(int j, int k, float S, float P) const {
     if (SMEM) {
@@ -226,8 +215,8 @@ struct AtmAcc {
       atomicAdd(&sP[t], P);
     } else {
       const size_t o = (size_t)j * N + k;
-      atomicAdd(&gS[o], (double)S);
-      atomicAdd(&gP[o], (double)P);
+      atomicAdd(&gS[o], S);
+      atomicAdd(&gP[o], P);
     }
   }
   __device__ __forceinline__ void energy(int x, float e) const {
@@ -247,7 +236,8 @@ struct AtmAcc {
 // flushed once per CTA with FP64 atomics; larger structures accumulate
 // straight into global memory.
 template <bool SMEM, bool GRAD, bool PGRAD>
-__global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
+__global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
+    atm_mixed_kernel(Ctx c) {
   extern __shared__ float s_acc[];
   const int b = blockIdx.y;
   const int cta = blockIdx.x;
@@ -265,8 +255,8 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
   acc.sS = s_acc;
   acc.sP = s_acc + P;
   acc.sE = s_acc + 2 * P;
-  acc.gS = GRAD ? c.w.pr_S + (size_t)b * N * N : nullptr;
-  acc.gP = GRAD ? c.w.pr_P + (size_t)b * N * N : nullptr;
+  acc.gS = GRAD ? c.w.prS32 + (size_t)b * N * N : nullptr;
+  acc.gP = GRAD ? c.w.prP32 + (size_t)b * N * N : nullptr;
   acc.gE = c.w.e3 + (size_t)b * N;
   if (SMEM) {
     for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
@@ -290,21 +280,24 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
       const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(1e30f, 0.f, 0.f, 0.f);
       const float rjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
       const float zjk = rjk * rjk;
-      const int mjk = rjk <= cut;
+      const float mjk = rjk <= cut ? 1.f : 0.f;
       float2 dajk = make_float2(0.f, 0.f);
       if (PGRAD && kok) dajk = Tda[(size_t)j * N + k];
       const float wj = weighted ? (float)W[j] : 1.f;
       const float wk = (weighted && kok) ? (float)W[k] : 1.f;
-      Acc32 Sjk, Pjk, Ej, Ek;
+      float Sjk = 0.f, Pjk = 0.f;
+      Acc32 Ej, Ek;
       for (int i = cta; i < j; i += K) {
         if (Zb[i] == 0) continue;
         const float4 pij = T[(size_t)i * N + j];
         float sij = 0.f, pij_e = 0.f, ei = 0.f;
         if (kok) {
           const float4 pik = T[(size_t)i * N + k];
-          const int mij = pij.x <= cut, mik = pik.x <= cut;
-          const int wcount = (mij & mik) + (mij & mjk) + (mik & mjk);
-          if (wcount > 0) {
+          const float mij = pij.x <= cut ? 1.f : 0.f, mik = pik.x <= cut ? 1.f : 0.f;
+          const float mi = mjk * (mij + mik);
+          const float mj = mik * (mij + mjk);
+          const float mk = mij * (mik + mjk);
+          if (mi + mj + mk > 0.f) {
             const float x = pij.x * pij.x, y = pik.x * pik.x, z = zjk;
             const float ir1 = pij.y * pik.y * irjk;
             const float ir2 = ir1 * ir1;
@@ -318,9 +311,6 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
             const float c9 = pij.w * pik.w * cjk;
             const float e = s9 * c9 * fd * ang;
             const float sixth = e * (1.0f / 6.0f);
-            const float mi = (float)(mjk * (mij + mik));
-            const float mj = (float)(mik * (mij + mjk));
-            const float mk = (float)(mij * (mik + mjk));
             ei = sixth * mi;
             Ej.add(sixth * mj);
             Ek.add(sixth * mk);
@@ -337,10 +327,10 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
               const float dey = fmaf(U, -BC + AC + AB, V * pik.y * pik.y);
               const float dez = fmaf(U, BC - AC + AB, V * irjk * irjk);
               sij = wgt * dex;
-              Sjk.add(wgt * dez);
+              Sjk = fmaf(wgt, dez, Sjk);
               const float we = wgt * e;
               pij_e = we;
-              Pjk.add(we);
+              Pjk += we;
               acc.pair(i, k, wgt * dey, we);
               if (PGRAD) {
                 const float dfdL = -6.0f * fd * fd * ta;
@@ -366,13 +356,10 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
           if (GRAD && (sij != 0.f || pij_e != 0.f)) acc.pair(i, j, sij, pij_e);
         }
       }
-      if (GRAD && kok) {
-        const float sv = (float)Sjk.value(), pv = (float)Pjk.value();
-        if (sv != 0.f || pv != 0.f) acc.pair(j, k, sv, pv);
-      }
-      const float ej = warp_sumf((float)Ej.value());
+      if (GRAD && kok && (Sjk != 0.f || Pjk != 0.f)) acc.pair(j, k, Sjk, Pjk);
+      const float ej = warp_sumf(Ej.hi) + warp_sumf(Ej.lo);
       if (lane == 0 && ej != 0.f) acc.energy(j, ej);
-      const float ek = (float)Ek.value();
+      const float ek = Ek.hi + Ek.lo;
       if (kok && ek != 0.f) acc.energy(k, ek);
     }
   }
@@ -397,8 +384,8 @@ __global__ void __launch_bounds__(ATM_THREADS) atm_mixed_kernel(Ctx c) {
           const float sv = acc.sS[t], pv = acc.sP[t];
           if (sv != 0.f || pv != 0.f) {
             const size_t o = ((size_t)b * N + j) * N + k;
-            atomicAdd(&c.w.pr_S[o], (double)sv);
-            atomicAdd(&c.w.pr_P[o], (double)pv);
+            atomicAdd(&c.w.prS32[o], sv);
+            atomicAdd(&c.w.prP32[o], pv);
           }
         }
       }
@@ -424,6 +411,7 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
     if (lane == 0) {
       c.w.dEdcn[ax] = 0.0;
       c.w.dEdq[ax] = 0.0;
+      c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
     if (lane < NFREQ)
       for (int s = 0; s < c.S; ++s) c.w.G0[(ax * c.S + s) * NFREQ + lane] = 0.0;
@@ -446,15 +434,15 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
       if (y == x || c.w.z[ay] == 0 || c.w.slot[ay] != s) continue;
       const int lo = min(x, y), hi = max(x, y);
       const size_t o = base + (size_t)lo * N + hi;
-      const float S = (float)c.w.pr_S[o];
-      const double Pv = c.w.pr_P[o];
+      const float S = c.w.prS32[o];
+      const float Pv = c.w.prP32[o];
       const float4 py = P[y];
       gx.add(2.0f * S * (px.x - py.x));
       gy.add(2.0f * S * (px.y - py.y));
       gz.add(2.0f * S * (px.z - py.z));
-      if (Pv != 0.0) {
+      if (Pv != 0.f) {
         const float cc = T[y].w;
-        const float D = (float)Pv / (2.0f * cc * cc);
+        const float D = Pv / (2.0f * cc * cc);
         const float *A0y = c.w.A032 + (ay * c.S + slot_x) * NFREQ;
 #pragma unroll
         for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[w], gacc[w]);
@@ -483,6 +471,7 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
   if (lane == 0) {
     c.w.dEdcn[ax] = dcn;
     c.w.dEdq[ax] = dq;
+    c.w.adj32[ax] = make_float4((float)dcn, 0.f, (float)c.w.q[ax], 0.f);
     c.out.d_gradient[3 * ax] += g0;
     c.out.d_gradient[3 * ax + 1] += g1;
     c.out.d_gradient[3 * ax + 2] += g2;
@@ -506,39 +495,34 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
   const float kcn = (float)p.kcn, k4 = (float)p.k4, k5 = (float)p.k5, k6 = (float)p.k6;
   const float cut_cn = (float)p.cut_cn, cut_q = (float)p.cut_cn_eeq;
   const float4 *P = c.w.pos32 + (size_t)b * N;
-  const float4 pi = P[i];
-  const float rci = (float)c.tab.cov_d3[zi], eni = (float)c.tab.en[zi];
-  const float radi = (float)c.tab.eeq_rad[zi];
-  const float gcn_i = (float)c.w.dEdcn[ai];
-  const float gq_i = eeq ? (float)c.w.dEdcnq[ai] : 0.f;
-  const float wi = eeq ? (float)c.w.eeq_w[ai] : 0.f, qi = (float)c.w.q[ai];
+  const float4 *X = c.w.aux32 + (size_t)b * N;
+  const float4 *D = c.w.adj32 + (size_t)b * N;
+  const float4 pi = P[i], xi = X[i], di = D[i];
   Acc32 gx, gy, gz;
   for (int j = lane; j < n; j += 32) {
     const size_t aj = (size_t)b * N + j;
-    const int zj = c.w.z[aj];
-    if (j == i || zj == 0) continue;
-    const float4 pj = P[j];
+    if (j == i || c.w.z[aj] == 0) continue;
+    const float4 pj = P[j], xj = X[j], dj = D[j];
     const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
     const float ir = rsqrtf(r2);
     const float r = r2 * ir;
     float dEdr = 0.f;
-    const float r0 = rci + (float)c.tab.cov_d3[zj];
+    const float r0 = xi.x + xj.x;
     const float xx = kcn * (r / r0 - 1.0f);
     if (xx < 9.0f) {
       const float dcf = -kcn / r0 * INV_SQRT_PI_F * __expf(-xx * xx);
       if (r <= cut_cn) {
-        const float t = fabsf(eni - (float)c.tab.en[zj]) + k5;
-        dEdr += (gcn_i + (float)c.w.dEdcn[aj]) * k4 * __expf(-(t * t) / k6) * dcf;
+        const float t = fabsf(xi.y - xj.y) + k5;
+        dEdr += (di.x + dj.x) * k4 * __expf(-(t * t) / k6) * dcf;
       }
-      if (eeq && r <= cut_q) dEdr += (gq_i + (float)c.w.dEdcnq[aj]) * dcf;
+      if (eeq && r <= cut_q) dEdr += (di.y + dj.y) * dcf;
     }
     if (eeq) {
-      const float radj = (float)c.tab.eeq_rad[zj];
-      const float g = rsqrtf(radi * radi + radj * radj);
+      const float g = rsqrtf(xi.z * xi.z + xj.z * xj.z);
       const float gr = g * r;
       const float dA = (2.0f * g * INV_SQRT_PI_F * __expf(-gr * gr) * r - erff(gr)) * ir * ir;
-      dEdr -= (wi * (float)c.w.q[aj] + (float)c.w.eeq_w[aj] * qi) * dA;
+      dEdr -= (di.w * dj.z + dj.w * di.z) * dA;
     }
     const float f = dEdr * ir;
     gx.add(f * dx);
@@ -603,10 +587,54 @@ __device__ void warp_backward_solve_f(const float *L, float *v, int ldv, int m) 
   }
 }
 
+// FP64 reciprocal square root: FP32 estimate refined by two Newton steps
+// y <- y (3 - a y^2) / 2 (quadratic convergence: 2^-22 -> 2^-44 -> below
+// one FP64 ulp), for a > 0 in the FP32 range.
+__device__ __forceinline__ double rsqrt_newton(double a) {
+  double y = (double)rsqrtf((float)a);
+  y = y * (1.5 - 0.5 * a * y * y);
+  y = y * (1.5 - 0.5 * a * y * y);
+  return y;
+}
+
+// Dense FP64 EEQ matrix of the real atoms (rows / columns in the order of
+// ``cidx``, leading dimension N).  One thread per lower-triangle entry,
+// mirrored; all structures at once.  erf(x) is exactly 1.0 in FP64 for
+// x > 6.5, where the entry is 1/r.
+__global__ void eeq_build_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
+  if (t >= (size_t)n * (n + 1) / 2) return;
+  int i = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while (tri_index(i + 1, 0) <= t) ++i;
+  while (i > 0 && tri_index(i, 0) > t) --i;
+  const int j = (int)(t - tri_index(i, 0));
+  const size_t ai = (size_t)b * N + i, aj = (size_t)b * N + j;
+  const int ci = c.w.cidx[ai], cj = c.w.cidx[aj];
+  if (ci < 0 || cj < 0) return;
+  const int zi = c.w.z[ai], zj = c.w.z[aj];
+  double *A = c.w.eeq_A64 + (size_t)b * N * N;
+  if (i == j) {
+    A[(size_t)ci * N + ci] = c.tab.eeq_eta[zi] + SQRT_2_OVER_PI / c.tab.eeq_rad[zi];
+    return;
+  }
+  const double *pi = c.positions + 3 * ai, *pj = c.positions + 3 * aj;
+  const double dx = pi[0] - pj[0], dy = pi[1] - pj[1], dz = pi[2] - pj[2];
+  const double r2 = dx * dx + dy * dy + dz * dz;
+  const double ir = rsqrt_newton(r2);
+  const double ra = c.tab.eeq_rad[zi], rb = c.tab.eeq_rad[zj];
+  const double x = r2 * ir * rsqrt_newton(ra * ra + rb * rb);
+  const double v = (x > 6.5 ? 1.0 : erf(x)) * ir;
+  A[(size_t)ci * N + cj] = v;
+  A[(size_t)cj * N + ci] = v;
+}
+
 // Shared-memory layout of the mixed EEQ kernels (in doubles):
 //   idx      int[N]               (N/2 + 1 doubles)
-//   x,y      double[2N]           solution
-//   rx,ry    double[2N]           FP64 residual / right-hand sides
+//   x        double[2N]           solution (two right-hand sides)
+//   rx       double[2N]           FP64 residual
 //   bb       double[2N]           right-hand sides (b, 1) in FP64
 //   vf       float[2N]            FP32 correction (N doubles)
 //   L        float[N(N+1)/2]      FP32 factor (SMEM only)
@@ -617,28 +645,38 @@ __host__ __device__ inline size_t eeq_mixed_vec_doubles(int N) {
 constexpr int EEQ_REFINE_MAX = 8;
 constexpr double EEQ_RESIDUAL_TOL = 1e-10;
 
-// max |b - A x| over ``nr`` right-hand sides (FP64 packed symmetric A)
+// rx = bb - A x for ``nr`` right-hand sides; one warp per row of the dense
+// FP64 matrix (coalesced).  Returns max |rx| over the block.
 __device__ double eeq_residual(const double *A64, const double *x, const double *bb, double *rx,
                                int m, int N, int nr, double *s_red) {
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   double mx = 0.0;
-  for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
-    const int r = t / m, k = t % m;
-    const double *xv = x + r * N;
-    double acc = bb[r * N + k];
-    const double *rowk = A64 + tri_index(k, 0);
-    for (int l = 0; l <= k; ++l) acc -= rowk[l] * xv[l];
-    for (int l = k + 1; l < m; ++l) acc -= A64[tri_index(l, k)] * xv[l];
-    rx[r * N + k] = acc;
-    mx = fmax(mx, fabs(acc));
+  for (int k = warp; k < m; k += nw) {
+    const double *row = A64 + (size_t)k * N;
+    double a0 = 0.0, a1 = 0.0;
+    for (int l = lane; l < m; l += 32) {
+      const double a = row[l];
+      a0 += a * x[l];
+      if (nr == 2) a1 += a * x[N + l];
+    }
+    a0 = warp_sum(a0);
+    if (nr == 2) a1 = warp_sum(a1);
+    if (lane == 0) {
+      const double r0 = bb[k] - a0;
+      rx[k] = r0;
+      mx = fmax(mx, fabs(r0));
+      if (nr == 2) {
+        const double r1 = bb[N + k] - a1;
+        rx[N + k] = r1;
+        mx = fmax(mx, fabs(r1));
+      }
+    }
   }
-  // block max
-#pragma unroll
-  for (int o = 16; o > 0; o >>= 1) mx = fmax(mx, __shfl_xor_sync(0xffffffffu, mx, o));
-  if ((threadIdx.x & 31) == 0) s_red[threadIdx.x >> 5] = mx;
+  if (lane == 0) s_red[warp] = mx;
   __syncthreads();
   if (threadIdx.x == 0) {
     double v = 0.0;
-    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) v = fmax(v, s_red[w]);
+    for (int w = 0; w < nw; ++w) v = fmax(v, s_red[w]);
     s_red[32] = v;
   }
   __syncthreads();
@@ -683,7 +721,7 @@ __device__ void eeq_refined_solve(const float *L, const double *A64, double *x, 
 }
 
 template <bool SMEM>
-__global__ void __launch_bounds__(256) eeq_mixed_kernel(Ctx c) {
+__global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
   extern __shared__ double s_dyn[];
   const int b = blockIdx.x;
   const int N = c.N;
@@ -698,31 +736,15 @@ __global__ void __launch_bounds__(256) eeq_mixed_kernel(Ctx c) {
   float *vf = reinterpret_cast<float *>(bb + 2 * N);
   const size_t NN2 = (size_t)N * (N + 1) / 2;
   float *L = SMEM ? vf + 2 * N : c.w.eeq_L32 + (size_t)b * NN2;
-  double *A64 = c.w.eeq_L + (size_t)b * NN2;
+  const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
-  const double *P = c.positions + (size_t)b * N * 3;
   const int *Zb = c.w.z + (size_t)b * N;
-  const size_t tri_m = (size_t)m * (m + 1) / 2;
-  for (size_t t = threadIdx.x; t < tri_m; t += blockDim.x) {
-    int ii = (int)((sqrt(8.0 * (double)t + 1.0) - 1.0) * 0.5);
-    while (tri_index(ii + 1, 0) <= t) ++ii;
-    while (tri_index(ii, 0) > t) --ii;
-    const int jj = (int)(t - tri_index(ii, 0));
-    const int ia = s_idx[ii], ja = s_idx[jj];
-    const int za = Zb[ia], zb = Zb[ja];
-    double v;
-    if (ii == jj) {
-      v = c.tab.eeq_eta[za] + SQRT_2_OVER_PI / c.tab.eeq_rad[za];
-    } else {
-      const double dx = P[3 * ia] - P[3 * ja], dy = P[3 * ia + 1] - P[3 * ja + 1],
-                   dz = P[3 * ia + 2] - P[3 * ja + 2];
-      const double r = sqrt(dx * dx + dy * dy + dz * dz);
-      const double ra = c.tab.eeq_rad[za], rb = c.tab.eeq_rad[zb];
-      const double g = 1.0 / sqrt(ra * ra + rb * rb);
-      v = erf(g * r) / r;
-    }
-    A64[t] = v;
-    L[t] = (float)v;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  // FP32 copy of the lower triangle, one warp per row
+  for (int ii = warp; ii < m; ii += nw) {
+    const double *row = A64 + (size_t)ii * N;
+    float *lrow = L + tri_index(ii, 0);
+    for (int jj = lane; jj <= ii; jj += 32) lrow[jj] = (float)row[jj];
   }
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const int ia = s_idx[k];
@@ -734,7 +756,6 @@ __global__ void __launch_bounds__(256) eeq_mixed_kernel(Ctx c) {
   }
   __syncthreads();
   // FP32 right-looking Cholesky
-  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   for (int k = 0; k < m; ++k) {
     if (threadIdx.x == 0) {
       float d = L[tri_index(k, k)];
@@ -787,12 +808,13 @@ __global__ void __launch_bounds__(256) eeq_mixed_kernel(Ctx c) {
   }
   if (SMEM) {
     float *G = c.w.eeq_L32 + (size_t)b * NN2;
+    const size_t tri_m = (size_t)m * (m + 1) / 2;
     for (size_t t = threadIdx.x; t < tri_m; t += blockDim.x) G[t] = L[t];
   }
 }
 
 // Adjoint: A u = dE/dq by the FP32 factor + FP64 refinement, w = u - nu y.
-__global__ void __launch_bounds__(256) eeq_adjoint_mixed_kernel(Ctx c) {
+__global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
   extern __shared__ double s_dyn[];
   const int b = blockIdx.x;
   const int N = c.N;
@@ -806,7 +828,7 @@ __global__ void __launch_bounds__(256) eeq_adjoint_mixed_kernel(Ctx c) {
   float *vf = reinterpret_cast<float *>(bb + 2 * N);
   const size_t NN2 = (size_t)N * (N + 1) / 2;
   const float *L = c.w.eeq_L32 + (size_t)b * NN2;
-  const double *A64 = c.w.eeq_L + (size_t)b * NN2;
+  const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
   for (int k = threadIdx.x; k < m; k += blockDim.x) bb[k] = c.w.dEdq[(size_t)b * N + s_idx[k]];
   __syncthreads();
@@ -831,7 +853,10 @@ __global__ void __launch_bounds__(256) eeq_adjoint_mixed_kernel(Ctx c) {
     c.w.eeq_w[a] = w;
     const double cq = c.w.cnq[a];
     const int z = c.w.z[a];
-    c.w.dEdcnq[a] = cq > 0.0 ? w * c.tab.eeq_kcn[z] * 0.5 / sqrt(cq) * c.w.dcnq[a] : 0.0;
+    const double dq = cq > 0.0 ? w * c.tab.eeq_kcn[z] * 0.5 / sqrt(cq) * c.w.dcnq[a] : 0.0;
+    c.w.dEdcnq[a] = dq;
+    c.w.adj32[a].y = (float)dq;
+    c.w.adj32[a].w = (float)w;
   }
 }
 
@@ -842,7 +867,8 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
   if (SMEM)
     cudaFuncSetAttribute(atm_mixed_kernel<SMEM, GRAD, PGRAD>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
-  atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(ATM_KMAX, c.B), ATM_THREADS, smem, st>>>(c);
+  const int threads = PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS;
+  atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(ATM_KMAX, c.B), threads, smem, st>>>(c);
 }
 
 int launch_mixed(const Ctx &c, cudaStream_t st) {
@@ -863,14 +889,16 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   const bool eeq_smem = vec_bytes + tri_bytes <= 220 * 1024;
   stage_begin(ST_EEQ, st);
   if (eeq) {
+    eeq_build_mixed_kernel<<<dim3((unsigned)(((size_t)N * (N + 1) / 2 + 255) / 256), B), 256, 0,
+                             st>>>(c);
     if (eeq_smem) {
       cudaFuncSetAttribute(eeq_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(vec_bytes + tri_bytes));
-      eeq_mixed_kernel<true><<<B, 256, vec_bytes + tri_bytes, st>>>(c);
+      eeq_mixed_kernel<true><<<B, 512, vec_bytes + tri_bytes, st>>>(c);
     } else {
       cudaFuncSetAttribute(eeq_mixed_kernel<false>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
-      eeq_mixed_kernel<false><<<B, 256, vec_bytes, st>>>(c);
+      eeq_mixed_kernel<false><<<B, 512, vec_bytes, st>>>(c);
     }
   } else {
     launch_charges_in(c, st);
@@ -919,7 +947,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
       stage_begin(ST_EEQ_ADJ, st);
       cudaFuncSetAttribute(eeq_adjoint_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)vec_bytes);
-      eeq_adjoint_mixed_kernel<<<B, 256, vec_bytes, st>>>(c);
+      eeq_adjoint_mixed_kernel<<<B, 512, vec_bytes, st>>>(c);
       stage_end(ST_EEQ_ADJ, st);
     }
     stage_begin(ST_PAIR_CN_BWD, st);
