@@ -127,6 +127,7 @@ typedef struct d4_outputs {
   double *d_charges;  /* [B][N] EEQ charges (optional) */
   double *d_cn;       /* [B][N] D4 coordination numbers (optional) */
   double *d_param_grad; /* [B][8] dE_b/d(s6,s8,s10,a1,a2,s9,alp,-), D4_FLAG_PARAM_GRAD */
+  double *d_cn_eeq;   /* [B][N] capped EEQ coordination numbers (optional) */
 } d4_outputs_t;
 
 /* Library ABI version (D4_ABI_VERSION). */

@@ -108,6 +108,7 @@ class Outputs(ctypes.Structure):
         ("d_charges", c_void_p),
         ("d_cn", c_void_p),
         ("d_param_grad", c_void_p),
+        ("d_cn_eeq", c_void_p),
     ]
 
 

@@ -57,13 +57,14 @@ struct Workspace {
                     // with sqrt(r4r2) in .w (both methods)
   float4 *aux32;    // [B*N] (cov_d3, en, eeq_rad, 0) in FP32 (both methods)
   int *cidx;        // [B*N] index among the real atoms of the structure, -1 padding
+  float *w32;       // [B*N] energy weights of the differentiated sum (1 by default)
   // precision form only
   float4 *adj32;    // [B*N] (dE/dCN, dE/dCN_EEQ, q, EEQ adjoint w) in FP32
   float *prS32;     // [B*N*N] ATM dE/d(r^2), FP32 accumulation
   float *prP32;     // [B*N*N] ATM weighted triple energies, FP32 accumulation
   double *eeq_A64;  // [B*N*N] dense FP64 EEQ matrix of the real atoms
-  float *A32;       // [B*N*S*23]
-  float *A032;      // [B*N*S*23]
+  float *A32;       // [B*S*23*N] (transposed: atoms contiguous per frequency)
+  float *A032;      // [B*S*23*N]
   float4 *ptf;      // [B*N*N] (r, 1/r, log(R0/r), sqrt(C6(q=0)))
   float2 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2)
   float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor
@@ -126,6 +127,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.pos32 = (float4 *)take(16 * BN);
   w.aux32 = (float4 *)take(16 * BN);
   w.cidx = (int *)take(sizeof(int) * BN);
+  w.w32 = (float *)take(sizeof(float) * BN);
   if (mixed) {
     w.adj32 = (float4 *)take(16 * BN);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;

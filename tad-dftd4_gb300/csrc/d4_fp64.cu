@@ -76,6 +76,7 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
     const bool ok = z > 0 && z < c.tab.n_ref_elem && z < MAX_ELEM_ID;
     int s = ok ? s_slot_of[z] : 0;
     c.w.z[a] = ok ? (int)z : 0;
+    c.w.w32[a] = c.weights ? (float)c.weights[a] : 1.0f;
     c.w.slot[a] = s < c.S ? s : c.S - 1;
     c.w.e3[a] = 0.0;
     if (ok) {
@@ -1028,6 +1029,7 @@ __global__ void finish_kernel(Ctx c) {
   if (t >= total) return;
   if (!(c.flags & D4_FLAG_GRADIENT)) c.out.d_energy[t] += c.w.e3[t];
   if (c.out.d_charges) c.out.d_charges[t] = c.w.q[t];
+  if (c.out.d_cn_eeq) c.out.d_cn_eeq[t] = c.w.cnq[t];
 }
 
 // Copy charges given by the caller into the workspace.

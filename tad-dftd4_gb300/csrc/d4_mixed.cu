@@ -22,13 +22,84 @@ constexpr int ATM_THREADS_PGRAD = 512;  // the parameter-gradient variant needs 
 
 // ---------------------------------------------------------------- convert
 
-// FP32 copies of the weighted polarisabilities.
+// FP32 copies of the weighted polarisabilities, transposed to
+// [b][slot][frequency][atom] so that lanes over partner atoms load
+// consecutive addresses.
 __global__ void mixed_convert_kernel(Ctx c) {
   const size_t nA = (size_t)c.B * c.N * c.S * NFREQ;
   const size_t stride = (size_t)gridDim.x * blockDim.x;
+  const int N = c.N, S = c.S;
   for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nA; t += stride) {
-    c.w.A32[t] = (float)c.w.A[t];
-    c.w.A032[t] = (float)c.w.A0[t];
+    // t indexes the transposed layout: ((b * S + s) * 23 + w) * N + i
+    const int i = (int)(t % N);
+    const size_t r = t / N;
+    const int w = (int)(r % NFREQ);
+    const size_t bs = r / NFREQ;
+    const int s = (int)(bs % S);
+    const size_t b = bs / S;
+    const size_t src = (((b * N + i) * S) + s) * NFREQ + w;
+    c.w.A32[t] = (float)c.w.A[src];
+    c.w.A032[t] = (float)c.w.A0[src];
+  }
+}
+
+// transposed index of (structure b, atom i, slot s, frequency w)
+__device__ __forceinline__ size_t a32_index(int b, int i, int s, int w, int N, int S) {
+  return (((size_t)b * S + s) * NFREQ + w) * N + i;
+}
+
+// ---------------------------------------------------------------- CN
+
+// D4 and EEQ coordination numbers in FP32 (precision form): the counting
+// function as 1/2 erfc(x) (no cancellation for small counts), compensated
+// per-lane sums, FP64 per-atom totals and the smooth EEQ cap in FP64.
+__global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  if (i >= N) return;
+  const size_t ai = (size_t)b * N + i;
+  const int zi = c.w.z[ai];
+  if (i >= n || zi == 0) {
+    if (lane == 0) {
+      c.w.cn[ai] = 0.0;
+      c.w.cnq[ai] = 0.0;
+      c.w.dcnq[ai] = 0.0;
+      if (c.out.d_cn) c.out.d_cn[ai] = 0.0;
+    }
+    return;
+  }
+  const float4 *P = c.w.pos32 + (size_t)b * N;
+  const float4 *X = c.w.aux32 + (size_t)b * N;
+  const float4 pi = P[i], xi = X[i];
+  const float kcn = (float)c.par.kcn, k4 = (float)c.par.k4, k5 = (float)c.par.k5;
+  const float k6 = (float)c.par.k6;
+  const float cut_cn = (float)c.par.cut_cn, cut_q = (float)c.par.cut_cn_eeq;
+  Acc32 s_d4, s_q;
+  for (int j = lane; j < n; j += 32) {
+    if (j == i || c.w.z[(size_t)b * N + j] == 0) continue;
+    const float4 pj = P[j], xj = X[j];
+    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float r = sqrtf(dx * dx + dy * dy + dz * dz);
+    const float x = kcn * (r / (xi.x + xj.x) - 1.0f);
+    if (x > 9.0f) continue;  // erfc(9) / 2 < 1e-36
+    const float cf = 0.5f * erfcf(x);
+    if (r <= cut_cn) {
+      const float t = fabsf(xi.y - xj.y) + k5;
+      s_d4.add(k4 * __expf(-(t * t) / k6) * cf);
+    }
+    if (r <= cut_q) s_q.add(cf);
+  }
+  const double d4 = warp_sum(s_d4.value());
+  const double q = warp_sum(s_q.value());
+  if (lane == 0) {
+    c.w.cn[ai] = d4;
+    const double m = c.par.cn_eeq_max;
+    c.w.cnq[ai] = log1p(exp(m)) - log1p(exp(m - q));
+    c.w.dcnq[ai] = 1.0 / (1.0 + exp(q - m));
+    if (c.out.d_cn) c.out.d_cn[ai] = d4;
   }
 }
 
@@ -67,7 +138,7 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
   const float a1 = (float)p.a1, a2 = (float)p.a2, cut2 = (float)p.cut_disp2;
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 pi = P[i];
-  const float wi = (float)atom_weight(c, ai);
+  const float wi = c.w.w32[ai];
   const int nslot = c.w.n_slots[b];
   const int slot_i = c.w.slot[ai];
   const double *fw = c.tab.freq_weights;
@@ -77,7 +148,7 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   for (int s = 0; s < nslot; ++s) {
     if (lane < NFREQ) {
-      const size_t o = (ai * c.S + s) * NFREQ + lane;
+      const size_t o = a32_index(b, i, s, lane, N, c.S);
       const float f = (float)(THOPI * fw[lane]);
       s_wa[warp][lane] = f * c.w.A32[o];
       s_wa0[warp][lane] = f * c.w.A032[o];
@@ -95,13 +166,13 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       const float r2 = dx * dx + dy * dy + dz * dz;
       const float ir = rsqrtf(r2);
       const float r = r2 * ir;
-      const float *Aj = c.w.A32 + (aj * c.S + slot_i) * NFREQ;
-      const float *A0j = c.w.A032 + (aj * c.S + slot_i) * NFREQ;
+      const float *Aj = c.w.A32 + a32_index(b, j, slot_i, 0, N, c.S);
+      const float *A0j = c.w.A032 + a32_index(b, j, slot_i, 0, N, c.S);
       float c6 = 0.f, c60 = 0.f;
 #pragma unroll
       for (int w = 0; w < NFREQ; ++w) {
-        c6 = fmaf(s_wa[warp][w], Aj[w], c6);
-        c60 = fmaf(s_wa0[warp][w], A0j[w], c60);
+        c6 = fmaf(s_wa[warp][w], Aj[(size_t)w * N], c6);
+        c60 = fmaf(s_wa0[warp][w], A0j[(size_t)w * N], c60);
       }
       const float sqq = SQRT3_F * pi.w * pj.w;  // sqrt(3 r4r2_i r4r2_j)
       const float qq = sqq * sqq;
@@ -138,7 +209,7 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
           pg[2] -= wi * c10 * t10;
         }
         e_acc.add(-0.5f * e);
-        const float phi = 0.5f * (wi + (float)atom_weight(c, aj));
+        const float phi = 0.5f * (wi + c.w.w32[aj]);
         dEdr *= phi;
         K *= phi;
         pg[3] += wi * 0.5f * dE_dR0 * sqq;
@@ -149,7 +220,7 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
         gz.add(f * dz);
         if (GRAD) {
 #pragma unroll
-          for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(K, Aj[w], gacc[w]);
+          for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(K, Aj[(size_t)w * N], gacc[w]);
         }
       }
     }
@@ -269,7 +340,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   const float alp3 = (float)(c.par.alp / 3.0);
   const float s9 = (float)c.par.s9;
   const bool weighted = c.weights != nullptr;
-  const double *W = c.weights ? c.weights + (size_t)b * N : nullptr;
+  const float *W = c.w.w32 + (size_t)b * N;
   float g_s9 = 0.f, g_alp = 0.f, g_a1 = 0.f, g_a2 = 0.f;
   int task = 0;
   for (int j = 1; j < n - 1; ++j) {
@@ -283,8 +354,8 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
       const float mjk = rjk <= cut ? 1.f : 0.f;
       float2 dajk = make_float2(0.f, 0.f);
       if (PGRAD && kok) dajk = Tda[(size_t)j * N + k];
-      const float wj = weighted ? (float)W[j] : 1.f;
-      const float wk = (weighted && kok) ? (float)W[k] : 1.f;
+      const float wj = W[j];
+      const float wk = kok ? W[k] : 1.f;
       float Sjk = 0.f, Pjk = 0.f;
       Acc32 Ej, Ek;
       for (int i = cta; i < j; i += K) {
@@ -315,7 +386,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
             Ej.add(sixth * mj);
             Ek.add(sixth * mk);
             if (GRAD) {
-              const float wi = weighted ? (float)W[i] : 1.f;
+              const float wi = weighted ? W[i] : 1.f;
               const float wgt = (wi * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
               const float Kc = s9 * c9;
               const float dfl = 6.0f * alp3 * ta * fd * fd;
@@ -443,9 +514,9 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
       if (Pv != 0.f) {
         const float cc = T[y].w;
         const float D = Pv / (2.0f * cc * cc);
-        const float *A0y = c.w.A032 + (ay * c.S + slot_x) * NFREQ;
+        const float *A0y = c.w.A032 + a32_index(b, y, slot_x, 0, N, c.S);
 #pragma unroll
-        for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[w], gacc[w]);
+        for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[(size_t)w * N], gacc[w]);
       }
     }
 #pragma unroll
@@ -539,54 +610,6 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
 
 // ---------------------------------------------------------------- EEQ
 
-// One-warp FP32 triangular solves on a packed lower factor.
-template <int NRHS>
-__device__ void warp_forward_solve_f(const float *L, float *v, int ldv, int m) {
-  const int lane = threadIdx.x & 31;
-  for (int i = 0; i < m; ++i) {
-    const float *row = L + tri_index(i, 0);
-    float s[NRHS];
-#pragma unroll
-    for (int r = 0; r < NRHS; ++r) s[r] = 0.f;
-    for (int k = lane; k < i; k += 32) {
-      const float l = row[k];
-#pragma unroll
-      for (int r = 0; r < NRHS; ++r) s[r] = fmaf(l, v[r * ldv + k], s[r]);
-    }
-#pragma unroll
-    for (int r = 0; r < NRHS; ++r) s[r] = warp_sumf(s[r]);
-    if (lane == 0) {
-      const float inv = 1.0f / row[i];
-#pragma unroll
-      for (int r = 0; r < NRHS; ++r) v[r * ldv + i] = (v[r * ldv + i] - s[r]) * inv;
-    }
-    __syncwarp();
-  }
-}
-
-template <int NRHS>
-__device__ void warp_backward_solve_f(const float *L, float *v, int ldv, int m) {
-  const int lane = threadIdx.x & 31;
-  for (int i = m - 1; i >= 0; --i) {
-    float s[NRHS];
-#pragma unroll
-    for (int r = 0; r < NRHS; ++r) s[r] = 0.f;
-    for (int k = i + 1 + lane; k < m; k += 32) {
-      const float l = L[tri_index(k, i)];
-#pragma unroll
-      for (int r = 0; r < NRHS; ++r) s[r] = fmaf(l, v[r * ldv + k], s[r]);
-    }
-#pragma unroll
-    for (int r = 0; r < NRHS; ++r) s[r] = warp_sumf(s[r]);
-    if (lane == 0) {
-      const float inv = 1.0f / L[tri_index(i, i)];
-#pragma unroll
-      for (int r = 0; r < NRHS; ++r) v[r * ldv + i] = (v[r * ldv + i] - s[r]) * inv;
-    }
-    __syncwarp();
-  }
-}
-
 // FP64 reciprocal square root: FP32 estimate refined by two Newton steps
 // y <- y (3 - a y^2) / 2 (quadratic convergence: 2^-22 -> 2^-44 -> below
 // one FP64 ulp), for a > 0 in the FP32 range.
@@ -637,9 +660,161 @@ __global__ void eeq_build_mixed_kernel(Ctx c) {
 //   rx       double[2N]           FP64 residual
 //   bb       double[2N]           right-hand sides (b, 1) in FP64
 //   vf       float[2N]            FP32 correction (N doubles)
+//   invd     float[N]             reciprocal diagonal of the factor
 //   L        float[N(N+1)/2]      FP32 factor (SMEM only)
 __host__ __device__ inline size_t eeq_mixed_vec_doubles(int N) {
-  return (size_t)(N + 1) / 2 + 1 + 6 * (size_t)N + (size_t)N;
+  return (size_t)(N + 1) / 2 + 1 + 6 * (size_t)N + (size_t)N + (size_t)(N + 1) / 2 + 1;
+}
+
+constexpr int PB = 32;  // panel width of the blocked factorisation and solves
+
+// Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
+// m x m FP32 matrix L, in place; invd receives 1 / L_kk.  Three barriers per
+// panel.  A non-positive pivot sets *bad and continues with pivot 1.
+__device__ void chol_blocked(float *L, float *invd, int m, int *bad) {
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  for (int k0 = 0; k0 < m; k0 += PB) {
+    const int kb = min(PB, m - k0);
+    if (warp == 0) {  // diagonal block: lane r owns row k0 + r
+      for (int cc = 0; cc < kb; ++cc) {
+        float d = L[tri_index(k0 + cc, k0 + cc)];
+        if (!(d > 0.f)) {
+          if (lane == 0) *bad = 1;
+          d = 1.f;
+        }
+        d = sqrtf(d);
+        const float inv = 1.0f / d;
+        __syncwarp();
+        if (lane == 0) {
+          L[tri_index(k0 + cc, k0 + cc)] = d;
+          invd[k0 + cc] = inv;
+        }
+        float lrc = 0.f;
+        if (lane > cc && lane < kb) {
+          lrc = L[tri_index(k0 + lane, k0 + cc)] * inv;
+          L[tri_index(k0 + lane, k0 + cc)] = lrc;
+        }
+        __syncwarp();
+        if (lane > cc && lane < kb) {
+          float *row = L + tri_index(k0 + lane, 0);
+          for (int c2 = cc + 1; c2 <= lane; ++c2)
+            row[k0 + c2] = fmaf(-lrc, L[tri_index(k0 + c2, k0 + cc)], row[k0 + c2]);
+        }
+        __syncwarp();
+      }
+    }
+    __syncthreads();
+    // panel below the block: rows solve against the block's transpose
+    for (int i = k0 + kb + tid; i < m; i += nt) {
+      float *row = L + tri_index(i, 0);
+      for (int cc = 0; cc < kb; ++cc) {
+        float v = row[k0 + cc];
+        const float *lc = L + tri_index(k0 + cc, 0);
+        for (int c2 = 0; c2 < cc; ++c2) v = fmaf(-row[k0 + c2], lc[k0 + c2], v);
+        row[k0 + cc] = v * invd[k0 + cc];
+      }
+    }
+    __syncthreads();
+    // trailing update of the lower triangle right of the panel
+    const int t0 = k0 + kb;
+    const int nrem = m - t0;
+    const int ntri = nrem * (nrem + 1) / 2;
+    for (int t = tid; t < ntri; t += nt) {
+      int ii = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+      while ((ii + 1) * (ii + 2) / 2 <= t) ++ii;
+      while (ii > 0 && ii * (ii + 1) / 2 > t) --ii;
+      const int jj = t - ii * (ii + 1) / 2;
+      const float *ri = L + tri_index(t0 + ii, 0) + k0;
+      const float *rj = L + tri_index(t0 + jj, 0) + k0;
+      float acc = 0.f;
+      for (int cc = 0; cc < kb; ++cc) acc = fmaf(ri[cc], rj[cc], acc);
+      L[tri_index(t0 + ii, t0 + jj)] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
+// Blocked solves with the packed factor (all threads of the block call
+// them): forward L z = v, backward L^T x = z, ``nr`` right-hand sides of
+// leading dimension ldv.  Within a 32-row block the recurrence runs on one
+// warp with shuffles; the rest of the rows are updated by all threads.
+__device__ void fwd_solve_blocked(const float *L, const float *invd, float *v, int ldv, int m,
+                                  int nr) {
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  for (int k0 = 0; k0 < m; k0 += PB) {
+    const int kb = min(PB, m - k0);
+    if (warp == 0) {
+      float x0 = lane < kb ? v[k0 + lane] : 0.f;
+      float x1 = (nr == 2 && lane < kb) ? v[ldv + k0 + lane] : 0.f;
+      for (int cc = 0; cc < kb; ++cc) {
+        const float inv = invd[k0 + cc];
+        const float xc0 = __shfl_sync(0xffffffffu, x0, cc) * inv;
+        const float xc1 = __shfl_sync(0xffffffffu, x1, cc) * inv;
+        if (lane == cc) {
+          x0 = xc0;
+          x1 = xc1;
+        } else if (lane > cc && lane < kb) {
+          const float l = L[tri_index(k0 + lane, k0 + cc)];
+          x0 = fmaf(-l, xc0, x0);
+          x1 = fmaf(-l, xc1, x1);
+        }
+      }
+      if (lane < kb) {
+        v[k0 + lane] = x0;
+        if (nr == 2) v[ldv + k0 + lane] = x1;
+      }
+    }
+    __syncthreads();
+    const int rows = m - k0 - kb;
+    for (int t = tid; t < rows * nr; t += nt) {
+      const int r = t / rows, i = k0 + kb + t % rows;
+      const float *row = L + tri_index(i, 0) + k0;
+      const float *xv = v + r * ldv + k0;
+      float acc = 0.f;
+      for (int cc = 0; cc < kb; ++cc) acc = fmaf(row[cc], xv[cc], acc);
+      v[r * ldv + i] -= acc;
+    }
+    __syncthreads();
+  }
+}
+
+__device__ void bwd_solve_blocked(const float *L, const float *invd, float *v, int ldv, int m,
+                                  int nr) {
+  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  if (m <= 0) return;
+  for (int k0 = ((m - 1) / PB) * PB; k0 >= 0; k0 -= PB) {
+    const int kb = min(PB, m - k0);
+    if (warp == 0) {
+      float x0 = lane < kb ? v[k0 + lane] : 0.f;
+      float x1 = (nr == 2 && lane < kb) ? v[ldv + k0 + lane] : 0.f;
+      for (int cc = kb - 1; cc >= 0; --cc) {
+        const float inv = invd[k0 + cc];
+        const float xc0 = __shfl_sync(0xffffffffu, x0, cc) * inv;
+        const float xc1 = __shfl_sync(0xffffffffu, x1, cc) * inv;
+        if (lane == cc) {
+          x0 = xc0;
+          x1 = xc1;
+        } else if (lane < cc) {
+          const float l = L[tri_index(k0 + cc, k0 + lane)];
+          x0 = fmaf(-l, xc0, x0);
+          x1 = fmaf(-l, xc1, x1);
+        }
+      }
+      if (lane < kb) {
+        v[k0 + lane] = x0;
+        if (nr == 2) v[ldv + k0 + lane] = x1;
+      }
+    }
+    __syncthreads();
+    for (int t = tid; t < k0 * nr; t += nt) {
+      const int r = t / k0, i = t % k0;
+      const float *xv = v + r * ldv + k0;
+      float acc = 0.f;
+      for (int cc = 0; cc < kb; ++cc) acc = fmaf(L[tri_index(k0 + cc, i)], xv[cc], acc);
+      v[r * ldv + i] -= acc;
+    }
+    __syncthreads();
+  }
 }
 
 constexpr int EEQ_REFINE_MAX = 8;
@@ -686,9 +861,9 @@ __device__ double eeq_residual(const double *A64, const double *x, const double 
 }
 
 // FP32 factor + FP64 refinement: x (nr columns) <- A^-1 bb.
-__device__ void eeq_refined_solve(const float *L, const double *A64, double *x, double *rx,
-                                  const double *bb, float *vf, int m, int N, int nr,
-                                  double *s_red) {
+__device__ void eeq_refined_solve(const float *L, const float *invd, const double *A64,
+                                  double *x, double *rx, const double *bb, float *vf, int m,
+                                  int N, int nr, double *s_red) {
   for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
     const int r = t / m, k = t % m;
     x[r * N + k] = 0.0;
@@ -701,16 +876,8 @@ __device__ void eeq_refined_solve(const float *L, const double *A64, double *x, 
       vf[r * N + k] = (float)rx[r * N + k];
     }
     __syncthreads();
-    if (threadIdx.x < 32) {
-      if (nr == 2) {
-        warp_forward_solve_f<2>(L, vf, N, m);
-        warp_backward_solve_f<2>(L, vf, N, m);
-      } else {
-        warp_forward_solve_f<1>(L, vf, N, m);
-        warp_backward_solve_f<1>(L, vf, N, m);
-      }
-    }
-    __syncthreads();
+    fwd_solve_blocked(L, invd, vf, N, m, nr);
+    bwd_solve_blocked(L, invd, vf, N, m, nr);
     for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
       const int r = t / m, k = t % m;
       x[r * N + k] += (double)vf[r * N + k];
@@ -727,19 +894,21 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
   const int N = c.N;
   const int n = c.w.n_eff[b];
   __shared__ int s_m;
-  __shared__ float s_inv;
   __shared__ double s_red[33];
   int *s_idx = reinterpret_cast<int *>(s_dyn);
   double *x = s_dyn + (N + 1) / 2 + 1;
   double *rx = x + 2 * N;
   double *bb = rx + 2 * N;
   float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
-  float *L = SMEM ? vf + 2 * N : c.w.eeq_L32 + (size_t)b * NN2;
+  float *L = SMEM ? invd + N + 2 : c.w.eeq_L32 + (size_t)b * NN2;
   const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
   const int *Zb = c.w.z + (size_t)b * N;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
+  __shared__ int s_bad;
+  if (threadIdx.x == 0) s_bad = 0;
   // FP32 copy of the lower triangle, one warp per row
   for (int ii = warp; ii < m; ii += nw) {
     const double *row = A64 + (size_t)ii * N;
@@ -755,30 +924,9 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
     bb[N + k] = 1.0;
   }
   __syncthreads();
-  // FP32 right-looking Cholesky
-  for (int k = 0; k < m; ++k) {
-    if (threadIdx.x == 0) {
-      float d = L[tri_index(k, k)];
-      if (!(d > 0.f)) {
-        set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
-        d = 1.f;
-      }
-      d = sqrtf(d);
-      L[tri_index(k, k)] = d;
-      s_inv = 1.0f / d;
-    }
-    __syncthreads();
-    const float inv = s_inv;
-    for (int i = k + 1 + threadIdx.x; i < m; i += blockDim.x) L[tri_index(i, k)] *= inv;
-    __syncthreads();
-    for (int i = k + 1 + warp; i < m; i += nw) {
-      const float lik = L[tri_index(i, k)];
-      float *row = L + tri_index(i, 0);
-      for (int j = k + 1 + lane; j <= i; j += 32) row[j] = fmaf(-lik, L[tri_index(j, k)], row[j]);
-    }
-    __syncthreads();
-  }
-  eeq_refined_solve(L, A64, x, rx, bb, vf, m, N, 2, s_red);
+  chol_blocked(L, invd, m, &s_bad);
+  if (threadIdx.x == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
+  eeq_refined_solve(L, invd, A64, x, rx, bb, vf, m, N, 2, s_red);
   if (warp == 0) {
     double sx = 0.0, sy = 0.0;
     for (int k = lane; k < m; k += 32) {
@@ -826,13 +974,17 @@ __global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
   double *rx = x + 2 * N;
   double *bb = rx + 2 * N;
   float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
   const float *L = c.w.eeq_L32 + (size_t)b * NN2;
   const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
-  for (int k = threadIdx.x; k < m; k += blockDim.x) bb[k] = c.w.dEdq[(size_t)b * N + s_idx[k]];
+  for (int k = threadIdx.x; k < m; k += blockDim.x) {
+    bb[k] = c.w.dEdq[(size_t)b * N + s_idx[k]];
+    invd[k] = 1.0f / L[tri_index(k, k)];
+  }
   __syncthreads();
-  eeq_refined_solve(L, A64, x, rx, bb, vf, m, N, 1, s_red);
+  eeq_refined_solve(L, invd, A64, x, rx, bb, vf, m, N, 1, s_red);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     double su = 0.0;
@@ -882,7 +1034,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   launch_prep(c, st);
   stage_end(ST_PREP, st);
   stage_begin(ST_CN, st);
-  launch_cn(c, st);
+  cn_mixed_kernel<<<atoms, 256, 0, st>>>(c);
   stage_end(ST_CN, st);
   const size_t vec_bytes = 8 * eeq_mixed_vec_doubles(N);
   const size_t tri_bytes = (size_t)4 * ((size_t)N * (N + 1) / 2);

@@ -71,7 +71,7 @@ class Runner:
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
-            cn_out: bool = False):
+            cn_out: bool = False, cn_eeq_out: bool = False):
         lib = _lib.load()
         device = positions.device
         B, N = self.numbers.shape
@@ -92,6 +92,8 @@ class Runner:
                  if param_grad else None)
         qout = torch.empty((B, N), dtype=torch.float64, device=device) if charges_out else None
         cnout = torch.empty((B, N), dtype=torch.float64, device=device) if cn_out else None
+        cnqout = (torch.empty((B, N), dtype=torch.float64, device=device)
+                  if cn_eeq_out else None)
         w = None if weights is None else weights.to(torch.float64).contiguous()
         ws_bytes = lib.d4_workspace_size(B, N, self.n_slots, flags)
         work = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
@@ -116,6 +118,7 @@ class Runner:
             d_charges=qout.data_ptr() if qout is not None else None,
             d_cn=cnout.data_ptr() if cnout is not None else None,
             d_param_grad=pgrad.data_ptr() if pgrad is not None else None,
+            d_cn_eeq=cnqout.data_ptr() if cnqout is not None else None,
         )
         cfg = _lib.ModelCfg(kind=_lib.MODEL_D4S if self.model.kind == "d4s" else _lib.MODEL_D4,
                             ga=self.model.ga, gc=self.model.gc,
@@ -132,6 +135,8 @@ class Runner:
                 if status == 6:
                     raise ValueError("non-finite positions or charges")
                 _lib.check(status, "d4_dispersion (device status)")
+        if cn_eeq_out:
+            return energy, grad, pgrad, qout, cnout, cnqout
         return energy, grad, pgrad, qout, cnout
 
 

@@ -66,7 +66,7 @@ STRUCTS = {
     "d4_batch_t": ("Batch", ["n_struct", "n_pad", "d_numbers", "d_positions", "d_charge",
                              "d_charges_in", "d_r4r2_in", "d_energy_weights"]),
     "d4_outputs_t": ("Outputs", ["d_energy", "d_gradient", "d_charges", "d_cn",
-                                 "d_param_grad"]),
+                                 "d_param_grad", "d_cn_eeq"]),
 }
 
 
