@@ -58,6 +58,7 @@ struct Workspace {
   float4 *aux32;    // [B*N] (cov_d3, en, eeq_rad, 0) in FP32 (both methods)
   int *cidx;        // [B*N] index among the real atoms of the structure, -1 padding
   float *w32;       // [B*N] energy weights of the differentiated sum (1 by default)
+  float *fw32;      // [23] (3/pi) times the Casimir-Polder weights, FP32
   // precision form only
   float4 *adj32;    // [B*N] (dE/dCN, dE/dCN_EEQ, q, EEQ adjoint w) in FP32
   float *prS32;     // [B*N*N] ATM dE/d(r^2), FP32 accumulation
@@ -65,6 +66,9 @@ struct Workspace {
   double *eeq_A64;  // [B*N*N] dense FP64 EEQ matrix of the real atoms
   float *A32;       // [B*S*23*N] (transposed: atoms contiguous per frequency)
   float *A032;      // [B*S*23*N]
+  float *dA32;      // [B*N*S*23*3] (dA/dCN, dA/dq, dA0/dCN) per atom, slot, frequency
+  float *G32;       // [B*N*S*23] dE/dA
+  float *G032;      // [B*N*S*23] dE/dA0
   float4 *ptf;      // [B*N*N] (r, 1/r, log(R0/r), sqrt(C6(q=0)))
   float2 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2)
   float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor
@@ -128,6 +132,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.aux32 = (float4 *)take(16 * BN);
   w.cidx = (int *)take(sizeof(int) * BN);
   w.w32 = (float *)take(sizeof(float) * BN);
+  w.fw32 = (float *)take(sizeof(float) * 32);
   if (mixed) {
     w.adj32 = (float4 *)take(16 * BN);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
@@ -135,6 +140,9 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.eeq_A64 = (double *)take(8 * BNN);
     w.A32 = (float *)take(4 * BNS23);
     w.A032 = (float *)take(4 * BNS23);
+    w.dA32 = grad ? (float *)take(4 * 3 * BNS23) : nullptr;
+    w.G32 = grad ? (float *)take(4 * BNS23) : nullptr;
+    w.G032 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.ptf = (float4 *)take(16 * BNN);
     w.ptf_da = pgrad ? (float2 *)take(8 * BNN) : nullptr;
     w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
@@ -143,8 +151,16 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   return w;
 }
 
+// FP32 copies of the parameters, converted once on the host so that no
+// kernel thread spends FP64-pipe cycles on setup.
+struct ParamsF {
+  float s6, s8, s10, a1, a2, s9, alp3;
+  float cut2, cut3, cut_cn, cut_q, kcn, k4, k5, k6, cn_max;
+};
+
 // Everything a kernel needs, passed by value.
 struct Ctx {
+  ParamsF pf;
   d4_tables_t tab;
   d4_model_cfg_t cfg;
   d4_params_t par;
@@ -235,6 +251,23 @@ struct Acc32 {
   }
   __device__ __forceinline__ double value() const { return (double)hi + (double)lo; }
 };
+
+// Compensated warp reduction of Acc32 partial sums: every shuffle step adds
+// the high parts with a two-sum and carries the rounding error into the low
+// parts (FP32 only).  All lanes receive the total.
+__device__ __forceinline__ Acc32 warp_sum_acc(Acc32 a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float h2 = __shfl_xor_sync(0xffffffffu, a.hi, o);
+    const float l2 = __shfl_xor_sync(0xffffffffu, a.lo, o);
+    const float t = a.hi + h2;
+    const float bp = t - a.hi;
+    const float err = (a.hi - (t - bp)) + (h2 - bp);
+    a.hi = t;
+    a.lo = a.lo + l2 + err;
+  }
+  return a;
+}
 
 // Real atoms of structure b compacted into s_idx[0..m).  Returns m.
 __device__ inline int compact_real_atoms(const Ctx &c, int b, int n, int *s_idx, int *s_tmp) {

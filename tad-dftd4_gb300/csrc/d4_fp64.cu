@@ -104,6 +104,8 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
     }
   }
   if (threadIdx.x < 8) c.w.pgrad[b * 8 + threadIdx.x] = 0.0;
+  if (b == 0 && threadIdx.x < NFREQ)
+    c.w.fw32[threadIdx.x] = (float)(THOPI * c.tab.freq_weights[threadIdx.x]);
   if (c.w.pr_S) {
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
       const int i = t / n, j = t % n;

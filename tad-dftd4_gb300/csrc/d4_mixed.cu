@@ -15,7 +15,7 @@ namespace d4 {
 
 constexpr float INV_SQRT_PI_F = 0.564189583547756f;
 constexpr float SQRT3_F = 1.7320508075688772f;
-constexpr double ATM_CTA_TRIPLES = 300000.0;  // target triples per ATM CTA
+constexpr int ATM_CTA_TRIPLES = 300000;  // target triples per ATM CTA
 constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
 constexpr int ATM_THREADS = 1024;       // 32 warps: one CTA per SM (shared memory)
 constexpr int ATM_THREADS_PGRAD = 512;  // the parameter-gradient variant needs more registers
@@ -40,6 +40,11 @@ __global__ void mixed_convert_kernel(Ctx c) {
     const size_t src = (((b * N + i) * S) + s) * NFREQ + w;
     c.w.A32[t] = (float)c.w.A[src];
     c.w.A032[t] = (float)c.w.A0[src];
+    if (c.w.dA32) {
+      c.w.dA32[3 * src] = (float)c.w.dA_dcn[src];
+      c.w.dA32[3 * src + 1] = (float)c.w.dA_dq[src];
+      c.w.dA32[3 * src + 2] = (float)c.w.dA0_dcn[src];
+    }
   }
 }
 
@@ -74,9 +79,8 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
   const float4 pi = P[i], xi = X[i];
-  const float kcn = (float)c.par.kcn, k4 = (float)c.par.k4, k5 = (float)c.par.k5;
-  const float k6 = (float)c.par.k6;
-  const float cut_cn = (float)c.par.cut_cn, cut_q = (float)c.par.cut_cn_eeq;
+  const float kcn = c.pf.kcn, k4 = c.pf.k4, k5 = c.pf.k5, k6 = c.pf.k6;
+  const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
   Acc32 s_d4, s_q;
   for (int j = lane; j < n; j += 32) {
     if (j == i || c.w.z[(size_t)b * N + j] == 0) continue;
@@ -92,13 +96,19 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
     }
     if (r <= cut_q) s_q.add(cf);
   }
-  const double d4 = warp_sum(s_d4.value());
-  const double q = warp_sum(s_q.value());
+  // FP32 warp reductions of the compensated per-lane sums (hi and lo apart)
+  const Acc32 d4a = warp_sum_acc(s_d4), qa = warp_sum_acc(s_q);
   if (lane == 0) {
+    const float q = qa.hi + qa.lo;
+    const float m = c.pf.cn_max;
+    const double d4 = d4a.value();
     c.w.cn[ai] = d4;
-    const double m = c.par.cn_eeq_max;
-    c.w.cnq[ai] = log1p(exp(m)) - log1p(exp(m - q));
-    c.w.dcnq[ai] = 1.0 / (1.0 + exp(q - m));
+    // log(1 + e^m) - log(1 + e^(m - q)) = log1p(expm1(q) / (1 + e^(q - m))):
+    // no cancellation, FP32 relative accuracy also for small q (the EEQ
+    // right-hand side takes its square root, which is steep near 0)
+    const float t = 1.0f + expf(q - m);
+    c.w.cnq[ai] = (double)log1pf(expm1f(q) / t);
+    c.w.dcnq[ai] = (double)(1.0f / t);
     if (c.out.d_cn) c.out.d_cn[ai] = d4;
   }
 }
@@ -130,28 +140,27 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       }
     }
     if (GRAD && lane < NFREQ)
-      for (int s = 0; s < c.S; ++s) c.w.G[(ai * c.S + s) * NFREQ + lane] = 0.0;
+      for (int s = 0; s < c.S; ++s) c.w.G32[(ai * c.S + s) * NFREQ + lane] = 0.f;
     return;
   }
   const d4_params_t &p = c.par;
-  const float s6 = (float)p.s6, s8 = (float)p.s8, s10 = (float)p.s10;
-  const float a1 = (float)p.a1, a2 = (float)p.a2, cut2 = (float)p.cut_disp2;
+  const float s6 = c.pf.s6, s8 = c.pf.s8, s10 = c.pf.s10;
+  const float a1 = c.pf.a1, a2 = c.pf.a2, cut2 = c.pf.cut2;
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 pi = P[i];
   const float wi = c.w.w32[ai];
   const int nslot = c.w.n_slots[b];
   const int slot_i = c.w.slot[ai];
-  const double *fw = c.tab.freq_weights;
   float4 *T = c.w.ptf + (size_t)ai * N;
   float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
   Acc32 e_acc, gx, gy, gz;
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  const float fw_l = lane < NFREQ ? c.w.fw32[lane] : 0.f;  // (3/pi) w_lane
   for (int s = 0; s < nslot; ++s) {
     if (lane < NFREQ) {
       const size_t o = a32_index(b, i, s, lane, N, c.S);
-      const float f = (float)(THOPI * fw[lane]);
-      s_wa[warp][lane] = f * c.w.A32[o];
-      s_wa0[warp][lane] = f * c.w.A032[o];
+      s_wa[warp][lane] = fw_l * c.w.A32[o];
+      s_wa0[warp][lane] = fw_l * c.w.A032[o];
     }
     __syncwarp();
     float gacc[NFREQ];
@@ -225,38 +234,40 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       }
     }
     if (GRAD) {
+      float mine = 0.f;
 #pragma unroll
       for (int w = 0; w < NFREQ; ++w) {
         const float g = warp_sumf(gacc[w]);
-        if (lane == w) c.w.G[(ai * c.S + s) * NFREQ + w] = THOPI * fw[w] * (double)g;
+        if (lane == w) mine = g;
       }
+      if (lane < NFREQ) c.w.G32[(ai * c.S + s) * NFREQ + lane] = fw_l * mine;
     }
     __syncwarp();
   }
   if (GRAD && lane < NFREQ)
-    for (int s = nslot; s < c.S; ++s) c.w.G[(ai * c.S + s) * NFREQ + lane] = 0.0;
-  const double e = warp_sum(e_acc.value());
+    for (int s = nslot; s < c.S; ++s) c.w.G32[(ai * c.S + s) * NFREQ + lane] = 0.f;
+  const Acc32 ea = warp_sum_acc(e_acc);
   if (PGRAD) {
-    double v[5];
+    float v[5];
 #pragma unroll
-    for (int k = 0; k < 5; ++k) v[k] = warp_sum((double)pg[k]);
+    for (int k = 0; k < 5; ++k) v[k] = warp_sumf(pg[k]);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * v[0]);
-      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * v[1]);
-      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * v[2]);
-      atomicAdd(&c.w.pgrad[b * 8 + 3], v[3]);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], v[4]);
+      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * (double)v[0]);
+      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * (double)v[1]);
+      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * (double)v[2]);
+      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)v[3]);
+      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)v[4]);
     }
   }
   if (GRAD) {
-    const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
+    const Acc32 g0 = warp_sum_acc(gx), g1 = warp_sum_acc(gy), g2 = warp_sum_acc(gz);
     if (lane == 0) {
-      c.out.d_gradient[3 * ai] = g0;
-      c.out.d_gradient[3 * ai + 1] = g1;
-      c.out.d_gradient[3 * ai + 2] = g2;
+      c.out.d_gradient[3 * ai] = g0.value();
+      c.out.d_gradient[3 * ai + 1] = g1.value();
+      c.out.d_gradient[3 * ai + 2] = g2.value();
     }
   }
-  if (lane == 0) c.out.d_energy[ai] = e;
+  if (lane == 0) c.out.d_energy[ai] = ea.value();
 }
 
 // ---------------------------------------------------------------- ATM
@@ -267,8 +278,9 @@ __device__ __forceinline__ int tri_u(int j, int k, int n) {  // j < k, upper tri
 
 // Number of CTAs that share one structure's triples.
 __device__ __forceinline__ int atm_ctas(int n) {
-  const double work = (double)n * n * n / 6.0;
-  int K = (int)ceil(work / ATM_CTA_TRIPLES);
+  const long long work = (long long)n * n * n / 6;
+  const long long per = (long long)ATM_CTA_TRIPLES;
+  const int K = (int)((work + per - 1) / per);
   return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
 }
 
@@ -336,9 +348,9 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   const int *Zb = c.w.z + (size_t)b * N;
   const float4 *T = c.w.ptf + (size_t)b * N * N;
   const float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
-  const float cut = (float)c.par.cut_disp3;
-  const float alp3 = (float)(c.par.alp / 3.0);
-  const float s9 = (float)c.par.s9;
+  const float cut = c.pf.cut3;
+  const float alp3 = c.pf.alp3;
+  const float s9 = c.pf.s9;
   const bool weighted = c.weights != nullptr;
   const float *W = c.w.w32 + (size_t)b * N;
   float g_s9 = 0.f, g_alp = 0.f, g_a1 = 0.f, g_a2 = 0.f;
@@ -463,7 +475,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     }
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
       const float ev = acc.sE[x];
-      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);
+      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);  // once per atom
     }
   }
 }
@@ -484,8 +496,6 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
       c.w.dEdq[ax] = 0.0;
       c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
     }
-    if (lane < NFREQ)
-      for (int s = 0; s < c.S; ++s) c.w.G0[(ax * c.S + s) * NFREQ + lane] = 0.0;
     return;
   }
   const float4 *P = c.w.pos32 + (size_t)b * N;
@@ -494,8 +504,9 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
   const int slot_x = c.w.slot[ax];
   const size_t base = (size_t)b * N * N;
   const float4 *T = c.w.ptf + base + (size_t)x * N;
-  const double *fw = c.tab.freq_weights;
+  const float fw_l = lane < NFREQ ? c.w.fw32[lane] : 0.f;  // (3/pi) w_lane
   Acc32 gx, gy, gz;
+  Acc32 dcn_acc, dq_acc;
   for (int s = 0; s < nslot; ++s) {
     float gacc[NFREQ];
 #pragma unroll
@@ -519,33 +530,32 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
         for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[(size_t)w * N], gacc[w]);
       }
     }
+    float mine = 0.f;
 #pragma unroll
     for (int w = 0; w < NFREQ; ++w) {
       const float g = warp_sumf(gacc[w]);
-      if (lane == w) c.w.G0[(ax * c.S + s) * NFREQ + w] = THOPI * fw[w] * (double)g;
+      if (lane == w) mine = g;
     }
-  }
-  if (lane < NFREQ)
-    for (int s = nslot; s < c.S; ++s) c.w.G0[(ax * c.S + s) * NFREQ + lane] = 0.0;
-  const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
-  __syncwarp();
-  double dcn = 0.0, dq = 0.0;
-  for (int s = 0; s < nslot; ++s) {
+    // chain rule to CN and q for this slot (lane = frequency)
     if (lane < NFREQ) {
       const size_t o = (ax * c.S + s) * NFREQ + lane;
-      dcn += c.w.G[o] * c.w.dA_dcn[o] + c.w.G0[o] * c.w.dA0_dcn[o];
-      dq += c.w.G[o] * c.w.dA_dq[o];
+      const float g0w = fw_l * mine;
+      const float gw = c.w.G32[o];
+      const float *d = c.w.dA32 + 3 * o;
+      dcn_acc.add(gw * d[0]);
+      dcn_acc.add(g0w * d[2]);
+      dq_acc.add(gw * d[1]);
     }
   }
-  dcn = warp_sum(dcn);
-  dq = warp_sum(dq);
+  const Acc32 g0 = warp_sum_acc(gx), g1 = warp_sum_acc(gy), g2 = warp_sum_acc(gz);
+  const Acc32 dcn = warp_sum_acc(dcn_acc), dq = warp_sum_acc(dq_acc);
   if (lane == 0) {
-    c.w.dEdcn[ax] = dcn;
-    c.w.dEdq[ax] = dq;
-    c.w.adj32[ax] = make_float4((float)dcn, 0.f, (float)c.w.q[ax], 0.f);
-    c.out.d_gradient[3 * ax] += g0;
-    c.out.d_gradient[3 * ax + 1] += g1;
-    c.out.d_gradient[3 * ax + 2] += g2;
+    c.w.dEdcn[ax] = dcn.value();
+    c.w.dEdq[ax] = dq.value();
+    c.w.adj32[ax] = make_float4(dcn.hi + dcn.lo, 0.f, (float)c.w.q[ax], 0.f);
+    c.out.d_gradient[3 * ax] += g0.value();
+    c.out.d_gradient[3 * ax + 1] += g1.value();
+    c.out.d_gradient[3 * ax + 2] += g2.value();
     c.out.d_energy[ax] += c.w.e3[ax];
   }
 }
@@ -562,9 +572,8 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
   const int n = c.w.n_eff[b];
   if (i >= n || zi == 0) return;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
-  const d4_params_t &p = c.par;
-  const float kcn = (float)p.kcn, k4 = (float)p.k4, k5 = (float)p.k5, k6 = (float)p.k6;
-  const float cut_cn = (float)p.cut_cn, cut_q = (float)p.cut_cn_eeq;
+  const float kcn = c.pf.kcn, k4 = c.pf.k4, k5 = c.pf.k5, k6 = c.pf.k6;
+  const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
   const float4 *D = c.w.adj32 + (size_t)b * N;
@@ -600,11 +609,11 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
     gy.add(f * dy);
     gz.add(f * dz);
   }
-  const double g0 = warp_sum(gx.value()), g1 = warp_sum(gy.value()), g2 = warp_sum(gz.value());
+  const Acc32 g0 = warp_sum_acc(gx), g1 = warp_sum_acc(gy), g2 = warp_sum_acc(gz);
   if (lane == 0) {
-    c.out.d_gradient[3 * ai] += g0;
-    c.out.d_gradient[3 * ai + 1] += g1;
-    c.out.d_gradient[3 * ai + 2] += g2;
+    c.out.d_gradient[3 * ai] += g0.value();
+    c.out.d_gradient[3 * ai + 1] += g1.value();
+    c.out.d_gradient[3 * ai + 2] += g2.value();
   }
 }
 
