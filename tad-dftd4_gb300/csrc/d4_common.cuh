@@ -69,8 +69,8 @@ struct Workspace {
   float *dA32;      // [B*N*S*23*3] (dA/dCN, dA/dq, dA0/dCN) per atom, slot, frequency
   float *G32;       // [B*N*S*23] dE/dA
   float *G032;      // [B*N*S*23] dE/dA0
-  float4 *ptf;      // [B*N*N] (r, 1/r, log(R0/r), sqrt(C6(q=0)))
-  float2 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2)
+  float4 *ptf;      // [B*N*N] (r^2, 1/r, alp/3 log2(R0/r), sqrt(C6(q=0)))
+  float4 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2, log(R0/r), 0)
   float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor
   size_t bytes;
 };
@@ -144,7 +144,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.G32 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.G032 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.ptf = (float4 *)take(16 * BNN);
-    w.ptf_da = pgrad ? (float2 *)take(8 * BNN) : nullptr;
+    w.ptf_da = pgrad ? (float4 *)take(16 * BNN) : nullptr;
     w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
   }
   w.bytes = align_up(off, 256);

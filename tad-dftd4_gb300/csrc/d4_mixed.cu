@@ -152,7 +152,8 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
   const int nslot = c.w.n_slots[b];
   const int slot_i = c.w.slot[ai];
   float4 *T = c.w.ptf + (size_t)ai * N;
-  float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
+  float4 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
+  const float alp3_log2e = c.pf.alp3 * 1.4426950408889634f;
   Acc32 e_acc, gx, gy, gz;
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
   const float fw_l = lane < NFREQ ? c.w.fw32[lane] : 0.f;  // (3/pi) w_lane
@@ -186,8 +187,9 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       const float sqq = SQRT3_F * pi.w * pj.w;  // sqrt(3 r4r2_i r4r2_j)
       const float qq = sqq * sqq;
       const float R0 = fmaf(a1, sqq, a2);
-      T[j] = make_float4(r, ir, logf(R0 * ir), sqrtf(c60));
-      if (PGRAD) Tda[j] = make_float2(sqq / R0, 1.0f / R0);
+      const float lnR0r = logf(R0 * ir);
+      T[j] = make_float4(r2, ir, alp3_log2e * lnR0r, sqrtf(c60));
+      if (PGRAD) Tda[j] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
       if (r <= cut2) {
         const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R02 * R02 * R02;
         const float t6 = 1.0f / (r6 + R06);
@@ -284,10 +286,12 @@ __device__ __forceinline__ int atm_ctas(int n) {
   return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
 }
 
-// Accumulation target of the per-pair / per-atom ATM adjoints.
+// Accumulation target of the per-pair / per-atom ATM adjoints.  Pair
+// values go to both (j, k) and (k, j) so that the backward pair kernel reads
+// rows.
 template <bool SMEM>
 struct AtmAcc {
-  float *sS, *sP, *sE;  // shared (SMEM)
+  float *sS, *sP, *sE;  // shared (SMEM): upper triangle and atoms
   float *gS, *gP;       // global pair blocks [N][N]
   double *gE;           // atom energies
   int n, N;
@@ -297,9 +301,10 @@ struct AtmAcc {
       atomicAdd(&sS[t], S);
       atomicAdd(&sP[t], P);
     } else {
-      const size_t o = (size_t)j * N + k;
-      atomicAdd(&gS[o], S);
-      atomicAdd(&gP[o], P);
+      atomicAdd(&gS[(size_t)j * N + k], S);
+      atomicAdd(&gP[(size_t)j * N + k], P);
+      atomicAdd(&gS[(size_t)k * N + j], S);
+      atomicAdd(&gP[(size_t)k * N + j], P);
     }
   }
   __device__ __forceinline__ void energy(int x, float e) const {
@@ -313,11 +318,14 @@ struct AtmAcc {
 // ATM energy and adjoint over triples i < j < k of one structure.  K CTAs
 // share a structure (the third atom i is interleaved over them).  A warp
 // takes a task (j, 32 consecutive k > j) and loops over i: lanes hold the
-// (j, k) pair in registers and read the (i, j) (broadcast) and (i, k)
-// (coalesced 128-bit) pair records.  Per-pair dE/dr^2 and mask-weighted
-// triple energies accumulate in shared memory (SMEM, n <= 234) and are
-// flushed once per CTA with FP64 atomics; larger structures accumulate
-// straight into global memory.
+// (j, k) pair record in registers and read the (i, j) (broadcast) and (i, k)
+// (coalesced 128-bit) records.  A pair record holds r^2, 1/r,
+// alp/3 log2(R0/r) and sqrt(C6(q=0)), so the damping is one exp2 and C9 two
+// products.  Per-pair dE/d(r^2) and mask-weighted triple energies
+// accumulate in shared memory (SMEM, n <= 234) without the s9 factor, which
+// is applied once when a CTA flushes them (FP32 global atomics, both
+// triangle halves); larger structures accumulate straight into global
+// memory.
 template <bool SMEM, bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     atm_mixed_kernel(Ctx c) {
@@ -347,12 +355,14 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   }
   const int *Zb = c.w.z + (size_t)b * N;
   const float4 *T = c.w.ptf + (size_t)b * N * N;
-  const float2 *Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
-  const float cut = c.pf.cut3;
+  const float4 *Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
+  const float cut2 = c.pf.cut3 * c.pf.cut3;
   const float alp3 = c.pf.alp3;
   const float s9 = c.pf.s9;
+  const float s9m = SMEM ? 1.f : s9;  // SMEM: s9 is applied at the flush
   const bool weighted = c.weights != nullptr;
   const float *W = c.w.w32 + (size_t)b * N;
+  const size_t step = (size_t)K * N;
   float g_s9 = 0.f, g_alp = 0.f, g_a1 = 0.f, g_a2 = 0.f;
   int task = 0;
   for (int j = 1; j < n - 1; ++j) {
@@ -360,68 +370,77 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
       if (task % nwarps != warp || Zb[j] == 0) continue;
       const int k = kc + lane;
       const bool kok = k < n && Zb[k] != 0;
-      const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(1e30f, 0.f, 0.f, 0.f);
-      const float rjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
-      const float zjk = rjk * rjk;
-      const float mjk = rjk <= cut ? 1.f : 0.f;
-      float2 dajk = make_float2(0.f, 0.f);
+      const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+      const float zjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
+      const bool mjk = kok && zjk <= cut2;
+      float4 dajk = make_float4(0.f, 0.f, 0.f, 0.f);
       if (PGRAD && kok) dajk = Tda[(size_t)j * N + k];
       const float wj = W[j];
-      const float wk = kok ? W[k] : 1.f;
-      float Sjk = 0.f, Pjk = 0.f;
-      Acc32 Ej, Ek;
-      for (int i = cta; i < j; i += K) {
+      const float wk = kok ? W[k] : 0.f;
+      float Sjk = 0.f, Pjk = 0.f, Ej = 0.f, Ek = 0.f;
+      const float4 *Tij = T + (size_t)cta * N + j;
+      const float4 *Tik = T + (size_t)cta * N + (kok ? k : j);
+      for (int i = cta; i < j; i += K, Tij += step, Tik += step) {
         if (Zb[i] == 0) continue;
-        const float4 pij = T[(size_t)i * N + j];
-        float sij = 0.f, pij_e = 0.f, ei = 0.f;
+        const float4 pij = *Tij;
+        float sij = 0.f, pe = 0.f, ei = 0.f;
         if (kok) {
-          const float4 pik = T[(size_t)i * N + k];
-          const float mij = pij.x <= cut ? 1.f : 0.f, mik = pik.x <= cut ? 1.f : 0.f;
-          const float mi = mjk * (mij + mik);
-          const float mj = mik * (mij + mjk);
-          const float mk = mij * (mik + mjk);
-          if (mi + mj + mk > 0.f) {
-            const float x = pij.x * pij.x, y = pik.x * pik.x, z = zjk;
-            const float ir1 = pij.y * pik.y * irjk;
+          const float4 pik = *Tik;
+          const bool mij = pij.x <= cut2, mik = pik.x <= cut2;
+          if ((int)mij + (int)mik + (int)mjk >= 2) {
+            const float x = pij.x, y = pik.x, z = zjk;
+            const float ir1 = pij.y * irjk * pik.y;
             const float ir2 = ir1 * ir1;
             const float ir3 = ir1 * ir2;
-            const float A = x + z - y, Bv = x - z + y, Cv = -x + z + y;
+            const float u = x - y, v = x + y;
+            const float A = u + z, Bv = v - z, Cv = z - u;
             const float sfac = A * Bv * Cv;
             const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-            const float Lsum = pij.z + pik.z + Ljk;
-            const float ta = __expf(alp3 * Lsum);
+            const float ta = exp2f(pij.z + pik.z + Ljk);
             const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
             const float c9 = pij.w * pik.w * cjk;
-            const float e = s9 * c9 * fd * ang;
-            const float sixth = e * (1.0f / 6.0f);
-            ei = sixth * mi;
-            Ej.add(sixth * mj);
-            Ek.add(sixth * mk);
+            const float eu = c9 * fd * ang;  // triple energy without s9
+            const float e = s9m * eu;
+            float wgt;
+            if (mij & mik & mjk) {
+              const float third = e * (1.0f / 3.0f);
+              ei = third;
+              Ej += third;
+              Ek += third;
+              wgt = ((weighted ? W[i] : 1.f) + wj + wk) * (1.0f / 3.0f);
+            } else {
+              const float fij = mij, fik = mik, fjk = mjk;
+              const float mi = fjk * (fij + fik), mj = fik * (fij + fjk), mk = fij * (fik + fjk);
+              const float sixth = e * (1.0f / 6.0f);
+              ei = sixth * mi;
+              Ej += sixth * mj;
+              Ek += sixth * mk;
+              wgt = ((weighted ? W[i] : 1.f) * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
+            }
             if (GRAD) {
-              const float wi = weighted ? W[i] : 1.f;
-              const float wgt = (wi * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
-              const float Kc = s9 * c9;
-              const float dfl = 6.0f * alp3 * ta * fd * fd;
-              const float Q = -(5.0f * ang - 2.0f * ir3);
-              const float U = Kc * fd * 0.375f * ir2 * ir3;
-              const float V = 0.5f * Kc * (fd * Q + ang * dfl);
+              const float kc9 = s9m * c9;
+              const float dfl = alp3 * fd * (1.0f - fd);  // = 6 alp/3 ta fd^2
+              const float Q = 2.0f * ir3 - 5.0f * ang;
+              const float U = 0.375f * kc9 * fd * ir2 * ir3;
+              const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
               const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
               const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
-              const float dey = fmaf(U, -BC + AC + AB, V * pik.y * pik.y);
-              const float dez = fmaf(U, BC - AC + AB, V * irjk * irjk);
+              const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
+              const float dez = fmaf(U, BC + AB - AC, V * irjk * irjk);
               sij = wgt * dex;
               Sjk = fmaf(wgt, dez, Sjk);
               const float we = wgt * e;
-              pij_e = we;
+              pe = we;
               Pjk += we;
               acc.pair(i, k, wgt * dey, we);
               if (PGRAD) {
-                const float dfdL = -6.0f * fd * fd * ta;
-                g_s9 += wgt * c9 * fd * ang;
-                g_alp += wgt * s9 * c9 * ang * dfdL * Lsum * (1.0f / 3.0f);
-                const float dfa = wgt * s9 * c9 * ang * dfdL * alp3;
-                const float2 daij = Tda[(size_t)i * N + j];
-                const float2 daik = Tda[(size_t)i * N + k];
+                const float4 daij = Tda[(size_t)i * N + j];
+                const float4 daik = Tda[(size_t)i * N + k];
+                const float lsum = daij.z + daik.z + dajk.z;
+                const float dfd = -fd * (1.0f - fd);  // d fd / d(alp/3 sum log(R0/r))
+                g_s9 += wgt * eu;
+                g_alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
+                const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
                 g_a1 += dfa * (daij.x + daik.x + dajk.x);
                 g_a2 += dfa * (daij.y + daik.y + dajk.y);
               }
@@ -431,19 +450,18 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
         // (i, j) and E_i: one value per warp
         if (GRAD) {
           sij = warp_sumf(sij);
-          pij_e = warp_sumf(pij_e);
+          pe = warp_sumf(pe);
         }
         ei = warp_sumf(ei);
         if (lane == 0) {
           if (ei != 0.f) acc.energy(i, ei);
-          if (GRAD && (sij != 0.f || pij_e != 0.f)) acc.pair(i, j, sij, pij_e);
+          if (GRAD && (sij != 0.f || pe != 0.f)) acc.pair(i, j, sij, pe);
         }
       }
       if (GRAD && kok && (Sjk != 0.f || Pjk != 0.f)) acc.pair(j, k, Sjk, Pjk);
-      const float ej = warp_sumf(Ej.hi) + warp_sumf(Ej.lo);
+      const float ej = warp_sumf(Ej);
       if (lane == 0 && ej != 0.f) acc.energy(j, ej);
-      const float ek = Ek.hi + Ek.lo;
-      if (kok && ek != 0.f) acc.energy(k, ek);
+      if (kok && Ek != 0.f) acc.energy(k, Ek);
     }
   }
   if (PGRAD) {
@@ -464,17 +482,19 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
       for (int k = j + 1 + lane; k < n; k += 32) {
         const int t = tri_u(j, k, n);
         if (GRAD) {
-          const float sv = acc.sS[t], pv = acc.sP[t];
+          const float sv = acc.sS[t] * s9, pv = acc.sP[t] * s9;
           if (sv != 0.f || pv != 0.f) {
-            const size_t o = ((size_t)b * N + j) * N + k;
-            atomicAdd(&c.w.prS32[o], sv);
-            atomicAdd(&c.w.prP32[o], pv);
+            const size_t base = (size_t)b * N * N;
+            atomicAdd(&c.w.prS32[base + (size_t)j * N + k], sv);
+            atomicAdd(&c.w.prP32[base + (size_t)j * N + k], pv);
+            atomicAdd(&c.w.prS32[base + (size_t)k * N + j], sv);
+            atomicAdd(&c.w.prP32[base + (size_t)k * N + j], pv);
           }
         }
       }
     }
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
-      const float ev = acc.sE[x];
+      const float ev = acc.sE[x] * s9;
       if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);  // once per atom
     }
   }
@@ -514,8 +534,7 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
     for (int y = lane; y < n; y += 32) {
       const size_t ay = (size_t)b * N + y;
       if (y == x || c.w.z[ay] == 0 || c.w.slot[ay] != s) continue;
-      const int lo = min(x, y), hi = max(x, y);
-      const size_t o = base + (size_t)lo * N + hi;
+      const size_t o = base + (size_t)x * N + y;
       const float S = c.w.prS32[o];
       const float Pv = c.w.prP32[o];
       const float4 py = P[y];
