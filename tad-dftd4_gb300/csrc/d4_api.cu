@@ -104,7 +104,7 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
           (float)pp.a2,        (float)pp.s9,         (float)(pp.alp / 3.0),
           (float)pp.cut_disp2, (float)pp.cut_disp3,  (float)pp.cut_cn, (float)pp.cut_cn_eeq,
           (float)pp.kcn,       (float)pp.k4,         (float)pp.k5,     (float)pp.k6,
-          (float)pp.cn_eeq_max};
+          (float)pp.cn_eeq_max, (float)cfg->wf,        (float)cfg->ga};
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   if (flags & D4_FLAG_MIXED)
     d4::launch_mixed(c, st);

@@ -11,6 +11,8 @@ namespace d4 {
 constexpr int NREF = D4_NREF;
 constexpr int NFREQ = D4_NFREQ;
 constexpr int MAX_ELEM_ID = 128;  // element ids are < 128 in every table
+constexpr int ERF_TAB = 1537;     // erf table nodes k / 256, k <= 1536 (x0 <= 6)
+constexpr float ERF_SCALE = 256.f;
 constexpr double THOPI = 3.0 / 3.141592653589793238462643383279502884197;  // utils.py:50
 constexpr double SQRT_2_OVER_PI = 0.79788456080286535587989211986876;
 constexpr double INV_SQRT_PI = 0.56418958354775628694807945156077;
@@ -63,10 +65,20 @@ struct Workspace {
   float4 *adj32;    // [B*N] (dE/dCN, dE/dCN_EEQ, q, EEQ adjoint w) in FP32
   float *prS32;     // [B*N*N] ATM dE/d(r^2), FP32 accumulation
   float *prP32;     // [B*N*N] ATM weighted triple energies, FP32 accumulation
-  double *eeq_A64;  // [B*N*N] dense FP64 EEQ matrix of the real atoms
+  float *eeq_hi;    // [B*N*N] dense EEQ matrix of the real atoms (compact order) as the
+  float *eeq_lo;    //         double-float hi + lo
+  int *ridx;        // [B*N] atom index of the k-th real atom
+  int *n_real;      // [B] real atoms
+  float4 *pos32lo;  // [B*N] low parts of the positions: pos32 + pos32lo = r - r_first
+  float4 *erf_tab;  // [ERF_TAB] (erf(x0) hi, lo, 2/sqrt(pi) exp(-x0^2) hi, lo), x0 = k/256
+  float2 *igam;     // [MAX_ELEM_ID^2] 1/sqrt(rad_a^2 + rad_b^2) as double-float
+  float2 *eeq_diag; // [MAX_ELEM_ID] eta + sqrt(2/pi)/rad as double-float
   float *A32;       // [B*S*23*N] (transposed: atoms contiguous per frequency)
   float *A032;      // [B*S*23*N]
   float *dA32;      // [B*N*S*23*3] (dA/dCN, dA/dq, dA0/dCN) per atom, slot, frequency
+  float *alpha32;   // [MAX_ELEM_ID*7*23] reference polarisabilities
+  float4 *ref32;    // [MAX_ELEM_ID*7] (refcovcn, refq + zeff, Gaussians, zeta at q = 0)
+  float2 *el32;     // [MAX_ELEM_ID] (zeff, gam * gc)
   float *G32;       // [B*N*S*23] dE/dA
   float *G032;      // [B*N*S*23] dE/dA0
   float4 *ptf;      // [B*N*N] (r^2, 1/r, alp/3 log2(R0/r), sqrt(C6(q=0)))
@@ -111,13 +123,13 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.dEdcnq = (double *)take(8 * BN);
   w.e3 = (double *)take(8 * BN);
   w.pgrad = (double *)take(8 * 8 * B);
-  w.A = (double *)take(8 * BNS23);
-  w.A0 = (double *)take(8 * BNS23);
-  w.dA_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
-  w.dA_dq = grad ? (double *)take(8 * BNS23) : nullptr;
-  w.dA0_dcn = grad ? (double *)take(8 * BNS23) : nullptr;
-  w.G = grad ? (double *)take(8 * BNS23) : nullptr;
-  w.G0 = grad ? (double *)take(8 * BNS23) : nullptr;
+  w.A = mixed ? nullptr : (double *)take(8 * BNS23);
+  w.A0 = mixed ? nullptr : (double *)take(8 * BNS23);
+  w.dA_dcn = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
+  w.dA_dq = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
+  w.dA0_dcn = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
+  w.G = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
+  w.G0 = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
   w.pr_r = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_ir = mixed ? nullptr : (double *)take(8 * BNN);
   w.pr_L = mixed ? nullptr : (double *)take(8 * BNN);
@@ -137,10 +149,20 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.adj32 = (float4 *)take(16 * BN);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.prP32 = grad ? (float *)take(4 * BNN) : nullptr;
-    w.eeq_A64 = (double *)take(8 * BNN);
+    w.eeq_hi = (float *)take(4 * BNN);
+    w.eeq_lo = (float *)take(4 * BNN);
+    w.ridx = (int *)take(sizeof(int) * BN);
+    w.n_real = (int *)take(sizeof(int) * B);
+    w.pos32lo = (float4 *)take(16 * BN);
+    w.erf_tab = (float4 *)take(16 * (size_t)ERF_TAB);
+    w.igam = (float2 *)take(8 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
+    w.eeq_diag = (float2 *)take(8 * (size_t)MAX_ELEM_ID);
     w.A32 = (float *)take(4 * BNS23);
     w.A032 = (float *)take(4 * BNS23);
     w.dA32 = grad ? (float *)take(4 * 3 * BNS23) : nullptr;
+    w.alpha32 = (float *)take(4 * (size_t)MAX_ELEM_ID * NREF * NFREQ);
+    w.ref32 = (float4 *)take(16 * (size_t)MAX_ELEM_ID * NREF);
+    w.el32 = (float2 *)take(8 * (size_t)MAX_ELEM_ID);
     w.G32 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.G032 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.ptf = (float4 *)take(16 * BNN);
@@ -156,6 +178,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
 struct ParamsF {
   float s6, s8, s10, a1, a2, s9, alp3;
   float cut2, cut3, cut_cn, cut_q, kcn, k4, k5, k6, cn_max;
+  float wf, ga;  // model weighting factor and charge-scaling height
 };
 
 // Everything a kernel needs, passed by value.
@@ -270,6 +293,95 @@ __device__ __forceinline__ Acc32 warp_sum_acc(Acc32 a) {
 }
 
 // Real atoms of structure b compacted into s_idx[0..m).  Returns m.
+
+// ---------------------------------------------------------------- double-float
+
+// A double-float value is the unevaluated sum hi + lo of two floats with
+// |lo| <= ulp(hi) / 2: about 48 significant bits on the FP32 pipe.  Built
+// from the error-free transformations TwoSum (Knuth), FastTwoSum (Dekker,
+// |a| >= |b|) and the FMA product error fma(a, b, -a b).
+struct dfl {
+  float hi, lo;
+};
+
+__device__ __forceinline__ dfl df_two_sum(float a, float b) {
+  const float s = a + b;
+  const float bb = s - a;
+  return {s, (a - (s - bb)) + (b - bb)};
+}
+
+__device__ __forceinline__ dfl df_fast(float a, float b) {
+  const float s = a + b;
+  return {s, b - (s - a)};
+}
+
+__device__ __forceinline__ dfl df_add(dfl a, dfl b) {
+  const dfl s = df_two_sum(a.hi, b.hi);
+  return df_fast(s.hi, s.lo + (a.lo + b.lo));
+}
+
+__device__ __forceinline__ dfl df_neg(dfl a) { return {-a.hi, -a.lo}; }
+
+__device__ __forceinline__ dfl df_mul(dfl a, dfl b) {
+  const float p = a.hi * b.hi;
+  float e = fmaf(a.hi, b.hi, -p);
+  e = fmaf(a.hi, b.lo, fmaf(a.lo, b.hi, e));
+  return df_fast(p, e);
+}
+
+__device__ __forceinline__ dfl df_sq(dfl a) {
+  const float p = a.hi * a.hi;
+  const float e = fmaf(2.f * a.hi, a.lo, fmaf(a.hi, a.hi, -p));
+  return df_fast(p, e);
+}
+
+__device__ __forceinline__ dfl df_from(double v) {
+  const float h = (float)v;
+  return {h, (float)(v - (double)h)};
+}
+
+__device__ __forceinline__ double df_to_double(dfl a) { return (double)a.hi + (double)a.lo; }
+
+// 1/sqrt(a), a > 0 and normal: the FP32 estimate y and one Newton step
+// y (1 + (1 - a y^2) / 2) whose residual 1 - a y^2 is formed in double-float
+// (y^2 is exact as yy + yye; 1 - t.hi is exact since t.hi is within 2^-21
+// of 1).  The relative error goes from ~2^-22 to ~2^-43.
+__device__ __forceinline__ dfl df_rsqrt(dfl a) {
+  const float y = rsqrtf(a.hi);
+  const float yy = y * y;
+  const dfl t = df_mul(a, dfl{yy, fmaf(y, y, -yy)});
+  const float e = (1.0f - t.hi) - t.lo;
+  return df_fast(y, 0.5f * y * e);
+}
+
+// erf(x) for x >= 0 in double-float, by Taylor expansion around the nearest
+// node x0 = k / 256 (|h| = |x - x0| <= 1/512):
+//   erf(x0 + h) = erf(x0) + D [h - x0 h^2 + (2 x0^2 - 1)/3 h^3
+//                 - x0 (2 x0^2 - 3)/6 h^4 + (4 x0^4 - 12 x0^2 + 3)/30 h^5 + ...]
+// with D = 2/sqrt(pi) exp(-x0^2) (the n-th derivative of erf is D times a
+// Hermite polynomial).  erf(x0) and D come from the table as double-floats,
+// D h is formed in double-float, the h^2 tail (|tail| < 2e-6) in FP32; the
+// omitted h^6 term is below 1e-15.  Absolute error about 5e-13; erf = 1 from
+// x = 6 on (erfc(6) = 2e-17).
+__device__ __forceinline__ dfl df_erf(dfl x, const float4 *tab) {
+  if (x.hi >= 6.0f) return {1.0f, 0.0f};
+  // clamped: a NaN argument (coincident atoms) must not index outside the table
+  const int k = min(max(__float2int_rn(x.hi * ERF_SCALE), 0), ERF_TAB - 1);
+  const float x0 = (float)k * (1.0f / ERF_SCALE);
+  const float hh = x.hi - x0;  // exact (Sterbenz)
+  const float4 t = tab[k];
+  const float p = t.z * hh;
+  const float e = fmaf(t.z, x.lo, fmaf(t.w, hh, fmaf(t.z, hh, -p)));
+  const float h = hh + x.lo;
+  const float x02 = x0 * x0;
+  const float c3 = (2.f * x02 - 1.f) * (1.f / 3.f);
+  const float c4 = -x0 * (2.f * x02 - 3.f) * (1.f / 6.f);
+  const float c5 = (4.f * x02 * x02 - 12.f * x02 + 3.f) * (1.f / 30.f);
+  const float tail = t.z * h * h * fmaf(h, fmaf(h, fmaf(h, c5, c4), c3), -x0);
+  const dfl s = df_two_sum(t.x, p);
+  return df_fast(s.hi, s.lo + (t.y + e + tail));
+}
+
 __device__ inline int compact_real_atoms(const Ctx &c, int b, int n, int *s_idx, int *s_tmp) {
   // serial prefix by warp 0 is enough for n <= a few thousand
   if (threadIdx.x < 32) {

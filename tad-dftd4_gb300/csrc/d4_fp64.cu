@@ -81,12 +81,17 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
     c.w.e3[a] = 0.0;
     if (ok) {
       const double *p = c.positions + 3 * a;
-      c.w.pos32[a] = make_float4((float)(p[0] - p0[0]), (float)(p[1] - p0[1]),
-                                 (float)(p[2] - p0[2]), (float)sqrt(atom_r4r2(c, a, z)));
+      const double dx = p[0] - p0[0], dy = p[1] - p0[1], dz = p[2] - p0[2];
+      c.w.pos32[a] = make_float4((float)dx, (float)dy, (float)dz, (float)sqrt(atom_r4r2(c, a, z)));
+      if (c.w.pos32lo)
+        c.w.pos32lo[a] = make_float4((float)(dx - (double)(float)dx),
+                                     (float)(dy - (double)(float)dy),
+                                     (float)(dz - (double)(float)dz), 0.f);
       c.w.aux32[a] = make_float4((float)c.tab.cov_d3[z], (float)c.tab.en[z],
                                  (float)c.tab.eeq_rad[z], 0.f);
     } else {
       c.w.pos32[a] = make_float4(0.f, 0.f, 0.f, 0.f);
+      if (c.w.pos32lo) c.w.pos32lo[a] = make_float4(0.f, 0.f, 0.f, 0.f);
       c.w.aux32[a] = make_float4(1.f, 0.f, 1.f, 0.f);
     }
   }
@@ -98,10 +103,12 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
       const int64_t z = i < N ? Z[i] : 0;
       const bool real = i < N && z > 0 && z < c.tab.n_ref_elem && z < MAX_ELEM_ID;
       const unsigned mask = __ballot_sync(0xffffffffu, real);
-      if (i < N) c.w.cidx[(size_t)b * N + i] =
-          real ? base + __popc(mask & ((1u << threadIdx.x) - 1u)) : -1;
+      const int k = base + __popc(mask & ((1u << threadIdx.x) - 1u));
+      if (i < N) c.w.cidx[(size_t)b * N + i] = real ? k : -1;
+      if (real && c.w.ridx) c.w.ridx[(size_t)b * N + k] = i;
       base += __popc(mask);
     }
+    if (threadIdx.x == 0 && c.w.n_real) c.w.n_real[b] = base;
   }
   if (threadIdx.x < 8) c.w.pgrad[b * 8 + threadIdx.x] = 0.0;
   if (b == 0 && threadIdx.x < NFREQ)

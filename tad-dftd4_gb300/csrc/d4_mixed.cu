@@ -1,11 +1,10 @@
-// Precision form of the D4 path: FP32 pair and triple arithmetic with
-// compensated accumulation, FP32 Cholesky of the EEQ matrix recovered by FP64
-// iterative refinement, FP64 for coordination numbers, reference weights,
-// residuals and the final per-atom / per-structure reductions.
+// Precision form of the D4 path: FP32 coordination numbers, reference
+// weights, pair and triple arithmetic with compensated accumulation, FP32
+// Cholesky of the EEQ matrix recovered by FP64 iterative refinement; FP64 for
+// the EEQ matrix and residuals and the final per-atom / per-structure
+// reductions.
 //
-// Shared stages (prep, CN, weights, finish) are the FP64 ones.  The CN kernel
-// skips pairs whose counting function is exactly zero in FP64, so it costs
-// little; the weights are per atom.
+// Shared stages (prep, finish) are the FP64 ones.
 #include <float.h>
 
 #include "d4_common.cuh"
@@ -20,31 +19,60 @@ constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
 constexpr int ATM_THREADS = 1024;       // 32 warps: one CTA per SM (shared memory)
 constexpr int ATM_THREADS_PGRAD = 512;  // the parameter-gradient variant needs more registers
 
-// ---------------------------------------------------------------- convert
+// ---------------------------------------------------------------- weights
 
-// FP32 copies of the weighted polarisabilities, transposed to
-// [b][slot][frequency][atom] so that lanes over partner atoms load
-// consecutive addresses.
-__global__ void mixed_convert_kernel(Ctx c) {
-  const size_t nA = (size_t)c.B * c.N * c.S * NFREQ;
-  const size_t stride = (size_t)gridDim.x * blockDim.x;
-  const int N = c.N, S = c.S;
-  for (size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x; t < nA; t += stride) {
-    // t indexes the transposed layout: ((b * S + s) * 23 + w) * N + i
-    const int i = (int)(t % N);
-    const size_t r = t / N;
-    const int w = (int)(r % NFREQ);
-    const size_t bs = r / NFREQ;
-    const int s = (int)(bs % S);
-    const size_t b = bs / S;
-    const size_t src = (((b * N + i) * S) + s) * NFREQ + w;
-    c.w.A32[t] = (float)c.w.A[src];
-    c.w.A032[t] = (float)c.w.A0[src];
-    if (c.w.dA32) {
-      c.w.dA32[3 * src] = (float)c.w.dA_dcn[src];
-      c.w.dA32[3 * src + 1] = (float)c.w.dA_dq[src];
-      c.w.dA32[3 * src + 2] = (float)c.w.dA0_dcn[src];
+// threads of tables32_kernel: the largest of its tables, 128 x 7 x 23
+constexpr int TABLES32_THREADS = ((MAX_ELEM_ID * NREF * NFREQ + 255) / 256) * 256;
+static_assert(TABLES32_THREADS >= MAX_ELEM_ID * MAX_ELEM_ID && TABLES32_THREADS >= ERF_TAB,
+              "tables32_kernel covers every table");
+
+// FP32 tables of the precision form, rebuilt on every call (20k values):
+// alpha32 [128][7][23]; ref32 [128][7] = (refcovcn, refq + zeff, Gaussians
+// per reference, zeta at q = 0 evaluated in FP64); el32 [128] = (zeff,
+// gam * gc); the erf nodes and 1/sqrt(rad_a^2 + rad_b^2) per element pair as
+// double-floats for the EEQ matrix.  Rows of elements without references are
+// zero.
+__global__ void tables32_kernel(Ctx c) {
+  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+  const int nz = c.tab.n_ref_elem < MAX_ELEM_ID ? c.tab.n_ref_elem : MAX_ELEM_ID;
+  if (t < MAX_ELEM_ID * NREF * NFREQ) {
+    const int z = t / (NREF * NFREQ);
+    c.w.alpha32[t] = z < nz ? (float)c.tab.alpha[t] : 0.f;
+  }
+  if (t < MAX_ELEM_ID * NREF) {
+    const int z = t / NREF;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (z < nz && z < c.tab.n_elem) {
+      const double zeff = (double)c.tab.zeff[z];
+      const double qref = c.tab.refq[t] + zeff;
+      double z0, dz0;
+      zeta_and_deriv(c.tab.gam[z] * c.cfg.gc, qref, zeff, c.cfg.ga, DBL_EPSILON, &z0, &dz0);
+      v = make_float4((float)c.tab.refcovcn[t], (float)qref, (float)c.tab.refc[t], (float)z0);
     }
+    c.w.ref32[t] = v;
+  }
+  if (t < MAX_ELEM_ID) {
+    float2 e = make_float2(0.f, 0.f);
+    if (t < nz && t < c.tab.n_elem)
+      e = make_float2((float)c.tab.zeff[t], (float)(c.tab.gam[t] * c.cfg.gc));
+    c.w.el32[t] = e;
+    dfl d = {0.f, 0.f};
+    if (t < c.tab.n_elem) d = df_from(c.tab.eeq_eta[t] + SQRT_2_OVER_PI / c.tab.eeq_rad[t]);
+    c.w.eeq_diag[t] = make_float2(d.hi, d.lo);
+  }
+  if (t < ERF_TAB) {  // nodes of the double-float erf
+    const double x0 = (double)t / (double)ERF_SCALE;
+    const dfl e = df_from(erf(x0)), d = df_from(2.0 / sqrt(M_PI) * exp(-x0 * x0));
+    c.w.erf_tab[t] = make_float4(e.hi, e.lo, d.hi, d.lo);
+  }
+  if (t < MAX_ELEM_ID * MAX_ELEM_ID) {  // 1 / sqrt(rad_a^2 + rad_b^2)
+    const int za = t / MAX_ELEM_ID, zb = t % MAX_ELEM_ID;
+    dfl g = {0.f, 0.f};
+    if (za < c.tab.n_elem && zb < c.tab.n_elem) {
+      const double ra = c.tab.eeq_rad[za], rb = c.tab.eeq_rad[zb];
+      g = df_from(1.0 / sqrt(ra * ra + rb * rb));
+    }
+    c.w.igam[t] = make_float2(g.hi, g.lo);
   }
 }
 
@@ -52,6 +80,134 @@ __global__ void mixed_convert_kernel(Ctx c) {
 __device__ __forceinline__ size_t a32_index(int b, int i, int s, int w, int N, int S) {
   return (((size_t)b * S + s) * NFREQ + w) * N + i;
 }
+
+// Charge-scaled Gaussian reference weights and the weighted polarisabilities
+// A_i(w) = sum_r gw_ir zeta_ir alpha_{Z_i r}(w) at q and at q = 0, with their
+// CN / q derivatives, in FP32 (model/d4.py:103-228, model/d4s.py:109-248).
+// One thread per (atom, slot); lanes over consecutive atoms, so that the
+// transposed A32 / A032 rows are stored coalesced.
+//
+// The Gaussian exponents c k dcn_r^2 are taken relative to the nearest
+// reference (smallest c dcn^2), whose first Gaussian becomes exp(0) = 1:
+// the normalised weight is the same as the reference's e_r / sum e_r and the
+// norm cannot underflow.  Where the
+// reference's FP64 norm underflows (every |dcn| > 11) it falls back to the
+// reference of largest refcovcn (model/d4.py:209-217), which is then also
+// the nearest one, so both give the same weights.
+__global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int S = c.S, N = c.N;
+  const int s = blockIdx.x % S;
+  const int i = (blockIdx.x / S) * blockDim.x + threadIdx.x;
+  if (i >= N) return;
+  const size_t ai = (size_t)b * N + i;
+  const int zi = c.w.z[ai];
+  const bool grad = c.w.dA32 != nullptr;
+  const bool live = i < c.w.n_eff[b] && zi != 0 && s < c.w.n_slots[b];
+  float gq[NREF], g0[NREF], dgc[NREF], dgq[NREF], dg0[NREF];
+#pragma unroll
+  for (int r = 0; r < NREF; ++r) gq[r] = g0[r] = dgc[r] = dgq[r] = dg0[r] = 0.f;
+  if (live) {
+    const bool d4s = c.cfg.kind == D4_MODEL_D4S;
+    // FP64 set-up per reference (a few FP64 instructions per atom): the CN
+    // offsets, the exponent differences to the nearest reference and q - q_ref
+    // are rounded to FP32 only after the cancellations.
+    const double cn = c.w.cn[ai];
+    const double q = c.w.q[ai];
+    const double wf = d4s ? c.tab.wfpair[zi * c.tab.n_elem + c.w.slot_elem[b * MAX_ELEM_ID + s]]
+                          : c.cfg.wf;
+    const float4 *R = c.w.ref32 + zi * NREF;
+    float4 rv[NREF];
+    float dcn[NREF], cf[NREF], dq[NREF];
+    double y64[NREF];
+    double best = INFINITY;
+#pragma unroll
+    for (int r = 0; r < NREF; ++r) {
+      rv[r] = R[r];
+      const int refc = (int)rv[r].z;
+      const double d = cn - c.tab.refcovcn[zi * NREF + r];
+      // D4: wf for 1 or 3 Gaussians, 1 otherwise; D4S: wf
+      const double cfr = (d4s || refc == 1 || refc == 3) ? wf : 1.0;
+      y64[r] = cfr * d * d;
+      dcn[r] = (float)d;
+      cf[r] = (float)cfr;
+      dq[r] = (float)(q - c.tab.refq[zi * NREF + r]);
+      if (refc > 0) best = fmin(best, y64[r]);
+    }
+    if (best < INFINITY) {
+      float e[NREF], de[NREF];
+      float norm = 0.f, dnorm = 0.f;
+#pragma unroll
+      for (int r = 0; r < NREF; ++r) {
+        e[r] = de[r] = 0.f;
+        const int refc = (int)rv[r].z;
+        if (refc <= 0) continue;
+        const float x1 = (float)(y64[r] - best);  // >= 0, 0 for the nearest reference
+        const float y = (float)y64[r];
+        const float t1 = expf(-x1);
+        float ee = t1, dd = t1;
+        if (refc == 3) {
+          const float t2 = expf(-(y + x1)), t3 = expf(-(2.f * y + x1));
+          ee = t1 + t2 + t3;
+          dd = t1 + 2.f * t2 + 3.f * t3;
+        }
+        e[r] = ee;
+        de[r] = -2.f * cf[r] * dcn[r] * dd;
+        norm += ee;
+        dnorm += de[r];
+      }
+      const float inorm = 1.0f / norm;
+      const float2 el = c.w.el32[zi];
+      const float qmod = (float)q + el.x;
+      const float ga = c.pf.ga, gam = el.y;
+#pragma unroll
+      for (int r = 0; r < NREF; ++r) {
+        if ((int)rv[r].z <= 0) continue;
+        const float gw = e[r] * inorm;
+        const float dgw = (de[r] - gw * dnorm) * inorm;
+        float z, dz;
+        if (qmod > 0.f) {
+          // model/base.py:308-335 as exp(-ga expm1(gam (q - q_ref) / (q + zeff)))
+          const float em1 = expm1f(gam * dq[r] / qmod);
+          z = expf(-ga * em1);
+          dz = -ga * z * (1.f + em1) * gam * rv[r].y / (qmod * qmod);
+        } else {
+          z = expf(ga);
+          dz = 0.f;
+        }
+        const float z0 = rv[r].w;
+        gq[r] = z * gw;
+        g0[r] = z0 * gw;
+        dgc[r] = z * dgw;
+        dgq[r] = dz * gw;
+        dg0[r] = z0 * dgw;
+      }
+    }
+  }
+  const float *al = c.w.alpha32 + (size_t)zi * NREF * NFREQ;
+  for (int w = 0; w < NFREQ; ++w) {
+    float a = 0.f, a0 = 0.f, da_dcn = 0.f, da_dq = 0.f, da0_dcn = 0.f;
+#pragma unroll
+    for (int r = 0; r < NREF; ++r) {
+      const float v = al[r * NFREQ + w];
+      a = fmaf(gq[r], v, a);
+      a0 = fmaf(g0[r], v, a0);
+      da_dcn = fmaf(dgc[r], v, da_dcn);
+      da_dq = fmaf(dgq[r], v, da_dq);
+      da0_dcn = fmaf(dg0[r], v, da0_dcn);
+    }
+    const size_t t = a32_index(b, i, s, w, N, S);
+    c.w.A32[t] = a;
+    c.w.A032[t] = a0;
+    if (grad) {
+      float *d = c.w.dA32 + 3 * ((ai * S + s) * NFREQ + w);
+      d[0] = da_dcn;
+      d[1] = da_dq;
+      d[2] = da0_dcn;
+    }
+  }
+}
+
 
 // ---------------------------------------------------------------- CN
 
@@ -638,60 +794,102 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
 
 // ---------------------------------------------------------------- EEQ
 
-// FP64 reciprocal square root: FP32 estimate refined by two Newton steps
-// y <- y (3 - a y^2) / 2 (quadratic convergence: 2^-22 -> 2^-44 -> below
-// one FP64 ulp), for a > 0 in the FP32 range.
-__device__ __forceinline__ double rsqrt_newton(double a) {
-  double y = (double)rsqrtf((float)a);
-  y = y * (1.5 - 0.5 * a * y * y);
-  y = y * (1.5 - 0.5 * a * y * y);
-  return y;
-}
-
-// Dense FP64 EEQ matrix of the real atoms (rows / columns in the order of
-// ``cidx``, leading dimension N).  One thread per lower-triangle entry,
-// mirrored; all structures at once.  erf(x) is exactly 1.0 in FP64 for
-// x > 6.5, where the entry is 1/r.
-__global__ void eeq_build_mixed_kernel(Ctx c) {
-  const int b = blockIdx.y;
+// Dense EEQ Coulomb matrix of the real atoms as the double-float pair of
+// FP32 matrices hi + lo (compact order, leading dimension N), the operator of
+// the FP64-accurate refinement residuals:
+//   A_kl = erf(r_kl / g_kl) / r_kl (k != l),  A_kk = eta + sqrt(2/pi) / rad,
+// g_kl = sqrt(rad_k^2 + rad_l^2) (tad_multicharge's EEQ, restated).  Off the
+// diagonal all of it runs in double-float on the FP32 pipe: positions as
+// pos32 + pos32lo, r^2 from them, 1/r by df_rsqrt, erf by df_erf, with
+// 1/g and the diagonal from per-element tables; no FP64 instruction.
+// Persistent blocks loop over the 32 x 32 tiles of the lower triangles of
+// all structures; a tile and its mirror are both stored coalesced (the
+// mirror through shared memory).
+__global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
+  __shared__ float4 s_erf[ERF_TAB];
+  __shared__ float s_hi[32][33], s_lo[32][33];
+  for (int k = threadIdx.x; k < ERF_TAB; k += blockDim.x) s_erf[k] = c.w.erf_tab[k];
+  __syncthreads();
   const int N = c.N;
-  const int n = c.w.n_eff[b];
-  const size_t t = (size_t)blockIdx.x * blockDim.x + threadIdx.x;
-  if (t >= (size_t)n * (n + 1) / 2) return;
-  int i = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-  while (tri_index(i + 1, 0) <= t) ++i;
-  while (i > 0 && tri_index(i, 0) > t) --i;
-  const int j = (int)(t - tri_index(i, 0));
-  const size_t ai = (size_t)b * N + i, aj = (size_t)b * N + j;
-  const int ci = c.w.cidx[ai], cj = c.w.cidx[aj];
-  if (ci < 0 || cj < 0) return;
-  const int zi = c.w.z[ai], zj = c.w.z[aj];
-  double *A = c.w.eeq_A64 + (size_t)b * N * N;
-  if (i == j) {
-    A[(size_t)ci * N + ci] = c.tab.eeq_eta[zi] + SQRT_2_OVER_PI / c.tab.eeq_rad[zi];
-    return;
+  const int T = (N + 31) / 32;
+  const int tp = T * (T + 1) / 2;
+  const size_t total = (size_t)c.B * tp;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (size_t t = blockIdx.x; t < total; t += gridDim.x) {
+    const int b = (int)(t / tp);
+    const int r = (int)(t % tp);
+    int ti = (int)((sqrtf(8.f * (float)r + 1.f) - 1.f) * 0.5f);
+    while ((ti + 1) * (ti + 2) / 2 <= r) ++ti;
+    while (ti > 0 && ti * (ti + 1) / 2 > r) --ti;
+    const int tj = r - ti * (ti + 1) / 2;
+    const int m = c.w.n_real[b];
+    if (ti * 32 >= m) continue;  // uniform over the block
+    const size_t bN = (size_t)b * N;
+    float *Hi = c.w.eeq_hi + bN * N;
+    float *Lo = c.w.eeq_lo + bN * N;
+    const int l = tj * 32 + tx;
+    int zl = 0;
+    float4 pl = make_float4(0.f, 0.f, 0.f, 0.f), pll = pl;
+    if (l < m) {
+      const int al = c.w.ridx[bN + l];
+      zl = c.w.z[bN + al];
+      pl = c.w.pos32[bN + al];
+      pll = c.w.pos32lo[bN + al];
+    }
+#pragma unroll 1
+    for (int kk = 0; kk < 4; ++kk) {
+      const int rr = ty + 8 * kk;
+      const int k = ti * 32 + rr;
+      dfl v = {0.f, 0.f};
+      if (k < m && l < m) {
+        const int ak = c.w.ridx[bN + k];
+        const int zk = c.w.z[bN + ak];
+        if (k == l) {
+          const float2 d = c.w.eeq_diag[zk];
+          v = dfl{d.x, d.y};
+        } else {
+          const float4 pk = c.w.pos32[bN + ak], pkl = c.w.pos32lo[bN + ak];
+          const dfl dx = df_add(dfl{pk.x, pkl.x}, dfl{-pl.x, -pll.x});
+          const dfl dy = df_add(dfl{pk.y, pkl.y}, dfl{-pl.y, -pll.y});
+          const dfl dz = df_add(dfl{pk.z, pkl.z}, dfl{-pl.z, -pll.z});
+          const dfl r2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+          const dfl ir = df_rsqrt(r2);
+          const float2 g = c.w.igam[zk * MAX_ELEM_ID + zl];
+          const dfl x = df_mul(df_mul(r2, ir), dfl{g.x, g.y});
+          v = df_mul(df_erf(x, s_erf), ir);
+        }
+        Hi[(size_t)k * N + l] = v.hi;
+        Lo[(size_t)k * N + l] = v.lo;
+      }
+      s_hi[rr][tx] = v.hi;
+      s_lo[rr][tx] = v.lo;
+    }
+    if (ti != tj) {
+      __syncthreads();
+#pragma unroll 1
+      for (int kk = 0; kk < 4; ++kk) {
+        const int rr = ty + 8 * kk;
+        const int l2 = tj * 32 + rr, k2 = ti * 32 + tx;
+        if (l2 < m && k2 < m) {
+          Hi[(size_t)l2 * N + k2] = s_hi[tx][rr];
+          Lo[(size_t)l2 * N + k2] = s_lo[tx][rr];
+        }
+      }
+    }
+    __syncthreads();
   }
-  const double *pi = c.positions + 3 * ai, *pj = c.positions + 3 * aj;
-  const double dx = pi[0] - pj[0], dy = pi[1] - pj[1], dz = pi[2] - pj[2];
-  const double r2 = dx * dx + dy * dy + dz * dz;
-  const double ir = rsqrt_newton(r2);
-  const double ra = c.tab.eeq_rad[zi], rb = c.tab.eeq_rad[zj];
-  const double x = r2 * ir * rsqrt_newton(ra * ra + rb * rb);
-  const double v = (x > 6.5 ? 1.0 : erf(x)) * ir;
-  A[(size_t)ci * N + cj] = v;
-  A[(size_t)cj * N + ci] = v;
 }
 
-// Shared-memory layout of the mixed EEQ kernels (in doubles):
-//   idx      int[N]               (N/2 + 1 doubles)
-//   x        double[2N]           solution (two right-hand sides)
-//   rx       double[2N]           FP64 residual
-//   bb       double[2N]           right-hand sides (b, 1) in FP64
-//   vf       float[2N]            FP32 correction (N doubles)
-//   invd     float[N]             reciprocal diagonal of the factor
-//   L        float[N(N+1)/2]      FP32 factor (SMEM only)
-__host__ __device__ inline size_t eeq_mixed_vec_doubles(int N) {
-  return (size_t)(N + 1) / 2 + 1 + 6 * (size_t)N + (size_t)N + (size_t)(N + 1) / 2 + 1;
+// Shared-memory layout of the mixed EEQ kernels (in floats):
+//   idx      int[Nr]          compact index -> atom (Nr = N rounded up to 4)
+//   X        float2[2N]       solution (two right-hand sides), double-float
+//   BB       float2[2N]       right-hand sides (b, 1), double-float
+//   vf       float[2N]        FP32 residual / correction
+//   invd     float[Nr]        reciprocal diagonal of the factor
+//   L        float[N(N+1)/2]  FP32 factor (SMEM only)
+__host__ __device__ inline int eeq_round4(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {
+  return 2 * (size_t)eeq_round4(N) + 10 * (size_t)N;
 }
 
 constexpr int PB = 32;  // panel width of the blocked factorisation and solves
@@ -846,120 +1044,145 @@ __device__ void bwd_solve_blocked(const float *L, const float *invd, float *v, i
 }
 
 constexpr int EEQ_REFINE_MAX = 8;
-constexpr double EEQ_RESIDUAL_TOL = 1e-10;
+constexpr float EEQ_RESIDUAL_TOL = 1e-10f;
 
-// rx = bb - A x for ``nr`` right-hand sides; one warp per row of the dense
-// FP64 matrix (coalesced).  Returns max |rx| over the block.
-__device__ double eeq_residual(const double *A64, const double *x, const double *bb, double *rx,
-                               int m, int N, int nr, double *s_red) {
+// acc + (h + lo) x for a double-float x; acc is left unnormalised (its low
+// part collects the rounding errors; a row has at most a few hundred terms
+// per lane).
+__device__ __forceinline__ dfl df_acc_prod(dfl acc, float h, float lo, float2 x) {
+  const float p = h * x.x;
+  const float e = fmaf(h, x.y, fmaf(lo, x.x, fmaf(h, x.x, -p)));
+  const dfl s = df_two_sum(acc.hi, p);
+  return {s.hi, acc.lo + (s.lo + e)};
+}
+
+__device__ __forceinline__ dfl df_warp_sum(dfl a) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) {
+    const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
+    const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
+    const dfl s = df_two_sum(a.hi, oh);
+    a = df_fast(s.hi, s.lo + (a.lo + ol));
+  }
+  return a;
+}
+
+// Residual r = BB - (hi + lo) X for ``nr`` right-hand sides, in double-float
+// (FP64-accurate, on the FP32 pipe): one warp per row, lanes over columns
+// (coalesced).  r is rounded to FP32 into vf, the right-hand side of the next
+// correction; returns max |r| over the block.
+__device__ float eeq_residual_df(const float *Hi, const float *Lo, const float2 *X,
+                                 const float2 *BB, float *vf, int m, int N, int nr,
+                                 float *s_red) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
-  double mx = 0.0;
+  float mx = 0.f;
   for (int k = warp; k < m; k += nw) {
-    const double *row = A64 + (size_t)k * N;
-    double a0 = 0.0, a1 = 0.0;
+    const float *hr = Hi + (size_t)k * N, *lr = Lo + (size_t)k * N;
+    dfl a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
     for (int l = lane; l < m; l += 32) {
-      const double a = row[l];
-      a0 += a * x[l];
-      if (nr == 2) a1 += a * x[N + l];
+      const float h = hr[l], lo = lr[l];
+      a0 = df_acc_prod(a0, h, lo, X[l]);
+      if (nr == 2) a1 = df_acc_prod(a1, h, lo, X[N + l]);
     }
-    a0 = warp_sum(a0);
-    if (nr == 2) a1 = warp_sum(a1);
+    a0 = df_warp_sum(a0);
+    if (nr == 2) a1 = df_warp_sum(a1);
     if (lane == 0) {
-      const double r0 = bb[k] - a0;
-      rx[k] = r0;
-      mx = fmax(mx, fabs(r0));
+      const dfl r0 = df_add(dfl{BB[k].x, BB[k].y}, df_neg(a0));
+      vf[k] = r0.hi;
+      mx = fmaxf(mx, fabsf(r0.hi));
       if (nr == 2) {
-        const double r1 = bb[N + k] - a1;
-        rx[N + k] = r1;
-        mx = fmax(mx, fabs(r1));
+        const dfl r1 = df_add(dfl{BB[N + k].x, BB[N + k].y}, df_neg(a1));
+        vf[N + k] = r1.hi;
+        mx = fmaxf(mx, fabsf(r1.hi));
       }
     }
   }
   if (lane == 0) s_red[warp] = mx;
   __syncthreads();
   if (threadIdx.x == 0) {
-    double v = 0.0;
-    for (int w = 0; w < nw; ++w) v = fmax(v, s_red[w]);
+    float v = 0.f;
+    for (int w = 0; w < nw; ++w) v = fmaxf(v, s_red[w]);
     s_red[32] = v;
   }
   __syncthreads();
-  const double out = s_red[32];
+  const float out = s_red[32];
   __syncthreads();
   return out;
 }
 
-// FP32 factor + FP64 refinement: x (nr columns) <- A^-1 bb.
-__device__ void eeq_refined_solve(const float *L, const float *invd, const double *A64,
-                                  double *x, double *rx, const double *bb, float *vf, int m,
-                                  int N, int nr, double *s_red) {
+// FP32 factor + double-float refinement: X (nr columns) <- A^-1 BB to an
+// FP64-level residual below 1e-10.
+__device__ void eeq_refined_solve(const float *L, const float *invd, const float *Hi,
+                                  const float *Lo, float2 *X, const float2 *BB, float *vf,
+                                  int m, int N, int nr, float *s_red) {
   for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
-    const int r = t / m, k = t % m;
-    x[r * N + k] = 0.0;
-    rx[r * N + k] = bb[r * N + k];
+    const int o = (t / m) * N + t % m;
+    X[o] = make_float2(0.f, 0.f);
+    vf[o] = BB[o].x;
   }
   __syncthreads();
   for (int it = 0; it < EEQ_REFINE_MAX; ++it) {
-    for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
-      const int r = t / m, k = t % m;
-      vf[r * N + k] = (float)rx[r * N + k];
-    }
-    __syncthreads();
     fwd_solve_blocked(L, invd, vf, N, m, nr);
     bwd_solve_blocked(L, invd, vf, N, m, nr);
     for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
-      const int r = t / m, k = t % m;
-      x[r * N + k] += (double)vf[r * N + k];
+      const int o = (t / m) * N + t % m;
+      const dfl s = df_add(dfl{X[o].x, X[o].y}, dfl{vf[o], 0.f});
+      X[o] = make_float2(s.hi, s.lo);
     }
     __syncthreads();
-    if (eeq_residual(A64, x, bb, rx, m, N, nr, s_red) < EEQ_RESIDUAL_TOL) break;
+    if (eeq_residual_df(Hi, Lo, X, BB, vf, m, N, nr, s_red) < EEQ_RESIDUAL_TOL) break;
   }
 }
 
 template <bool SMEM>
 __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
-  extern __shared__ double s_dyn[];
+  extern __shared__ float4 s_dyn4[];
+  float *s_f = reinterpret_cast<float *>(s_dyn4);
   const int b = blockIdx.x;
   const int N = c.N;
   const int n = c.w.n_eff[b];
   __shared__ int s_m;
-  __shared__ double s_red[33];
-  int *s_idx = reinterpret_cast<int *>(s_dyn);
-  double *x = s_dyn + (N + 1) / 2 + 1;
-  double *rx = x + 2 * N;
-  double *bb = rx + 2 * N;
-  float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  __shared__ float s_red[33];
+  __shared__ double s_lam;
+  const int Nr = eeq_round4(N);
+  int *s_idx = reinterpret_cast<int *>(s_f);
+  float2 *X = reinterpret_cast<float2 *>(s_f + Nr);
+  float2 *BB = X + 2 * N;
+  float *vf = reinterpret_cast<float *>(BB + 2 * N);
   float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
-  float *L = SMEM ? invd + N + 2 : c.w.eeq_L32 + (size_t)b * NN2;
-  const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
+  float *L = SMEM ? invd + Nr : c.w.eeq_L32 + (size_t)b * NN2;
+  const float *Hi = c.w.eeq_hi + (size_t)b * N * N;
+  const float *Lo = c.w.eeq_lo + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
   const int *Zb = c.w.z + (size_t)b * N;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
-  // FP32 copy of the lower triangle, one warp per row
+  // FP32 factor input: the hi part of the lower triangle, one warp per row
   for (int ii = warp; ii < m; ii += nw) {
-    const double *row = A64 + (size_t)ii * N;
+    const float *row = Hi + (size_t)ii * N;
     float *lrow = L + tri_index(ii, 0);
-    for (int jj = lane; jj <= ii; jj += 32) lrow[jj] = (float)row[jj];
+    for (int jj = lane; jj <= ii; jj += 32) lrow[jj] = row[jj];
   }
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const int ia = s_idx[k];
     const int z = Zb[ia];
     const double cq = c.w.cnq[(size_t)b * N + ia];
     const double sq = cq > 0.0 ? sqrt(cq) : 0.0;
-    bb[k] = -c.tab.eeq_chi[z] + c.tab.eeq_kcn[z] * sq;
-    bb[N + k] = 1.0;
+    const dfl bk = df_from(-c.tab.eeq_chi[z] + c.tab.eeq_kcn[z] * sq);
+    BB[k] = make_float2(bk.hi, bk.lo);
+    BB[N + k] = make_float2(1.f, 0.f);
   }
   __syncthreads();
   chol_blocked(L, invd, m, &s_bad);
   if (threadIdx.x == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
-  eeq_refined_solve(L, invd, A64, x, rx, bb, vf, m, N, 2, s_red);
+  eeq_refined_solve(L, invd, Hi, Lo, X, BB, vf, m, N, 2, s_red);
   if (warp == 0) {
     double sx = 0.0, sy = 0.0;
     for (int k = lane; k < m; k += 32) {
-      sx += x[k];
-      sy += x[N + k];
+      sx += (double)X[k].x + (double)X[k].y;
+      sy += (double)X[N + k].x + (double)X[N + k].y;
     }
     sx = warp_sum(sx);
     sy = warp_sum(sy);
@@ -967,11 +1190,11 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
       const double lam = m > 0 ? (sx - c.charge[b]) / sy : 0.0;
       c.w.eeq_sum[2 * b] = sy;
       c.w.eeq_sum[2 * b + 1] = lam;
-      s_red[32] = lam;
+      s_lam = lam;
     }
   }
   __syncthreads();
-  const double lam = s_red[32];
+  const double lam = s_lam;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     c.w.q[(size_t)b * N + i] = 0.0;
     c.w.eeq_y[(size_t)b * N + i] = 0.0;
@@ -979,8 +1202,10 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
   __syncthreads();
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const size_t a = (size_t)b * N + s_idx[k];
-    c.w.q[a] = x[k] - lam * x[N + k];
-    c.w.eeq_y[a] = x[N + k];
+    const double x0 = (double)X[k].x + (double)X[k].y;
+    const double x1 = (double)X[N + k].x + (double)X[N + k].y;
+    c.w.q[a] = x0 - lam * x1;
+    c.w.eeq_y[a] = x1;
   }
   if (SMEM) {
     float *G = c.w.eeq_L32 + (size_t)b * NN2;
@@ -989,39 +1214,44 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
   }
 }
 
-// Adjoint: A u = dE/dq by the FP32 factor + FP64 refinement, w = u - nu y.
+// Adjoint: A u = dE/dq by the FP32 factor + double-float refinement,
+// w = u - nu y.
 __global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
-  extern __shared__ double s_dyn[];
+  extern __shared__ float4 s_dyn4[];
+  float *s_f = reinterpret_cast<float *>(s_dyn4);
   const int b = blockIdx.x;
   const int N = c.N;
   const int n = c.w.n_eff[b];
   __shared__ int s_m;
-  __shared__ double s_red[33];
-  int *s_idx = reinterpret_cast<int *>(s_dyn);
-  double *x = s_dyn + (N + 1) / 2 + 1;
-  double *rx = x + 2 * N;
-  double *bb = rx + 2 * N;
-  float *vf = reinterpret_cast<float *>(bb + 2 * N);
+  __shared__ float s_red[33];
+  __shared__ double s_nu;
+  const int Nr = eeq_round4(N);
+  int *s_idx = reinterpret_cast<int *>(s_f);
+  float2 *X = reinterpret_cast<float2 *>(s_f + Nr);
+  float2 *BB = X + 2 * N;
+  float *vf = reinterpret_cast<float *>(BB + 2 * N);
   float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
   const float *L = c.w.eeq_L32 + (size_t)b * NN2;
-  const double *A64 = c.w.eeq_A64 + (size_t)b * N * N;
+  const float *Hi = c.w.eeq_hi + (size_t)b * N * N;
+  const float *Lo = c.w.eeq_lo + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
-    bb[k] = c.w.dEdq[(size_t)b * N + s_idx[k]];
+    const dfl g = df_from(c.w.dEdq[(size_t)b * N + s_idx[k]]);
+    BB[k] = make_float2(g.hi, g.lo);
     invd[k] = 1.0f / L[tri_index(k, k)];
   }
   __syncthreads();
-  eeq_refined_solve(L, invd, A64, x, rx, bb, vf, m, N, 1, s_red);
+  eeq_refined_solve(L, invd, Hi, Lo, X, BB, vf, m, N, 1, s_red);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     double su = 0.0;
-    for (int k = lane; k < m; k += 32) su += x[k];
+    for (int k = lane; k < m; k += 32) su += (double)X[k].x + (double)X[k].y;
     su = warp_sum(su);
-    if (lane == 0) s_red[32] = m > 0 ? su / c.w.eeq_sum[2 * b] : 0.0;
+    if (lane == 0) s_nu = m > 0 ? su / c.w.eeq_sum[2 * b] : 0.0;
   }
   __syncthreads();
-  const double nu = s_red[32];
+  const double nu = s_nu;
   for (int i = threadIdx.x; i < N; i += blockDim.x) {
     c.w.eeq_w[(size_t)b * N + i] = 0.0;
     c.w.dEdcnq[(size_t)b * N + i] = 0.0;
@@ -1029,7 +1259,7 @@ __global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
   __syncthreads();
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const size_t a = (size_t)b * N + s_idx[k];
-    const double w = x[k] - nu * c.w.eeq_y[a];
+    const double w = (double)X[k].x + (double)X[k].y - nu * c.w.eeq_y[a];
     c.w.eeq_w[a] = w;
     const double cq = c.w.cnq[a];
     const int z = c.w.z[a];
@@ -1041,6 +1271,23 @@ __global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
 }
 
 // ---------------------------------------------------------------- launch
+
+// persistent grid of the EEQ build: 4 blocks per SM, at most one per tile
+static unsigned build_blocks(const Ctx &c) {
+  static int sms[64] = {0};
+  int dev = 0;
+  cudaGetDevice(&dev);
+  int &n = sms[dev & 63];
+  if (n == 0) {
+    int v = 0;
+    cudaDeviceGetAttribute(&v, cudaDevAttrMultiProcessorCount, dev);
+    n = v > 0 ? v : 1;
+  }
+  const size_t T = (size_t)(c.N + 31) / 32;
+  const size_t tiles = (size_t)c.B * T * (T + 1) / 2;
+  const size_t want = (size_t)4 * n;
+  return (unsigned)(tiles < want ? (tiles > 0 ? tiles : 1) : want);
+}
 
 template <bool SMEM, bool GRAD, bool PGRAD>
 static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
@@ -1060,17 +1307,17 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   timing_next_call();
   stage_begin(ST_PREP, st);
   launch_prep(c, st);
+  tables32_kernel<<<TABLES32_THREADS / 256, 256, 0, st>>>(c);
   stage_end(ST_PREP, st);
   stage_begin(ST_CN, st);
   cn_mixed_kernel<<<atoms, 256, 0, st>>>(c);
   stage_end(ST_CN, st);
-  const size_t vec_bytes = 8 * eeq_mixed_vec_doubles(N);
+  const size_t vec_bytes = 4 * eeq_mixed_vec_floats(N);
   const size_t tri_bytes = (size_t)4 * ((size_t)N * (N + 1) / 2);
   const bool eeq_smem = vec_bytes + tri_bytes <= 220 * 1024;
   stage_begin(ST_EEQ, st);
   if (eeq) {
-    eeq_build_mixed_kernel<<<dim3((unsigned)(((size_t)N * (N + 1) / 2 + 255) / 256), B), 256, 0,
-                             st>>>(c);
+    eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
     if (eeq_smem) {
       cudaFuncSetAttribute(eeq_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
                            (int)(vec_bytes + tri_bytes));
@@ -1085,11 +1332,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   }
   stage_end(ST_EEQ, st);
   stage_begin(ST_WEIGHTS, st);
-  launch_weights(c, st);
-  const size_t BN = (size_t)B * N;
-  size_t conv_blocks = (BN * c.S * NFREQ + 255) / 256;
-  if (conv_blocks > 65535) conv_blocks = 65535;
-  mixed_convert_kernel<<<(unsigned)conv_blocks, 256, 0, st>>>(c);
+  weights_mixed_kernel<<<dim3((unsigned)(((N + 127) / 128) * c.S), B), 128, 0, st>>>(c);
   stage_end(ST_WEIGHTS, st);
   stage_begin(ST_PAIR_FWD, st);
   if (pgrad)
