@@ -885,110 +885,223 @@ __global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
 //   X        float2[2N]       solution (two right-hand sides), double-float
 //   BB       float2[2N]       right-hand sides (b, 1), double-float
 //   vf       float[2N]        FP32 residual / correction
-//   invd     float[Nr]        reciprocal diagonal of the factor
-//   L        float[N(N+1)/2]  FP32 factor (SMEM only)
+//   (16-byte aligned from here)
+//   PT       float[32 * ldp]  transposed panel of the factorisation (SMEM only)
+//   L        float[N(N+1)/2]  FP32 factor (SMEM only; the adjoint has no PT)
 __host__ __device__ inline int eeq_round4(int n) { return (n + 3) & ~3; }
-__host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {
-  return 2 * (size_t)eeq_round4(N) + 10 * (size_t)N;
+__host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {  // multiple of 4 (16 bytes)
+  return ((size_t)eeq_round4(N) + 10 * (size_t)N + 3) & ~(size_t)3;
 }
 
 constexpr int PB = 32;  // panel width of the blocked factorisation and solves
+constexpr unsigned FULL = 0xffffffffu;
+
+// Diagonal 32 x 32 block (rows / columns k0 .. k0+kb-1) of the packed lower
+// matrix L, by one warp, in registers: the Cholesky factor (lane r holds row
+// r; rows beyond the matrix are padded with the identity), then the inverse
+// of the factor (lane c computes column c), which replaces the block in
+// place: the panel and the triangular solves only need the inverse.  A
+// non-positive pivot sets *bad and goes on with pivot 1.
+__device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
+  const int r = threadIdx.x & 31;
+  const bool live = r < kb;
+  float *row = L + tri_index(k0 + (live ? r : 0), k0);
+  float a[PB];
+#pragma unroll
+  for (int j = 0; j < PB; ++j) a[j] = live ? (j <= r ? row[j] : 0.f) : (j == r ? 1.f : 0.f);
+#pragma unroll
+  for (int c = 0; c < PB; ++c) {
+    float d = __shfl_sync(FULL, a[c], c);
+    if (!(d > 0.f)) {
+      if (r == 0) *bad = 1;
+      d = 1.f;
+    }
+    const float inv = rsqrtf(d);
+    if (r == c) a[c] = d * inv;
+    else if (r > c) a[c] *= inv;
+#pragma unroll
+    for (int j = 0; j < PB; ++j) {
+      if (j > c) {
+        const float lj = __shfl_sync(FULL, a[c], j);
+        if (r >= j) a[j] = fmaf(-a[c], lj, a[j]);
+      }
+    }
+  }
+#pragma unroll
+  for (int j = 0; j < PB; ++j)
+    if (live && j <= r) row[j] = a[j];
+  __syncwarp();
+  // inverse: X[rr][c] = -(sum_{k=c}^{rr-1} L[rr][k] X[k][c]) / L[rr][rr]; x = column c
+  const int c = r;
+  float x[PB];
+#pragma unroll
+  for (int rr = 0; rr < PB; ++rr) {
+    x[rr] = 0.f;
+    if (rr < kb) {
+      const float *lr = L + tri_index(k0 + rr, k0);
+      float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+      for (int k = 0; k < rr; ++k) {
+        if (k & 1) acc1 = fmaf(lr[k], x[k], acc1);
+        else acc0 = fmaf(lr[k], x[k], acc0);
+      }
+      const float dii = 1.0f / lr[rr];
+      x[rr] = rr == c ? dii : (rr > c ? -(acc0 + acc1) * dii : 0.f);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int rr = 0; rr < PB; ++rr)
+    if (rr < kb && rr >= c) L[tri_index(k0 + rr, k0 + c)] = x[rr];
+  __syncwarp();
+}
+
+// Leading dimension of the transposed panel PT[32][ldp] of chol_blocked:
+// rows of at most N - 32 entries, rounded up to 8 (the 8-wide tiles read up
+// to there) plus 4 (16-byte rows, spread banks).
+__host__ __device__ inline int chol_panel_ld(int N) {
+  const int n = N > 40 ? N - 32 : 8;
+  return ((n + 7) & ~7) + 4;
+}
+
+// (ti, tj), tj <= ti, of the t-th tile of a packed lower triangle of tiles
+__device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
+  ti = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
+  while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
+  while (ti > 0 && ti * (ti + 1) / 2 > t) --ti;
+  tj = t - ti * (ti + 1) / 2;
+}
 
 // Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
-// m x m FP32 matrix L, in place; invd receives 1 / L_kk.  Three barriers per
-// panel.  A non-positive pivot sets *bad and continues with pivot 1.
-__device__ void chol_blocked(float *L, float *invd, int m, int *bad) {
+// m x m FP32 matrix L, in place, except that each diagonal block holds the
+// inverse of its factor.  Per panel: the diagonal block by warp 0 in
+// registers, the panel L21 = A21 X^T (X the block inverse; one warp per row,
+// lane = column), and the trailing update A22 -= L21 L21^T.  With a panel
+// buffer PT (shared memory, 32 x ldp) the panel is also stored transposed and
+// the update runs on 8 x 8 register tiles read as float4 (64 FMAs per four
+// 16-byte loads); without it (PT == nullptr) on 4 x 4 tiles read from the
+// packed rows.
+__device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
+  const int nw = nt >> 5;
   for (int k0 = 0; k0 < m; k0 += PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) {  // diagonal block: lane r owns row k0 + r
-      for (int cc = 0; cc < kb; ++cc) {
-        float d = L[tri_index(k0 + cc, k0 + cc)];
-        if (!(d > 0.f)) {
-          if (lane == 0) *bad = 1;
-          d = 1.f;
-        }
-        d = sqrtf(d);
-        const float inv = 1.0f / d;
-        __syncwarp();
-        if (lane == 0) {
-          L[tri_index(k0 + cc, k0 + cc)] = d;
-          invd[k0 + cc] = inv;
-        }
-        float lrc = 0.f;
-        if (lane > cc && lane < kb) {
-          lrc = L[tri_index(k0 + lane, k0 + cc)] * inv;
-          L[tri_index(k0 + lane, k0 + cc)] = lrc;
-        }
-        __syncwarp();
-        if (lane > cc && lane < kb) {
-          float *row = L + tri_index(k0 + lane, 0);
-          for (int c2 = cc + 1; c2 <= lane; ++c2)
-            row[k0 + c2] = fmaf(-lrc, L[tri_index(k0 + c2, k0 + cc)], row[k0 + c2]);
-        }
-        __syncwarp();
-      }
-    }
+    if (warp == 0) chol_diag_block(L, k0, kb, bad);
     __syncthreads();
-    // panel below the block: rows solve against the block's transpose
-    for (int i = k0 + kb + tid; i < m; i += nt) {
-      float *row = L + tri_index(i, 0);
-      for (int cc = 0; cc < kb; ++cc) {
-        float v = row[k0 + cc];
-        const float *lc = L + tri_index(k0 + cc, 0);
-        for (int c2 = 0; c2 < cc; ++c2) v = fmaf(-row[k0 + c2], lc[k0 + c2], v);
-        row[k0 + cc] = v * invd[k0 + cc];
-      }
-    }
-    __syncthreads();
-    // trailing update of the lower triangle right of the panel
     const int t0 = k0 + kb;
+    // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T
+    for (int i = t0 + warp; i < m; i += nw) {
+      float *row = L + tri_index(i, k0);
+      float v = 0.f;
+      if (lane < kb) {
+        const float *xc = L + tri_index(k0 + lane, k0);
+        for (int cc = 0; cc <= lane; ++cc) v = fmaf(row[cc], xc[cc], v);
+      }
+      __syncwarp();
+      if (lane < kb) {
+        row[lane] = v;
+        if (PT) PT[lane * ldp + (i - t0)] = v;
+      }
+    }
+    __syncthreads();
     const int nrem = m - t0;
-    const int ntri = nrem * (nrem + 1) / 2;
-    for (int t = tid; t < ntri; t += nt) {
-      int ii = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-      while ((ii + 1) * (ii + 2) / 2 <= t) ++ii;
-      while (ii > 0 && ii * (ii + 1) / 2 > t) --ii;
-      const int jj = t - ii * (ii + 1) / 2;
-      const float *ri = L + tri_index(t0 + ii, 0) + k0;
-      const float *rj = L + tri_index(t0 + jj, 0) + k0;
-      float acc = 0.f;
-      for (int cc = 0; cc < kb; ++cc) acc = fmaf(ri[cc], rj[cc], acc);
-      L[tri_index(t0 + ii, t0 + jj)] -= acc;
+    if (PT) {
+      const int T8 = (nrem + 7) >> 3;
+      const int ntile = T8 * (T8 + 1) / 2;
+      for (int t = tid; t < ntile; t += nt) {
+        int ti, tj;
+        tri_tile(t, ti, tj);
+        const int i0 = 8 * ti, j0 = 8 * tj;  // relative to t0
+        float acc[8][8];
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
+        for (int cc = 0; cc < kb; ++cc) {
+          const float4 *p = reinterpret_cast<const float4 *>(PT + cc * ldp);
+          const float4 xa = p[i0 >> 2], xb = p[(i0 >> 2) + 1];
+          const float4 ya = p[j0 >> 2], yb = p[(j0 >> 2) + 1];
+          const float x[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
+          const float y[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
+#pragma unroll
+          for (int q = 0; q < 8; ++q)
+#pragma unroll
+            for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
+        }
+#pragma unroll
+        for (int q = 0; q < 8; ++q) {
+          const int i = t0 + i0 + q;
+          if (i < m) {
+            float *ri = L + tri_index(i, 0);
+#pragma unroll
+            for (int u = 0; u < 8; ++u) {
+              const int j = t0 + j0 + u;
+              if (j <= i) ri[j] -= acc[q][u];
+            }
+          }
+        }
+      }
+    } else {
+      const int T4 = (nrem + 3) >> 2;
+      const int ntile = T4 * (T4 + 1) / 2;
+      for (int t = tid; t < ntile; t += nt) {
+        int ti, tj;
+        tri_tile(t, ti, tj);
+        const int i0 = t0 + 4 * ti, j0 = t0 + 4 * tj;
+        size_t ri[4], rj[4];  // offsets of the panel segments of rows i0+q, j0+q
+#pragma unroll
+        for (int q = 0; q < 4; ++q) {
+          ri[q] = tri_index(min(i0 + q, m - 1), k0);
+          rj[q] = tri_index(min(j0 + q, m - 1), k0);
+        }
+        float acc[4][4];
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) acc[q][u] = 0.f;
+        for (int cc = 0; cc < kb; ++cc) {
+          float x[4], y[4];
+#pragma unroll
+          for (int q = 0; q < 4; ++q) {
+            x[q] = L[ri[q] + cc];
+            y[q] = L[rj[q] + cc];
+          }
+#pragma unroll
+          for (int q = 0; q < 4; ++q)
+#pragma unroll
+            for (int u = 0; u < 4; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
+        }
+#pragma unroll
+        for (int q = 0; q < 4; ++q)
+#pragma unroll
+          for (int u = 0; u < 4; ++u) {
+            const int i = i0 + q, j = j0 + u;
+            if (i < m && j <= i) L[tri_index(i, j)] -= acc[q][u];
+          }
+      }
     }
     __syncthreads();
   }
 }
 
-// Blocked solves with the packed factor (all threads of the block call
-// them): forward L z = v, backward L^T x = z, ``nr`` right-hand sides of
-// leading dimension ldv.  Within a 32-row block the recurrence runs on one
-// warp with shuffles; the rest of the rows are updated by all threads.
-__device__ void fwd_solve_blocked(const float *L, const float *invd, float *v, int ldv, int m,
-                                  int nr) {
+// Blocked solves with the packed factor whose diagonal blocks hold their
+// inverses (all threads of the block call them): forward L z = v, backward
+// L^T x = z, ``nr`` <= 2 right-hand sides of leading dimension ldv.  Per
+// 32-row block: a 32 x 32 product with the block inverse (warp w handles
+// right-hand side w), then the update of the other rows by all threads.
+__device__ void fwd_solve_blocked(const float *L, float *v, int ldv, int m, int nr) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   for (int k0 = 0; k0 < m; k0 += PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) {
-      float x0 = lane < kb ? v[k0 + lane] : 0.f;
-      float x1 = (nr == 2 && lane < kb) ? v[ldv + k0 + lane] : 0.f;
-      for (int cc = 0; cc < kb; ++cc) {
-        const float inv = invd[k0 + cc];
-        const float xc0 = __shfl_sync(0xffffffffu, x0, cc) * inv;
-        const float xc1 = __shfl_sync(0xffffffffu, x1, cc) * inv;
-        if (lane == cc) {
-          x0 = xc0;
-          x1 = xc1;
-        } else if (lane > cc && lane < kb) {
-          const float l = L[tri_index(k0 + lane, k0 + cc)];
-          x0 = fmaf(-l, xc0, x0);
-          x1 = fmaf(-l, xc1, x1);
-        }
-      }
+    if (warp < nr) {
+      float *vr = v + warp * ldv + k0;
+      float z = 0.f;
       if (lane < kb) {
-        v[k0 + lane] = x0;
-        if (nr == 2) v[ldv + k0 + lane] = x1;
+        const float *xr = L + tri_index(k0 + lane, k0);
+        for (int cc = 0; cc <= lane; ++cc) z = fmaf(xr[cc], vr[cc], z);
       }
+      __syncwarp();
+      if (lane < kb) vr[lane] = z;
     }
     __syncthreads();
     const int rows = m - k0 - kb;
@@ -1004,32 +1117,18 @@ __device__ void fwd_solve_blocked(const float *L, const float *invd, float *v, i
   }
 }
 
-__device__ void bwd_solve_blocked(const float *L, const float *invd, float *v, int ldv, int m,
-                                  int nr) {
+__device__ void bwd_solve_blocked(const float *L, float *v, int ldv, int m, int nr) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   if (m <= 0) return;
   for (int k0 = ((m - 1) / PB) * PB; k0 >= 0; k0 -= PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) {
-      float x0 = lane < kb ? v[k0 + lane] : 0.f;
-      float x1 = (nr == 2 && lane < kb) ? v[ldv + k0 + lane] : 0.f;
-      for (int cc = kb - 1; cc >= 0; --cc) {
-        const float inv = invd[k0 + cc];
-        const float xc0 = __shfl_sync(0xffffffffu, x0, cc) * inv;
-        const float xc1 = __shfl_sync(0xffffffffu, x1, cc) * inv;
-        if (lane == cc) {
-          x0 = xc0;
-          x1 = xc1;
-        } else if (lane < cc) {
-          const float l = L[tri_index(k0 + cc, k0 + lane)];
-          x0 = fmaf(-l, xc0, x0);
-          x1 = fmaf(-l, xc1, x1);
-        }
-      }
-      if (lane < kb) {
-        v[k0 + lane] = x0;
-        if (nr == 2) v[ldv + k0 + lane] = x1;
-      }
+    if (warp < nr) {
+      float *vr = v + warp * ldv + k0;
+      float z = 0.f;
+      if (lane < kb)
+        for (int cc = lane; cc < kb; ++cc) z = fmaf(L[tri_index(k0 + cc, k0 + lane)], vr[cc], z);
+      __syncwarp();
+      if (lane < kb) vr[lane] = z;
     }
     __syncthreads();
     for (int t = tid; t < k0 * nr; t += nt) {
@@ -1044,6 +1143,7 @@ __device__ void bwd_solve_blocked(const float *L, const float *invd, float *v, i
 }
 
 constexpr int EEQ_REFINE_MAX = 8;
+constexpr int EEQ_THREADS = 256;
 constexpr float EEQ_RESIDUAL_TOL = 1e-10f;
 
 // acc + (h + lo) x for a double-float x; acc is left unnormalised (its low
@@ -1079,10 +1179,22 @@ __device__ float eeq_residual_df(const float *Hi, const float *Lo, const float2 
   for (int k = warp; k < m; k += nw) {
     const float *hr = Hi + (size_t)k * N, *lr = Lo + (size_t)k * N;
     dfl a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
-    for (int l = lane; l < m; l += 32) {
-      const float h = hr[l], lo = lr[l];
-      a0 = df_acc_prod(a0, h, lo, X[l]);
-      if (nr == 2) a1 = df_acc_prod(a1, h, lo, X[N + l]);
+    for (int l0 = lane; l0 < m; l0 += 256) {
+      float h[8], lo[8];  // eight independent load pairs in flight per lane
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int l = l0 + 32 * u;
+        h[u] = l < m ? hr[l] : 0.f;
+        lo[u] = l < m ? lr[l] : 0.f;
+      }
+#pragma unroll
+      for (int u = 0; u < 8; ++u) {
+        const int l = l0 + 32 * u;
+        if (l < m) {
+          a0 = df_acc_prod(a0, h[u], lo[u], X[l]);
+          if (nr == 2) a1 = df_acc_prod(a1, h[u], lo[u], X[N + l]);
+        }
+      }
     }
     a0 = df_warp_sum(a0);
     if (nr == 2) a1 = df_warp_sum(a1);
@@ -1112,9 +1224,9 @@ __device__ float eeq_residual_df(const float *Hi, const float *Lo, const float2 
 
 // FP32 factor + double-float refinement: X (nr columns) <- A^-1 BB to an
 // FP64-level residual below 1e-10.
-__device__ void eeq_refined_solve(const float *L, const float *invd, const float *Hi,
-                                  const float *Lo, float2 *X, const float2 *BB, float *vf,
-                                  int m, int N, int nr, float *s_red) {
+__device__ void eeq_refined_solve(const float *L, const float *Hi, const float *Lo, float2 *X,
+                                  const float2 *BB, float *vf, int m, int N, int nr,
+                                  float *s_red) {
   for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
     const int o = (t / m) * N + t % m;
     X[o] = make_float2(0.f, 0.f);
@@ -1122,8 +1234,8 @@ __device__ void eeq_refined_solve(const float *L, const float *invd, const float
   }
   __syncthreads();
   for (int it = 0; it < EEQ_REFINE_MAX; ++it) {
-    fwd_solve_blocked(L, invd, vf, N, m, nr);
-    bwd_solve_blocked(L, invd, vf, N, m, nr);
+    fwd_solve_blocked(L, vf, N, m, nr);
+    bwd_solve_blocked(L, vf, N, m, nr);
     for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
       const int o = (t / m) * N + t % m;
       const dfl s = df_add(dfl{X[o].x, X[o].y}, dfl{vf[o], 0.f});
@@ -1135,7 +1247,7 @@ __device__ void eeq_refined_solve(const float *L, const float *invd, const float
 }
 
 template <bool SMEM>
-__global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
+__global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_mixed_kernel(Ctx c) {
   extern __shared__ float4 s_dyn4[];
   float *s_f = reinterpret_cast<float *>(s_dyn4);
   const int b = blockIdx.x;
@@ -1149,9 +1261,10 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
   float2 *X = reinterpret_cast<float2 *>(s_f + Nr);
   float2 *BB = X + 2 * N;
   float *vf = reinterpret_cast<float *>(BB + 2 * N);
-  float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
-  float *L = SMEM ? invd + Nr : c.w.eeq_L32 + (size_t)b * NN2;
+  const int ldp = chol_panel_ld(N);
+  float *PT = SMEM ? s_f + eeq_mixed_vec_floats(N) : nullptr;
+  float *L = SMEM ? PT + PB * ldp : c.w.eeq_L32 + (size_t)b * NN2;
   const float *Hi = c.w.eeq_hi + (size_t)b * N * N;
   const float *Lo = c.w.eeq_lo + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
@@ -1175,9 +1288,9 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
     BB[N + k] = make_float2(1.f, 0.f);
   }
   __syncthreads();
-  chol_blocked(L, invd, m, &s_bad);
+  chol_blocked(L, PT, ldp, m, &s_bad);
   if (threadIdx.x == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
-  eeq_refined_solve(L, invd, Hi, Lo, X, BB, vf, m, N, 2, s_red);
+  eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 2, s_red);
   if (warp == 0) {
     double sx = 0.0, sy = 0.0;
     for (int k = lane; k < m; k += 32) {
@@ -1215,8 +1328,9 @@ __global__ void __launch_bounds__(512) eeq_mixed_kernel(Ctx c) {
 }
 
 // Adjoint: A u = dE/dq by the FP32 factor + double-float refinement,
-// w = u - nu y.
-__global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
+// w = u - nu y.  SMEM: the factor is staged in shared memory.
+template <bool SMEM>
+__global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_adjoint_mixed_kernel(Ctx c) {
   extern __shared__ float4 s_dyn4[];
   float *s_f = reinterpret_cast<float *>(s_dyn4);
   const int b = blockIdx.x;
@@ -1230,19 +1344,24 @@ __global__ void __launch_bounds__(512) eeq_adjoint_mixed_kernel(Ctx c) {
   float2 *X = reinterpret_cast<float2 *>(s_f + Nr);
   float2 *BB = X + 2 * N;
   float *vf = reinterpret_cast<float *>(BB + 2 * N);
-  float *invd = vf + 2 * N;
   const size_t NN2 = (size_t)N * (N + 1) / 2;
-  const float *L = c.w.eeq_L32 + (size_t)b * NN2;
+  const float *Lg = c.w.eeq_L32 + (size_t)b * NN2;
   const float *Hi = c.w.eeq_hi + (size_t)b * N * N;
   const float *Lo = c.w.eeq_lo + (size_t)b * N * N;
   const int m = compact_real_atoms(c, b, n, s_idx, &s_m);
+  const float *L = Lg;
+  if (SMEM) {
+    float *Ls = s_f + eeq_mixed_vec_floats(N);
+    const size_t tri_m = (size_t)m * (m + 1) / 2;
+    for (size_t t = threadIdx.x; t < tri_m; t += blockDim.x) Ls[t] = Lg[t];
+    L = Ls;
+  }
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const dfl g = df_from(c.w.dEdq[(size_t)b * N + s_idx[k]]);
     BB[k] = make_float2(g.hi, g.lo);
-    invd[k] = 1.0f / L[tri_index(k, k)];
   }
   __syncthreads();
-  eeq_refined_solve(L, invd, Hi, Lo, X, BB, vf, m, N, 1, s_red);
+  eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 1, s_red);
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     double su = 0.0;
@@ -1314,18 +1433,19 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   stage_end(ST_CN, st);
   const size_t vec_bytes = 4 * eeq_mixed_vec_floats(N);
   const size_t tri_bytes = (size_t)4 * ((size_t)N * (N + 1) / 2);
-  const bool eeq_smem = vec_bytes + tri_bytes <= 220 * 1024;
+  const size_t pt_bytes = (size_t)4 * PB * chol_panel_ld(N);
+  const bool eeq_smem = vec_bytes + pt_bytes + tri_bytes <= 220 * 1024;
   stage_begin(ST_EEQ, st);
   if (eeq) {
     eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
     if (eeq_smem) {
       cudaFuncSetAttribute(eeq_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(vec_bytes + tri_bytes));
-      eeq_mixed_kernel<true><<<B, 512, vec_bytes + tri_bytes, st>>>(c);
+                           (int)(vec_bytes + pt_bytes + tri_bytes));
+      eeq_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + pt_bytes + tri_bytes, st>>>(c);
     } else {
       cudaFuncSetAttribute(eeq_mixed_kernel<false>,
                            cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
-      eeq_mixed_kernel<false><<<B, 512, vec_bytes, st>>>(c);
+      eeq_mixed_kernel<false><<<B, EEQ_THREADS, vec_bytes, st>>>(c);
     }
   } else {
     launch_charges_in(c, st);
@@ -1368,9 +1488,16 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
     stage_end(ST_PAIR_ATM_BWD, st);
     if (eeq) {
       stage_begin(ST_EEQ_ADJ, st);
-      cudaFuncSetAttribute(eeq_adjoint_mixed_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)vec_bytes);
-      eeq_adjoint_mixed_kernel<<<B, 512, vec_bytes, st>>>(c);
+      if (eeq_smem) {
+        cudaFuncSetAttribute(eeq_adjoint_mixed_kernel<true>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize,
+                             (int)(vec_bytes + tri_bytes));
+        eeq_adjoint_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + tri_bytes, st>>>(c);
+      } else {
+        cudaFuncSetAttribute(eeq_adjoint_mixed_kernel<false>,
+                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
+        eeq_adjoint_mixed_kernel<false><<<B, EEQ_THREADS, vec_bytes, st>>>(c);
+      }
       stage_end(ST_EEQ_ADJ, st);
     }
     stage_begin(ST_PAIR_CN_BWD, st);
