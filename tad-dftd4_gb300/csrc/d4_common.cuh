@@ -19,6 +19,32 @@ constexpr double INV_SQRT_PI = 0.56418958354775628694807945156077;
 
 // Workspace carved out of one caller-provided buffer.  The same function
 // computes the layout for d4_workspace_size and d4_dispersion.
+// ---------------------------------------------------------------- EEQ sizes
+
+// Shared memory of the one-CTA EEQ kernels of the precision form (floats):
+// vectors (compact index, double-float solution and right-hand sides, FP32
+// residual), the transposed panel PT[32][ldp] and the packed factor.
+__host__ __device__ inline int eeq_round4(int n) { return (n + 3) & ~3; }
+__host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {  // multiple of 4 (16 bytes)
+  return ((size_t)eeq_round4(N) + 10 * (size_t)N + 3) & ~(size_t)3;
+}
+// Leading dimension of the transposed panel PT[32][ldp] of chol_blocked:
+// rows of at most N - 32 entries, rounded up to 8 (the 8-wide tiles read up
+// to there) plus 4 (16-byte rows, spread banks).
+__host__ __device__ inline int chol_panel_ld(int N) {
+  const int n = N > 40 ? N - 32 : 8;
+  return ((n + 7) & ~7) + 4;
+}
+__host__ __device__ inline size_t eeq_small_bytes(int N) {
+  return 4 * (eeq_mixed_vec_floats(N) + (size_t)32 * chol_panel_ld(N) +
+              (size_t)N * (N + 1) / 2);
+}
+// Structures padded to N are solved by one CTA each when everything fits in
+// shared memory (N <= 290), else by the multi-CTA path.
+__host__ __device__ inline bool eeq_small_fits(int N) { return eeq_small_bytes(N) <= 220 * 1024; }
+constexpr int EEQ_BIG_REFINE = 4;  // refinement iterations of the multi-CTA path at most
+
+
 struct Workspace {
   int *status;      // [1]
   int *n_eff;       // [B]   highest real atom index + 1
@@ -83,7 +109,12 @@ struct Workspace {
   float *G032;      // [B*N*S*23] dE/dA0
   float4 *ptf;      // [B*N*N] (r^2, 1/r, alp/3 log2(R0/r), sqrt(C6(q=0)))
   float4 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2, log(R0/r), 0)
-  float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor
+  float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor (one-CTA path)
+  float *eeq_F;     // [B*N*N] dense FP32 factor, block inverses on the diagonal (multi-CTA)
+  float *eeq_V;     // [B*2*N] FP32 residual / correction (multi-CTA)
+  float2 *eeq_X;    // [B*2*N] double-float solution (multi-CTA)
+  float2 *eeq_B;    // [B*2*N] double-float right-hand sides (multi-CTA)
+  unsigned *eeq_res;  // [B*EEQ_BIG_REFINE] max |residual| per iteration (float bits)
   size_t bytes;
 };
 
@@ -167,7 +198,15 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.G032 = grad ? (float *)take(4 * BNS23) : nullptr;
     w.ptf = (float4 *)take(16 * BNN);
     w.ptf_da = pgrad ? (float4 *)take(16 * BNN) : nullptr;
-    w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
+    if (eeq_small_fits(N)) {
+      w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
+    } else {
+      w.eeq_F = (float *)take(4 * BNN);
+      w.eeq_V = (float *)take(4 * 2 * BN);
+      w.eeq_X = (float2 *)take(8 * 2 * BN);
+      w.eeq_B = (float2 *)take(8 * 2 * BN);
+      w.eeq_res = (unsigned *)take(4 * (size_t)B * EEQ_BIG_REFINE);
+    }
   }
   w.bytes = align_up(off, 256);
   return w;
@@ -198,6 +237,7 @@ struct Ctx {
   Workspace w;
   d4_outputs_t out;
 };
+
 
 // ---------------------------------------------------------------- helpers
 

@@ -1,0 +1,523 @@
+// Multi-CTA EEQ solve of the precision form, for structures too large for
+// one CTA's shared memory (N > 290): blocked right-looking FP32 Cholesky of
+// the dense matrix in panels of 128 columns, blocked triangular solves and
+// double-float refinement residuals, every stage spread over all SMs.
+//
+//   factor (per panel k0):  diag   one CTA per structure: Cholesky of the
+//                                  128 x 128 diagonal block (chol_blocked in
+//                                  shared memory) and the full inverse X of
+//                                  its factor, stored over the block
+//                          panel   L21 = A21 X^T, 64-row tiles
+//                          syrk    A22 -= L21 L21^T, 128 x 128 lower tiles,
+//                                  8 x 8 register tiles (an FP32 SGEMM)
+//   solve  (per iteration): forward and backward block sweeps (X products
+//                          on the diagonal blocks, GEMV updates off them),
+//                          then x += v and the double-float residual of
+//                          (hi + lo) x, whose max |r| per structure decides
+//                          (on the device) whether later iterations run.
+//
+// Rows and columns are in compact order (real atoms only, ``ridx``); the
+// structures of a batch are processed together (grid y), each up to its own
+// size n_real[b].
+#include <float.h>
+
+#include "d4_chol.cuh"
+#include "d4_common.cuh"
+#include "d4_kernels.cuh"
+
+namespace d4 {
+
+constexpr int BNB = 128;  // panel width
+constexpr float BIG_TOL = 1e-10f;
+
+__device__ __forceinline__ bool big_skip(const Ctx &c, int b, int it) {
+  return it > 0 && __uint_as_float(c.w.eeq_res[b * EEQ_BIG_REFINE + it - 1]) < BIG_TOL;
+}
+
+// ---------------------------------------------------------------- factor
+
+// Diagonal block [k0, k0 + kb) of structure b: Cholesky in shared memory,
+// then the full inverse X of the kb x kb factor by block forward
+// substitution (X_cc = D_c^-1, X_rc = -D_r^-1 sum_k L_rk X_kc), written over
+// the block (lower part).
+__global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
+  extern __shared__ float4 s_dyn4[];
+  float *P = reinterpret_cast<float *>(s_dyn4);  // packed kb x kb
+  const int ldp = chol_panel_ld(BNB);
+  float *PT = P + ((BNB * (BNB + 1) / 2 + 3) & ~3);  // 32 x ldp, also the T scratch
+  float *Xs = PT + 32 * ldp;                        // dense [BNB][BNB + 1]
+  __shared__ int s_bad;
+  const int b = blockIdx.x;
+  const int m = c.w.n_real[b];
+  if (k0 >= m) return;
+  const int kb = min(BNB, m - k0);
+  const int N = c.N;
+  float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  if (tid == 0) s_bad = 0;
+  for (int t = tid; t < kb * (kb + 1) / 2; t += nt) {
+    int i, j;
+    tri_tile(t, i, j);
+    P[t] = F[(size_t)(k0 + i) * N + k0 + j];
+  }
+  __syncthreads();
+  chol_blocked(P, PT, ldp, kb, &s_bad);
+  if (tid == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
+  constexpr int LX = BNB + 1;
+  // X = 0, diagonal 32-blocks = their inverses (held by P)
+  for (int t = tid; t < BNB * BNB; t += nt) {
+    const int i = t / BNB, j = t % BNB;
+    Xs[i * LX + j] = (i < kb && j <= i && (i >> 5) == (j >> 5)) ? P[tri_index(i, j)] : 0.f;
+  }
+  __syncthreads();
+  const int nbk = (kb + 31) >> 5;
+  for (int rb = 1; rb < nbk; ++rb) {
+    const int r0 = rb * 32, rows = min(32, kb - r0), cols = r0;
+    // T[r][c] = sum_{k in [c's block, r0)} L[r0 + r][k] X[k][c]
+    for (int t = tid; t < rows * cols; t += nt) {
+      const int r = t / cols, cc = t % cols;
+      const float *lr = P + tri_index(r0 + r, 0);
+      float acc = 0.f;
+      for (int k = (cc >> 5) << 5; k < r0; ++k) acc = fmaf(lr[k], Xs[k * LX + cc], acc);
+      PT[r * ldp + cc] = acc;
+    }
+    __syncthreads();
+    // X[r0 + r][c] = -sum_{r' <= r} D^-1[r][r'] T[r'][c]
+    for (int t = tid; t < rows * cols; t += nt) {
+      const int r = t / cols, cc = t % cols;
+      float acc = 0.f;
+      for (int q = 0; q <= r; ++q) acc = fmaf(P[tri_index(r0 + r, r0 + q)], PT[q * ldp + cc], acc);
+      Xs[(r0 + r) * LX + cc] = -acc;
+    }
+    __syncthreads();
+  }
+  for (int t = tid; t < kb * kb; t += nt) {
+    const int i = t / kb, j = t % kb;
+    if (j <= i) F[(size_t)(k0 + i) * N + k0 + j] = Xs[i * LX + j];
+  }
+}
+
+size_t eeq_big_diag_smem() {
+  const size_t p = (BNB * (BNB + 1) / 2 + 3) & ~3;
+  return 4 * (p + (size_t)32 * chol_panel_ld(BNB) + (size_t)BNB * (BNB + 1));
+}
+
+// Panel rows [t0 + 64 blockIdx.x, +64): L21 = A21 X^T (X lower, kb x kb).
+// Thread tile 4 rows x 8 columns; both operands transposed in shared memory.
+__global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
+  extern __shared__ float4 s_dyn4[];
+  constexpr int LXT = BNB + 4, LAT = 64 + 4;
+  float *XT = reinterpret_cast<float *>(s_dyn4);  // XT[cc][col] = X[col][cc]
+  float *AT = XT + BNB * LXT;                      // AT[cc][row] = A21[row][cc]
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (k0 >= m) return;
+  const int kb = min(BNB, m - k0);
+  const int t0 = k0 + kb;
+  const int r0 = t0 + 64 * blockIdx.x;
+  if (r0 >= m) return;
+  const int N = c.N;
+  float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int tid = threadIdx.x;
+  for (int t = tid; t < BNB * BNB; t += 256) {
+    const int col = t / BNB, cc = t % BNB;  // coalesced over cc
+    XT[cc * LXT + col] =
+        (col < kb && cc <= col) ? F[(size_t)(k0 + col) * N + k0 + cc] : 0.f;
+  }
+  for (int t = tid; t < 64 * BNB; t += 256) {
+    const int row = t / BNB, cc = t % BNB;
+    const int i = r0 + row;
+    AT[cc * LAT + row] = (i < m && cc < kb) ? F[(size_t)i * N + k0 + cc] : 0.f;
+  }
+  __syncthreads();
+  const int ty = tid >> 4, tx = tid & 15;  // rows 4 ty .. +4, columns 8 tx .. +8
+  float acc[4][8];
+#pragma unroll
+  for (int q = 0; q < 4; ++q)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
+  for (int cc = 0; cc < kb; ++cc) {
+    const float4 a = *reinterpret_cast<const float4 *>(AT + cc * LAT + 4 * ty);
+    const float4 x0 = *reinterpret_cast<const float4 *>(XT + cc * LXT + 8 * tx);
+    const float4 x1 = *reinterpret_cast<const float4 *>(XT + cc * LXT + 8 * tx + 4);
+    const float av[4] = {a.x, a.y, a.z, a.w};
+    const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+#pragma unroll
+    for (int q = 0; q < 4; ++q)
+#pragma unroll
+      for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], xv[u], acc[q][u]);
+  }
+#pragma unroll
+  for (int q = 0; q < 4; ++q) {
+    const int i = r0 + 4 * ty + q;
+    if (i >= m) continue;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int col = 8 * tx + u;
+      if (col < kb) F[(size_t)i * N + k0 + col] = acc[q][u];
+    }
+  }
+}
+
+size_t eeq_big_panel_smem() { return 4 * ((size_t)BNB * (BNB + 4) + (size_t)BNB * (64 + 4)); }
+
+// Trailing update A22 -= L21 L21^T of the lower 128 x 128 tiles (ti >= tj)
+// right of the panel.  K = kb in chunks of 16 staged transposed in shared
+// memory; 16 x 16 threads with 8 x 8 register tiles.
+constexpr int SK = 16;
+__global__ void __launch_bounds__(256) eeq_big_syrk_kernel(Ctx c, int k0) {
+  __shared__ __align__(16) float As[SK][BNB + 4];
+  __shared__ __align__(16) float Bs[SK][BNB + 4];
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (k0 >= m) return;
+  const int kb = min(BNB, m - k0);
+  const int t0 = k0 + kb;
+  int ti, tj;
+  tri_tile(blockIdx.x, ti, tj);
+  const int i0 = t0 + BNB * ti, j0 = t0 + BNB * tj;
+  if (i0 >= m) return;
+  const int N = c.N;
+  float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int tid = threadIdx.x;
+  const int ty = tid >> 4, tx = tid & 15;
+  float acc[8][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
+  // loader: thread t stages row t >> 1, columns 8 (t & 1) .. +8 of the chunk
+  const int lrow = tid >> 1, lcol = (tid & 1) * 8;
+  const int ia = i0 + lrow, jb = j0 + lrow;
+  const float *pa = F + (size_t)min(ia, m - 1) * N + k0;
+  const float *pb = F + (size_t)min(jb, m - 1) * N + k0;
+  for (int c0 = 0; c0 < kb; c0 += SK) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int cc = c0 + lcol + q;
+      As[lcol + q][lrow] = (ia < m && cc < kb) ? pa[cc] : 0.f;
+      Bs[lcol + q][lrow] = (jb < m && cc < kb) ? pb[cc] : 0.f;
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < SK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][8 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][8 * ty + 4]);
+      const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][8 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk][8 * tx + 4]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], bv[u], acc[q][u]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int i = i0 + 8 * ty + q;
+    if (i >= m) continue;
+    float *row = F + (size_t)i * N;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = j0 + 8 * tx + u;
+      if (j <= i) row[j] -= acc[q][u];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- solves
+
+// Right-hand sides and starting point: x = 0, v = FP32 rounding of b.
+// Forward: b = (-chi + kcn sqrt(cn_q), 1); adjoint: b = dE/dq.
+__global__ void eeq_big_rhs_kernel(Ctx c, int adjoint) {
+  const int b = blockIdx.y;
+  const int N = c.N;
+  const int m = c.w.n_real[b];
+  if (blockIdx.x == 0 && threadIdx.x < EEQ_BIG_REFINE) c.w.eeq_res[b * EEQ_BIG_REFINE + threadIdx.x] = 0u;
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m) return;
+  const size_t ia = (size_t)b * N + c.w.ridx[(size_t)b * N + k];
+  const size_t o = (size_t)b * 2 * N + k;
+  dfl v;
+  if (adjoint) {
+    v = df_from(c.w.dEdq[ia]);
+  } else {
+    const int z = c.w.z[ia];
+    const double cq = c.w.cnq[ia];
+    v = df_from(-c.tab.eeq_chi[z] + c.tab.eeq_kcn[z] * (cq > 0.0 ? sqrt(cq) : 0.0));
+    c.w.eeq_B[o + N] = make_float2(1.f, 0.f);
+    c.w.eeq_X[o + N] = make_float2(0.f, 0.f);
+    c.w.eeq_V[o + N] = 1.f;
+  }
+  c.w.eeq_B[o] = make_float2(v.hi, v.lo);
+  c.w.eeq_X[o] = make_float2(0.f, 0.f);
+  c.w.eeq_V[o] = v.hi;
+}
+
+// Diagonal block of a sweep: v_blk <- X v_blk (forward) or X^T v_blk
+// (backward), for nr right-hand sides.
+__global__ void __launch_bounds__(BNB) eeq_big_trsv_kernel(Ctx c, int k0, int it, int trans,
+                                                           int nr) {
+  __shared__ float s_v[2][BNB];
+  const int b = blockIdx.x;
+  const int m = c.w.n_real[b];
+  if (k0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(BNB, m - k0);
+  const int N = c.N;
+  const float *F = c.w.eeq_F + (size_t)b * N * N;
+  float *V = c.w.eeq_V + (size_t)b * 2 * N;
+  const int i = threadIdx.x;
+  for (int r = 0; r < nr; ++r) s_v[r][i] = i < kb ? V[r * N + k0 + i] : 0.f;
+  __syncthreads();
+  if (i >= kb) return;
+  for (int r = 0; r < nr; ++r) {
+    float z = 0.f;
+    if (trans) {
+      for (int cc = i; cc < kb; ++cc) z = fmaf(F[(size_t)(k0 + cc) * N + k0 + i], s_v[r][cc], z);
+    } else {
+      const float *row = F + (size_t)(k0 + i) * N + k0;
+      for (int cc = 0; cc <= i; ++cc) z = fmaf(row[cc], s_v[r][cc], z);
+    }
+    V[r * N + k0 + i] = z;
+  }
+}
+
+// Forward sweep update below the block: v_i -= F[i][blk] . v_blk, warp per row.
+__global__ void __launch_bounds__(256) eeq_big_below_kernel(Ctx c, int k0, int it, int nr) {
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (k0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(BNB, m - k0);
+  const int i = k0 + kb + blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (i >= m) return;
+  const int lane = threadIdx.x & 31;
+  const int N = c.N;
+  const float *row = c.w.eeq_F + (size_t)b * N * N + (size_t)i * N + k0;
+  float *V = c.w.eeq_V + (size_t)b * 2 * N;
+  for (int r = 0; r < nr; ++r) {
+    const float *z = V + r * N + k0;
+    float acc = 0.f;
+    for (int cc = lane; cc < kb; cc += 32) acc = fmaf(row[cc], z[cc], acc);
+    acc = warp_sumf(acc);
+    if (lane == 0) V[r * N + i] -= acc;
+  }
+}
+
+// Backward sweep update above the block: v_i -= F[blk][i] . v_blk, thread per
+// row (coalesced over i).
+__global__ void __launch_bounds__(256) eeq_big_above_kernel(Ctx c, int k0, int it, int nr) {
+  __shared__ float s_v[2][BNB];
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (k0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(BNB, m - k0);
+  const int N = c.N;
+  float *V = c.w.eeq_V + (size_t)b * 2 * N;
+  for (int t = threadIdx.x; t < nr * BNB; t += blockDim.x) {
+    const int r = t / BNB, cc = t % BNB;
+    s_v[r][cc] = cc < kb ? V[r * N + k0 + cc] : 0.f;
+  }
+  __syncthreads();
+  const int i = blockIdx.x * blockDim.x + threadIdx.x;
+  if (i >= k0) return;
+  const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)k0 * N + i;
+  for (int r = 0; r < nr; ++r) {
+    float acc = 0.f;
+    for (int cc = 0; cc < kb; ++cc) acc = fmaf(F[(size_t)cc * N], s_v[r][cc], acc);
+    V[r * N + i] -= acc;
+  }
+}
+
+// x += v (double-float).
+__global__ void eeq_big_update_kernel(Ctx c, int it, int nr) {
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  const int k = blockIdx.x * blockDim.x + threadIdx.x;
+  if (k >= m || big_skip(c, b, it)) return;
+  const int N = c.N;
+  for (int r = 0; r < nr; ++r) {
+    const size_t o = (size_t)b * 2 * N + (size_t)r * N + k;
+    const float2 x = c.w.eeq_X[o];
+    const dfl s = df_add(dfl{x.x, x.y}, dfl{c.w.eeq_V[o], 0.f});
+    c.w.eeq_X[o] = make_float2(s.hi, s.lo);
+  }
+}
+
+// r = b - (hi + lo) x in double-float, warp per row; v <- FP32 r and the
+// structure's max |r| of this iteration.
+__global__ void __launch_bounds__(256) eeq_big_residual_kernel(Ctx c, int it, int nr) {
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (big_skip(c, b, it)) return;
+  const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
+  if (k >= m) return;
+  const int lane = threadIdx.x & 31;
+  const int N = c.N;
+  const float *hr = c.w.eeq_hi + (size_t)b * N * N + (size_t)k * N;
+  const float *lr = c.w.eeq_lo + (size_t)b * N * N + (size_t)k * N;
+  const float2 *X = c.w.eeq_X + (size_t)b * 2 * N;
+  dfl a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
+  for (int l0 = lane; l0 < m; l0 += 128) {
+    float h[4], lo[4];
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int l = l0 + 32 * u;
+      h[u] = l < m ? hr[l] : 0.f;
+      lo[u] = l < m ? lr[l] : 0.f;
+    }
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      const int l = l0 + 32 * u;
+      if (l < m) {
+        const float2 x0 = X[l];
+        {
+          const float p = h[u] * x0.x;
+          const float e = fmaf(h[u], x0.y, fmaf(lo[u], x0.x, fmaf(h[u], x0.x, -p)));
+          const dfl s = df_two_sum(a0.hi, p);
+          a0 = {s.hi, a0.lo + (s.lo + e)};
+        }
+        if (nr == 2) {
+          const float2 x1 = X[N + l];
+          const float p = h[u] * x1.x;
+          const float e = fmaf(h[u], x1.y, fmaf(lo[u], x1.x, fmaf(h[u], x1.x, -p)));
+          const dfl s = df_two_sum(a1.hi, p);
+          a1 = {s.hi, a1.lo + (s.lo + e)};
+        }
+      }
+    }
+  }
+  float mx = 0.f;
+  for (int r = 0; r < nr; ++r) {
+    dfl a = r == 0 ? a0 : a1;
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
+      const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
+      const dfl s = df_two_sum(a.hi, oh);
+      a = df_fast(s.hi, s.lo + (a.lo + ol));
+    }
+    if (lane == 0) {
+      const float2 bb = c.w.eeq_B[(size_t)b * 2 * N + (size_t)r * N + k];
+      const dfl res = df_add(dfl{bb.x, bb.y}, df_neg(a));
+      c.w.eeq_V[(size_t)b * 2 * N + (size_t)r * N + k] = res.hi;
+      mx = fmaxf(mx, fabsf(res.hi));
+    }
+  }
+  if (lane == 0) atomicMax(&c.w.eeq_res[b * EEQ_BIG_REFINE + it], __float_as_uint(mx));
+}
+
+// Charges (forward) or the adjoint charges (adjoint) from the solutions,
+// one CTA per structure; FP64 sums.
+__global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint) {
+  __shared__ double s_a[32], s_b[32];
+  __shared__ double s_par;
+  const int b = blockIdx.x;
+  const int N = c.N;
+  const int m = c.w.n_real[b];
+  const float2 *X = c.w.eeq_X + (size_t)b * 2 * N;
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  double sa = 0.0, sb = 0.0;
+  for (int k = tid; k < m; k += blockDim.x) {
+    sa += (double)X[k].x + (double)X[k].y;
+    if (!adjoint) sb += (double)X[N + k].x + (double)X[N + k].y;
+  }
+  sa = warp_sum(sa);
+  sb = warp_sum(sb);
+  if (lane == 0) {
+    s_a[warp] = sa;
+    s_b[warp] = sb;
+  }
+  __syncthreads();
+  if (tid == 0) {
+    double ta = 0.0, tb = 0.0;
+    for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
+      ta += s_a[w];
+      tb += s_b[w];
+    }
+    if (adjoint) {
+      s_par = m > 0 ? ta / c.w.eeq_sum[2 * b] : 0.0;
+    } else {
+      const double lam = m > 0 ? (ta - c.charge[b]) / tb : 0.0;
+      c.w.eeq_sum[2 * b] = tb;
+      c.w.eeq_sum[2 * b + 1] = lam;
+      s_par = lam;
+    }
+  }
+  __syncthreads();
+  const double par = s_par;
+  for (int i = tid; i < N; i += blockDim.x) {
+    if (adjoint) {
+      c.w.eeq_w[(size_t)b * N + i] = 0.0;
+      c.w.dEdcnq[(size_t)b * N + i] = 0.0;
+    } else {
+      c.w.q[(size_t)b * N + i] = 0.0;
+      c.w.eeq_y[(size_t)b * N + i] = 0.0;
+    }
+  }
+  __syncthreads();
+  for (int k = tid; k < m; k += blockDim.x) {
+    const size_t a = (size_t)b * N + c.w.ridx[(size_t)b * N + k];
+    const double x0 = (double)X[k].x + (double)X[k].y;
+    if (adjoint) {
+      const double w = x0 - par * c.w.eeq_y[a];
+      c.w.eeq_w[a] = w;
+      const double cq = c.w.cnq[a];
+      const int z = c.w.z[a];
+      const double dq = cq > 0.0 ? w * c.tab.eeq_kcn[z] * 0.5 / sqrt(cq) * c.w.dcnq[a] : 0.0;
+      c.w.dEdcnq[a] = dq;
+      c.w.adj32[a].y = (float)dq;
+      c.w.adj32[a].w = (float)w;
+    } else {
+      const double x1 = (double)X[N + k].x + (double)X[N + k].y;
+      c.w.q[a] = x0 - par * x1;
+      c.w.eeq_y[a] = x1;
+    }
+  }
+}
+
+// ---------------------------------------------------------------- launch
+
+// Forward (adjoint = 0: factorisation, two right-hand sides, charges) or
+// adjoint (reuses the factor; one right-hand side dE/dq) multi-CTA EEQ.
+void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
+  const int B = c.B, N = c.N;
+  const int npan = (N + BNB - 1) / BNB;
+  if (!adjoint) {
+    cudaMemcpyAsync(c.w.eeq_F, c.w.eeq_hi, (size_t)4 * B * N * N, cudaMemcpyDeviceToDevice, st);
+    cudaFuncSetAttribute(eeq_big_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)eeq_big_diag_smem());
+    cudaFuncSetAttribute(eeq_big_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)eeq_big_panel_smem());
+    for (int p = 0; p < npan; ++p) {
+      const int k0 = p * BNB;
+      eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), st>>>(c, k0);
+      const int rest = N - k0 - BNB;
+      if (rest <= 0) break;
+      eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), st>>>(c, k0);
+      const int T = (rest + BNB - 1) / BNB;
+      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), 256, 0, st>>>(c, k0);
+    }
+  }
+  const int nr = adjoint ? 1 : 2;
+  eeq_big_rhs_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, adjoint ? 1 : 0);
+  for (int it = 0; it < EEQ_BIG_REFINE; ++it) {
+    for (int p = 0; p < npan; ++p) {
+      const int k0 = p * BNB;
+      eeq_big_trsv_kernel<<<B, BNB, 0, st>>>(c, k0, it, 0, nr);
+      const int rest = N - k0 - BNB;
+      if (rest > 0) eeq_big_below_kernel<<<dim3((rest + 7) / 8, B), 256, 0, st>>>(c, k0, it, nr);
+    }
+    for (int p = npan - 1; p >= 0; --p) {
+      const int k0 = p * BNB;
+      eeq_big_trsv_kernel<<<B, BNB, 0, st>>>(c, k0, it, 1, nr);
+      if (k0 > 0) eeq_big_above_kernel<<<dim3((k0 + 255) / 256, B), 256, 0, st>>>(c, k0, it, nr);
+    }
+    eeq_big_update_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, it, nr);
+    eeq_big_residual_kernel<<<dim3((N + 7) / 8, B), 256, 0, st>>>(c, it, nr);
+  }
+  eeq_big_finish_kernel<<<B, 1024, 0, st>>>(c, adjoint ? 1 : 0);
+}
+
+}  // namespace d4

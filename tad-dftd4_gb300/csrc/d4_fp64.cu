@@ -16,6 +16,10 @@ namespace d4 {
 
 // ---------------------------------------------------------------- prep
 
+// Structures padded beyond this size have their N x N pair accumulators
+// cleared by memsets instead of by the prep kernel.
+constexpr int PREP_ZERO_MAX_N = 256;
+
 // n_eff, input validation, D4S element slots, zeroing of accumulators.
 __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
   const int b = blockIdx.x;
@@ -113,7 +117,7 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
   if (threadIdx.x < 8) c.w.pgrad[b * 8 + threadIdx.x] = 0.0;
   if (b == 0 && threadIdx.x < NFREQ)
     c.w.fw32[threadIdx.x] = (float)(THOPI * c.tab.freq_weights[threadIdx.x]);
-  if (c.w.pr_S) {
+  if (c.w.pr_S && c.N <= PREP_ZERO_MAX_N) {
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
       const int i = t / n, j = t % n;
       const size_t o = ((size_t)b * N + i) * N + j;
@@ -121,7 +125,7 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
       c.w.pr_P[o] = 0.0;
     }
   }
-  if (c.w.prS32) {
+  if (c.w.prS32 && c.N <= PREP_ZERO_MAX_N) {
     for (int t = threadIdx.x; t < n * n; t += blockDim.x) {
       const int i = t / n, j = t % n;
       const size_t o = ((size_t)b * N + i) * N + j;
@@ -1091,9 +1095,8 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
   timing_next_call();
-  cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
   stage_begin(ST_PREP, st);
-  prep_kernel<<<B, 256, 0, st>>>(c);
+  launch_prep(c, st);
   stage_end(ST_PREP, st);
   stage_begin(ST_CN, st);
   cn_kernel<<<atoms, 256, 0, st>>>(c);
@@ -1160,6 +1163,13 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
 
 void launch_prep(const Ctx &c, cudaStream_t st) {
   cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
+  if (c.N > PREP_ZERO_MAX_N) {  // the pair accumulators of large structures: plain memsets
+    const size_t bnn = (size_t)c.B * c.N * c.N;
+    if (c.w.pr_S) cudaMemsetAsync(c.w.pr_S, 0, 8 * bnn, st);
+    if (c.w.pr_P) cudaMemsetAsync(c.w.pr_P, 0, 8 * bnn, st);
+    if (c.w.prS32) cudaMemsetAsync(c.w.prS32, 0, 4 * bnn, st);
+    if (c.w.prP32) cudaMemsetAsync(c.w.prP32, 0, 4 * bnn, st);
+  }
   prep_kernel<<<c.B, 256, 0, st>>>(c);
 }
 

@@ -8,6 +8,7 @@
 #include <float.h>
 
 #include "d4_common.cuh"
+#include "d4_chol.cuh"
 #include "d4_kernels.cuh"
 
 namespace d4 {
@@ -442,9 +443,10 @@ __device__ __forceinline__ int atm_ctas(int n) {
   return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
 }
 
-// Accumulation target of the per-pair / per-atom ATM adjoints.  Pair
-// values go to both (j, k) and (k, j) so that the backward pair kernel reads
-// rows.
+// Accumulation target of the per-pair / per-atom ATM adjoints.  SMEM: the
+// upper triangle of the structure in shared memory (flushed to both halves
+// of the global pair arrays).  Global: FP32 atomics on the upper half only
+// (j < k in every call), mirrored by atm_mirror_kernel afterwards.
 template <bool SMEM>
 struct AtmAcc {
   float *sS, *sP, *sE;  // shared (SMEM): upper triangle and atoms
@@ -459,8 +461,6 @@ struct AtmAcc {
     } else {
       atomicAdd(&gS[(size_t)j * N + k], S);
       atomicAdd(&gP[(size_t)j * N + k], P);
-      atomicAdd(&gS[(size_t)k * N + j], S);
-      atomicAdd(&gP[(size_t)k * N + j], P);
     }
   }
   __device__ __forceinline__ void energy(int x, float e) const {
@@ -471,17 +471,152 @@ struct AtmAcc {
   }
 };
 
-// ATM energy and adjoint over triples i < j < k of one structure.  K CTAs
-// share a structure (the third atom i is interleaved over them).  A warp
+// Constant inputs of the ATM triple loop of one structure.
+struct AtmIn {
+  const int *Zb;
+  const float4 *T, *Tda;
+  const float *W;
+  float cut2, alp3, s9, s9m;
+  bool weighted;
+  int N;
+};
+
+// Parameter-gradient partial sums of one warp.
+struct AtmPg {
+  float s9 = 0.f, alp = 0.f, a1 = 0.f, a2 = 0.f;
+};
+
+// One task of the ATM loop: the pair (j, k = kc + lane) held by the lanes,
+// the third atom i < j running from i0 in steps of istep.  Triple energy
+// without s9 (applied at the flush, SMEM) or with it (global).
+template <bool SMEM, bool GRAD, bool PGRAD>
+__device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &acc, int n, int j,
+                                         int kc, int i0, int istep, AtmPg &pg) {
+  const int lane = threadIdx.x & 31;
+  const int N = in.N;
+  const float cut2 = in.cut2, alp3 = in.alp3, s9 = in.s9, s9m = in.s9m;
+  const float4 *T = in.T;
+  const float *W = in.W;
+  const int k = kc + lane;
+  const bool kok = k < n && in.Zb[k] != 0;
+  const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float zjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
+  const bool mjk = kok && zjk <= cut2;
+  float4 dajk = make_float4(0.f, 0.f, 0.f, 0.f);
+  if (PGRAD && kok) dajk = in.Tda[(size_t)j * N + k];
+  const float wj = W[j];
+  const float wk = kok ? W[k] : 0.f;
+  float Sjk = 0.f, Pjk = 0.f, Ej = 0.f, Ek = 0.f;
+  const size_t step = (size_t)istep * N;
+  const float4 *Tij = T + (size_t)i0 * N + j;
+  const float4 *Tik = T + (size_t)i0 * N + (kok ? k : j);
+  for (int i = i0; i < j; i += istep, Tij += step, Tik += step) {
+    if (in.Zb[i] == 0) continue;
+    const float4 pij = *Tij;
+    float sij = 0.f, pe = 0.f, ei = 0.f;
+    if (kok) {
+      const float4 pik = *Tik;
+      const bool mij = pij.x <= cut2, mik = pik.x <= cut2;
+      if ((int)mij + (int)mik + (int)mjk >= 2) {
+        const float x = pij.x, y = pik.x, z = zjk;
+        const float ir1 = pij.y * irjk * pik.y;
+        const float ir2 = ir1 * ir1;
+        const float ir3 = ir1 * ir2;
+        const float u = x - y, v = x + y;
+        const float A = u + z, Bv = v - z, Cv = z - u;
+        const float sfac = A * Bv * Cv;
+        const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
+        const float ta = exp2f(pij.z + pik.z + Ljk);
+        const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
+        const float c9 = pij.w * pik.w * cjk;
+        const float eu = c9 * fd * ang;  // triple energy without s9
+        const float e = s9m * eu;
+        float wgt;
+        if (mij & mik & mjk) {
+          const float third = e * (1.0f / 3.0f);
+          ei = third;
+          Ej += third;
+          Ek += third;
+          wgt = ((in.weighted ? W[i] : 1.f) + wj + wk) * (1.0f / 3.0f);
+        } else {
+          const float fij = mij, fik = mik, fjk = mjk;
+          const float mi = fjk * (fij + fik), mj = fik * (fij + fjk), mk = fij * (fik + fjk);
+          const float sixth = e * (1.0f / 6.0f);
+          ei = sixth * mi;
+          Ej += sixth * mj;
+          Ek += sixth * mk;
+          wgt = ((in.weighted ? W[i] : 1.f) * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
+        }
+        if (GRAD) {
+          const float kc9 = s9m * c9;
+          const float dfl = alp3 * fd * (1.0f - fd);  // = 6 alp/3 ta fd^2
+          const float Q = 2.0f * ir3 - 5.0f * ang;
+          const float U = 0.375f * kc9 * fd * ir2 * ir3;
+          const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
+          const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
+          const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
+          const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
+          const float dez = fmaf(U, BC + AB - AC, V * irjk * irjk);
+          sij = wgt * dex;
+          Sjk = fmaf(wgt, dez, Sjk);
+          const float we = wgt * e;
+          pe = we;
+          Pjk += we;
+          acc.pair(i, k, wgt * dey, we);
+          if (PGRAD) {
+            const float4 daij = in.Tda[(size_t)i * N + j];
+            const float4 daik = in.Tda[(size_t)i * N + k];
+            const float lsum = daij.z + daik.z + dajk.z;
+            const float dfd = -fd * (1.0f - fd);  // d fd / d(alp/3 sum log(R0/r))
+            pg.s9 += wgt * eu;
+            pg.alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
+            const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
+            pg.a1 += dfa * (daij.x + daik.x + dajk.x);
+            pg.a2 += dfa * (daij.y + daik.y + dajk.y);
+          }
+        }
+      }
+    }
+    // (i, j) and E_i: one value per warp
+    if (GRAD) {
+      sij = warp_sumf(sij);
+      pe = warp_sumf(pe);
+    }
+    ei = warp_sumf(ei);
+    if (lane == 0) {
+      if (ei != 0.f) acc.energy(i, ei);
+      if (GRAD && (sij != 0.f || pe != 0.f)) acc.pair(i, j, sij, pe);
+    }
+  }
+  if (GRAD && kok && (Sjk != 0.f || Pjk != 0.f)) acc.pair(j, k, Sjk, Pjk);
+  const float ej = warp_sumf(Ej);
+  if (lane == 0 && ej != 0.f) acc.energy(j, ej);
+  if (kok && Ek != 0.f) acc.energy(k, Ek);
+}
+
+// CTAs per structure of the global-accumulation ATM (large structures):
+// about ATM_BIG_TRIPLES triples each, at most ATM_BIG_KMAX.
+constexpr long long ATM_BIG_TRIPLES = 250000;
+constexpr int ATM_BIG_KMAX = 1024;
+__host__ __device__ inline int atm_ctas_big(int n) {
+  const long long work = (long long)n * n * n / 6;
+  const long long K = (work + ATM_BIG_TRIPLES - 1) / ATM_BIG_TRIPLES;
+  return K < 1 ? 1 : (K > ATM_BIG_KMAX ? ATM_BIG_KMAX : (int)K);
+}
+
+// ATM energy and adjoint over triples i < j < k of one structure.  A warp
 // takes a task (j, 32 consecutive k > j) and loops over i: lanes hold the
 // (j, k) pair record in registers and read the (i, j) (broadcast) and (i, k)
 // (coalesced 128-bit) records.  A pair record holds r^2, 1/r,
 // alp/3 log2(R0/r) and sqrt(C6(q=0)), so the damping is one exp2 and C9 two
-// products.  Per-pair dE/d(r^2) and mask-weighted triple energies
-// accumulate in shared memory (SMEM, n <= 234) without the s9 factor, which
-// is applied once when a CTA flushes them (FP32 global atomics, both
-// triangle halves); larger structures accumulate straight into global
-// memory.
+// products.
+//   SMEM (n <= 234): K <= 8 CTAs share a structure, interleaving i; per-pair
+//     dE/d(r^2) and mask-weighted triple energies accumulate in shared memory
+//     without the s9 factor, applied when a CTA flushes them (FP32 global
+//     atomics, both triangle halves).
+//   Global (large structures): up to 1024 CTAs per structure, the tasks
+//     (j, k-chunk) dealt round-robin over all their warps, i running over
+//     all i < j; FP32 global atomics on the upper half.
 template <bool SMEM, bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     atm_mixed_kernel(Ctx c) {
@@ -491,7 +626,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   const int N = c.N;
   const int n = c.w.n_eff[b];
   if (n < 3) return;
-  const int K = atm_ctas(n);
+  const int K = SMEM ? atm_ctas(n) : atm_ctas_big(n);
   if (cta >= K) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
@@ -509,130 +644,51 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
     __syncthreads();
   }
-  const int *Zb = c.w.z + (size_t)b * N;
-  const float4 *T = c.w.ptf + (size_t)b * N * N;
-  const float4 *Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
-  const float cut2 = c.pf.cut3 * c.pf.cut3;
-  const float alp3 = c.pf.alp3;
-  const float s9 = c.pf.s9;
-  const float s9m = SMEM ? 1.f : s9;  // SMEM: s9 is applied at the flush
-  const bool weighted = c.weights != nullptr;
-  const float *W = c.w.w32 + (size_t)b * N;
-  const size_t step = (size_t)K * N;
-  float g_s9 = 0.f, g_alp = 0.f, g_a1 = 0.f, g_a2 = 0.f;
-  int task = 0;
-  for (int j = 1; j < n - 1; ++j) {
-    for (int kc = j + 1; kc < n; kc += 32, ++task) {
-      if (task % nwarps != warp || Zb[j] == 0) continue;
-      const int k = kc + lane;
-      const bool kok = k < n && Zb[k] != 0;
-      const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
-      const float zjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
-      const bool mjk = kok && zjk <= cut2;
-      float4 dajk = make_float4(0.f, 0.f, 0.f, 0.f);
-      if (PGRAD && kok) dajk = Tda[(size_t)j * N + k];
-      const float wj = W[j];
-      const float wk = kok ? W[k] : 0.f;
-      float Sjk = 0.f, Pjk = 0.f, Ej = 0.f, Ek = 0.f;
-      const float4 *Tij = T + (size_t)cta * N + j;
-      const float4 *Tik = T + (size_t)cta * N + (kok ? k : j);
-      for (int i = cta; i < j; i += K, Tij += step, Tik += step) {
-        if (Zb[i] == 0) continue;
-        const float4 pij = *Tij;
-        float sij = 0.f, pe = 0.f, ei = 0.f;
-        if (kok) {
-          const float4 pik = *Tik;
-          const bool mij = pij.x <= cut2, mik = pik.x <= cut2;
-          if ((int)mij + (int)mik + (int)mjk >= 2) {
-            const float x = pij.x, y = pik.x, z = zjk;
-            const float ir1 = pij.y * irjk * pik.y;
-            const float ir2 = ir1 * ir1;
-            const float ir3 = ir1 * ir2;
-            const float u = x - y, v = x + y;
-            const float A = u + z, Bv = v - z, Cv = z - u;
-            const float sfac = A * Bv * Cv;
-            const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-            const float ta = exp2f(pij.z + pik.z + Ljk);
-            const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
-            const float c9 = pij.w * pik.w * cjk;
-            const float eu = c9 * fd * ang;  // triple energy without s9
-            const float e = s9m * eu;
-            float wgt;
-            if (mij & mik & mjk) {
-              const float third = e * (1.0f / 3.0f);
-              ei = third;
-              Ej += third;
-              Ek += third;
-              wgt = ((weighted ? W[i] : 1.f) + wj + wk) * (1.0f / 3.0f);
-            } else {
-              const float fij = mij, fik = mik, fjk = mjk;
-              const float mi = fjk * (fij + fik), mj = fik * (fij + fjk), mk = fij * (fik + fjk);
-              const float sixth = e * (1.0f / 6.0f);
-              ei = sixth * mi;
-              Ej += sixth * mj;
-              Ek += sixth * mk;
-              wgt = ((weighted ? W[i] : 1.f) * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
-            }
-            if (GRAD) {
-              const float kc9 = s9m * c9;
-              const float dfl = alp3 * fd * (1.0f - fd);  // = 6 alp/3 ta fd^2
-              const float Q = 2.0f * ir3 - 5.0f * ang;
-              const float U = 0.375f * kc9 * fd * ir2 * ir3;
-              const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
-              const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
-              const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
-              const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
-              const float dez = fmaf(U, BC + AB - AC, V * irjk * irjk);
-              sij = wgt * dex;
-              Sjk = fmaf(wgt, dez, Sjk);
-              const float we = wgt * e;
-              pe = we;
-              Pjk += we;
-              acc.pair(i, k, wgt * dey, we);
-              if (PGRAD) {
-                const float4 daij = Tda[(size_t)i * N + j];
-                const float4 daik = Tda[(size_t)i * N + k];
-                const float lsum = daij.z + daik.z + dajk.z;
-                const float dfd = -fd * (1.0f - fd);  // d fd / d(alp/3 sum log(R0/r))
-                g_s9 += wgt * eu;
-                g_alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
-                const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
-                g_a1 += dfa * (daij.x + daik.x + dajk.x);
-                g_a2 += dfa * (daij.y + daik.y + dajk.y);
-              }
-            }
-          }
-        }
-        // (i, j) and E_i: one value per warp
-        if (GRAD) {
-          sij = warp_sumf(sij);
-          pe = warp_sumf(pe);
-        }
-        ei = warp_sumf(ei);
-        if (lane == 0) {
-          if (ei != 0.f) acc.energy(i, ei);
-          if (GRAD && (sij != 0.f || pe != 0.f)) acc.pair(i, j, sij, pe);
-        }
+  AtmIn in;
+  in.Zb = c.w.z + (size_t)b * N;
+  in.T = c.w.ptf + (size_t)b * N * N;
+  in.Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
+  in.W = c.w.w32 + (size_t)b * N;
+  in.cut2 = c.pf.cut3 * c.pf.cut3;
+  in.alp3 = c.pf.alp3;
+  in.s9 = c.pf.s9;
+  in.s9m = SMEM ? 1.f : c.pf.s9;  // SMEM: s9 is applied at the flush
+  in.weighted = c.weights != nullptr;
+  in.N = N;
+  AtmPg pg;
+  if (SMEM) {
+    int task = 0;
+    for (int j = 1; j < n - 1; ++j) {
+      for (int kc = j + 1; kc < n; kc += 32, ++task) {
+        if (task % nwarps != warp || in.Zb[j] == 0) continue;
+        atm_task<SMEM, GRAD, PGRAD>(in, acc, n, j, kc, cta, K, pg);
       }
-      if (GRAD && kok && (Sjk != 0.f || Pjk != 0.f)) acc.pair(j, k, Sjk, Pjk);
-      const float ej = warp_sumf(Ej);
-      if (lane == 0 && ej != 0.f) acc.energy(j, ej);
-      if (kok && Ek != 0.f) acc.energy(k, Ek);
+    }
+  } else {
+    const int NC = (n + 31) / 32;  // chunk slots per row j
+    const long long slots = (long long)n * NC;
+    const int G = K * nwarps;
+    for (long long sl = (long long)cta * nwarps + warp; sl < slots; sl += G) {
+      const int j = (int)(sl / NC), ch = (int)(sl % NC);
+      const int kc = j + 1 + 32 * ch;
+      if (j < 1 || j >= n - 1 || kc >= n || in.Zb[j] == 0) continue;
+      atm_task<SMEM, GRAD, PGRAD>(in, acc, n, j, kc, 0, 1, pg);
     }
   }
   if (PGRAD) {
-    g_s9 = warp_sumf(g_s9);
-    g_alp = warp_sumf(g_alp);
-    g_a1 = warp_sumf(g_a1);
-    g_a2 = warp_sumf(g_a2);
+    pg.s9 = warp_sumf(pg.s9);
+    pg.alp = warp_sumf(pg.alp);
+    pg.a1 = warp_sumf(pg.a1);
+    pg.a2 = warp_sumf(pg.a2);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)g_a1);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)g_a2);
-      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)g_s9);
-      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)g_alp);
+      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)pg.a1);
+      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)pg.a2);
+      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)pg.s9);
+      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)pg.alp);
     }
   }
   if (SMEM) {
+    const float s9 = c.pf.s9;
     __syncthreads();
     for (int j = warp; j < n; j += nwarps) {
       for (int k = j + 1 + lane; k < n; k += 32) {
@@ -652,6 +708,34 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
       const float ev = acc.sE[x] * s9;
       if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);  // once per atom
+    }
+  }
+}
+
+// Lower half of the ATM pair accumulators from the upper half (global
+// accumulation), 32 x 32 tiles through shared memory.
+__global__ void atm_mirror_kernel(Ctx c) {
+  __shared__ float sS[32][33], sP[32][33];
+  const int b = blockIdx.z;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  const int ti = blockIdx.y, tj = blockIdx.x;  // source tile (rows ti, columns tj), tj >= ti
+  if (tj < ti || ti * 32 >= n || tj * 32 >= n) return;
+  float *S = c.w.prS32 + (size_t)b * N * N;
+  float *P = c.w.prP32 + (size_t)b * N * N;
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += blockDim.x >> 5) {
+    const int i = ti * 32 + r, j = tj * 32 + tx;
+    const bool ok = i < n && j < n && j > i;
+    sS[r][tx] = ok ? S[(size_t)i * N + j] : 0.f;
+    sP[r][tx] = ok ? P[(size_t)i * N + j] : 0.f;
+  }
+  __syncthreads();
+  for (int r = ty; r < 32; r += blockDim.x >> 5) {
+    const int i = tj * 32 + r, j = ti * 32 + tx;  // destination (i > j)
+    if (i < n && j < n && i > j) {
+      S[(size_t)i * N + j] = sS[tx][r];
+      P[(size_t)i * N + j] = sP[tx][r];
     }
   }
 }
@@ -888,259 +972,6 @@ __global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
 //   (16-byte aligned from here)
 //   PT       float[32 * ldp]  transposed panel of the factorisation (SMEM only)
 //   L        float[N(N+1)/2]  FP32 factor (SMEM only; the adjoint has no PT)
-__host__ __device__ inline int eeq_round4(int n) { return (n + 3) & ~3; }
-__host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {  // multiple of 4 (16 bytes)
-  return ((size_t)eeq_round4(N) + 10 * (size_t)N + 3) & ~(size_t)3;
-}
-
-constexpr int PB = 32;  // panel width of the blocked factorisation and solves
-constexpr unsigned FULL = 0xffffffffu;
-
-// Diagonal 32 x 32 block (rows / columns k0 .. k0+kb-1) of the packed lower
-// matrix L, by one warp, in registers: the Cholesky factor (lane r holds row
-// r; rows beyond the matrix are padded with the identity), then the inverse
-// of the factor (lane c computes column c), which replaces the block in
-// place: the panel and the triangular solves only need the inverse.  A
-// non-positive pivot sets *bad and goes on with pivot 1.
-__device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
-  const int r = threadIdx.x & 31;
-  const bool live = r < kb;
-  float *row = L + tri_index(k0 + (live ? r : 0), k0);
-  float a[PB];
-#pragma unroll
-  for (int j = 0; j < PB; ++j) a[j] = live ? (j <= r ? row[j] : 0.f) : (j == r ? 1.f : 0.f);
-#pragma unroll
-  for (int c = 0; c < PB; ++c) {
-    float d = __shfl_sync(FULL, a[c], c);
-    if (!(d > 0.f)) {
-      if (r == 0) *bad = 1;
-      d = 1.f;
-    }
-    const float inv = rsqrtf(d);
-    if (r == c) a[c] = d * inv;
-    else if (r > c) a[c] *= inv;
-#pragma unroll
-    for (int j = 0; j < PB; ++j) {
-      if (j > c) {
-        const float lj = __shfl_sync(FULL, a[c], j);
-        if (r >= j) a[j] = fmaf(-a[c], lj, a[j]);
-      }
-    }
-  }
-#pragma unroll
-  for (int j = 0; j < PB; ++j)
-    if (live && j <= r) row[j] = a[j];
-  __syncwarp();
-  // inverse: X[rr][c] = -(sum_{k=c}^{rr-1} L[rr][k] X[k][c]) / L[rr][rr]; x = column c
-  const int c = r;
-  float x[PB];
-#pragma unroll
-  for (int rr = 0; rr < PB; ++rr) {
-    x[rr] = 0.f;
-    if (rr < kb) {
-      const float *lr = L + tri_index(k0 + rr, k0);
-      float acc0 = 0.f, acc1 = 0.f;
-#pragma unroll
-      for (int k = 0; k < rr; ++k) {
-        if (k & 1) acc1 = fmaf(lr[k], x[k], acc1);
-        else acc0 = fmaf(lr[k], x[k], acc0);
-      }
-      const float dii = 1.0f / lr[rr];
-      x[rr] = rr == c ? dii : (rr > c ? -(acc0 + acc1) * dii : 0.f);
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int rr = 0; rr < PB; ++rr)
-    if (rr < kb && rr >= c) L[tri_index(k0 + rr, k0 + c)] = x[rr];
-  __syncwarp();
-}
-
-// Leading dimension of the transposed panel PT[32][ldp] of chol_blocked:
-// rows of at most N - 32 entries, rounded up to 8 (the 8-wide tiles read up
-// to there) plus 4 (16-byte rows, spread banks).
-__host__ __device__ inline int chol_panel_ld(int N) {
-  const int n = N > 40 ? N - 32 : 8;
-  return ((n + 7) & ~7) + 4;
-}
-
-// (ti, tj), tj <= ti, of the t-th tile of a packed lower triangle of tiles
-__device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
-  ti = (int)((sqrtf(8.0f * (float)t + 1.0f) - 1.0f) * 0.5f);
-  while ((ti + 1) * (ti + 2) / 2 <= t) ++ti;
-  while (ti > 0 && ti * (ti + 1) / 2 > t) --ti;
-  tj = t - ti * (ti + 1) / 2;
-}
-
-// Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
-// m x m FP32 matrix L, in place, except that each diagonal block holds the
-// inverse of its factor.  Per panel: the diagonal block by warp 0 in
-// registers, the panel L21 = A21 X^T (X the block inverse; one warp per row,
-// lane = column), and the trailing update A22 -= L21 L21^T.  With a panel
-// buffer PT (shared memory, 32 x ldp) the panel is also stored transposed and
-// the update runs on 8 x 8 register tiles read as float4 (64 FMAs per four
-// 16-byte loads); without it (PT == nullptr) on 4 x 4 tiles read from the
-// packed rows.
-__device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
-  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
-  const int nw = nt >> 5;
-  for (int k0 = 0; k0 < m; k0 += PB) {
-    const int kb = min(PB, m - k0);
-    if (warp == 0) chol_diag_block(L, k0, kb, bad);
-    __syncthreads();
-    const int t0 = k0 + kb;
-    // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T
-    for (int i = t0 + warp; i < m; i += nw) {
-      float *row = L + tri_index(i, k0);
-      float v = 0.f;
-      if (lane < kb) {
-        const float *xc = L + tri_index(k0 + lane, k0);
-        for (int cc = 0; cc <= lane; ++cc) v = fmaf(row[cc], xc[cc], v);
-      }
-      __syncwarp();
-      if (lane < kb) {
-        row[lane] = v;
-        if (PT) PT[lane * ldp + (i - t0)] = v;
-      }
-    }
-    __syncthreads();
-    const int nrem = m - t0;
-    if (PT) {
-      const int T8 = (nrem + 7) >> 3;
-      const int ntile = T8 * (T8 + 1) / 2;
-      for (int t = tid; t < ntile; t += nt) {
-        int ti, tj;
-        tri_tile(t, ti, tj);
-        const int i0 = 8 * ti, j0 = 8 * tj;  // relative to t0
-        float acc[8][8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-#pragma unroll
-          for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
-        for (int cc = 0; cc < kb; ++cc) {
-          const float4 *p = reinterpret_cast<const float4 *>(PT + cc * ldp);
-          const float4 xa = p[i0 >> 2], xb = p[(i0 >> 2) + 1];
-          const float4 ya = p[j0 >> 2], yb = p[(j0 >> 2) + 1];
-          const float x[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-          const float y[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
-#pragma unroll
-          for (int q = 0; q < 8; ++q)
-#pragma unroll
-            for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int i = t0 + i0 + q;
-          if (i < m) {
-            float *ri = L + tri_index(i, 0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const int j = t0 + j0 + u;
-              if (j <= i) ri[j] -= acc[q][u];
-            }
-          }
-        }
-      }
-    } else {
-      const int T4 = (nrem + 3) >> 2;
-      const int ntile = T4 * (T4 + 1) / 2;
-      for (int t = tid; t < ntile; t += nt) {
-        int ti, tj;
-        tri_tile(t, ti, tj);
-        const int i0 = t0 + 4 * ti, j0 = t0 + 4 * tj;
-        size_t ri[4], rj[4];  // offsets of the panel segments of rows i0+q, j0+q
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          ri[q] = tri_index(min(i0 + q, m - 1), k0);
-          rj[q] = tri_index(min(j0 + q, m - 1), k0);
-        }
-        float acc[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q][u] = 0.f;
-        for (int cc = 0; cc < kb; ++cc) {
-          float x[4], y[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            x[q] = L[ri[q] + cc];
-            y[q] = L[rj[q] + cc];
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int i = i0 + q, j = j0 + u;
-            if (i < m && j <= i) L[tri_index(i, j)] -= acc[q][u];
-          }
-      }
-    }
-    __syncthreads();
-  }
-}
-
-// Blocked solves with the packed factor whose diagonal blocks hold their
-// inverses (all threads of the block call them): forward L z = v, backward
-// L^T x = z, ``nr`` <= 2 right-hand sides of leading dimension ldv.  Per
-// 32-row block: a 32 x 32 product with the block inverse (warp w handles
-// right-hand side w), then the update of the other rows by all threads.
-__device__ void fwd_solve_blocked(const float *L, float *v, int ldv, int m, int nr) {
-  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
-  for (int k0 = 0; k0 < m; k0 += PB) {
-    const int kb = min(PB, m - k0);
-    if (warp < nr) {
-      float *vr = v + warp * ldv + k0;
-      float z = 0.f;
-      if (lane < kb) {
-        const float *xr = L + tri_index(k0 + lane, k0);
-        for (int cc = 0; cc <= lane; ++cc) z = fmaf(xr[cc], vr[cc], z);
-      }
-      __syncwarp();
-      if (lane < kb) vr[lane] = z;
-    }
-    __syncthreads();
-    const int rows = m - k0 - kb;
-    for (int t = tid; t < rows * nr; t += nt) {
-      const int r = t / rows, i = k0 + kb + t % rows;
-      const float *row = L + tri_index(i, 0) + k0;
-      const float *xv = v + r * ldv + k0;
-      float acc = 0.f;
-      for (int cc = 0; cc < kb; ++cc) acc = fmaf(row[cc], xv[cc], acc);
-      v[r * ldv + i] -= acc;
-    }
-    __syncthreads();
-  }
-}
-
-__device__ void bwd_solve_blocked(const float *L, float *v, int ldv, int m, int nr) {
-  const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
-  if (m <= 0) return;
-  for (int k0 = ((m - 1) / PB) * PB; k0 >= 0; k0 -= PB) {
-    const int kb = min(PB, m - k0);
-    if (warp < nr) {
-      float *vr = v + warp * ldv + k0;
-      float z = 0.f;
-      if (lane < kb)
-        for (int cc = lane; cc < kb; ++cc) z = fmaf(L[tri_index(k0 + cc, k0 + lane)], vr[cc], z);
-      __syncwarp();
-      if (lane < kb) vr[lane] = z;
-    }
-    __syncthreads();
-    for (int t = tid; t < k0 * nr; t += nt) {
-      const int r = t / k0, i = t % k0;
-      const float *xv = v + r * ldv + k0;
-      float acc = 0.f;
-      for (int cc = 0; cc < kb; ++cc) acc = fmaf(L[tri_index(k0 + cc, i)], xv[cc], acc);
-      v[r * ldv + i] -= acc;
-    }
-    __syncthreads();
-  }
-}
 
 constexpr int EEQ_REFINE_MAX = 8;
 constexpr int EEQ_THREADS = 256;
@@ -1414,7 +1245,12 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
     cudaFuncSetAttribute(atm_mixed_kernel<SMEM, GRAD, PGRAD>,
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int threads = PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS;
-  atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(ATM_KMAX, c.B), threads, smem, st>>>(c);
+  const int K = SMEM ? ATM_KMAX : atm_ctas_big(c.N);
+  atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(K, c.B), threads, smem, st>>>(c);
+  if (!SMEM && GRAD) {
+    const int T = (c.N + 31) / 32;
+    atm_mirror_kernel<<<dim3(T, T, c.B), 256, 0, st>>>(c);
+  }
 }
 
 int launch_mixed(const Ctx &c, cudaStream_t st) {
@@ -1434,7 +1270,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   const size_t vec_bytes = 4 * eeq_mixed_vec_floats(N);
   const size_t tri_bytes = (size_t)4 * ((size_t)N * (N + 1) / 2);
   const size_t pt_bytes = (size_t)4 * PB * chol_panel_ld(N);
-  const bool eeq_smem = vec_bytes + pt_bytes + tri_bytes <= 220 * 1024;
+  const bool eeq_smem = eeq_small_fits(N);
   stage_begin(ST_EEQ, st);
   if (eeq) {
     eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
@@ -1443,9 +1279,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
                            (int)(vec_bytes + pt_bytes + tri_bytes));
       eeq_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + pt_bytes + tri_bytes, st>>>(c);
     } else {
-      cudaFuncSetAttribute(eeq_mixed_kernel<false>,
-                           cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
-      eeq_mixed_kernel<false><<<B, EEQ_THREADS, vec_bytes, st>>>(c);
+      launch_eeq_big(c, st, false);
     }
   } else {
     launch_charges_in(c, st);
@@ -1494,9 +1328,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
                              (int)(vec_bytes + tri_bytes));
         eeq_adjoint_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + tri_bytes, st>>>(c);
       } else {
-        cudaFuncSetAttribute(eeq_adjoint_mixed_kernel<false>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize, (int)vec_bytes);
-        eeq_adjoint_mixed_kernel<false><<<B, EEQ_THREADS, vec_bytes, st>>>(c);
+        launch_eeq_big(c, st, true);
       }
       stage_end(ST_EEQ_ADJ, st);
     }

@@ -150,3 +150,46 @@ def test_float32_inputs_use_precision_form(d4):
     e = d4.dftd4(nt.to(dev), pt.to(dev, torch.float32), ct.to(dev), PARAM)
     assert e.dtype == torch.float32
     assert np.abs(e.double().cpu().numpy().sum(-1) - e_ref.numpy().sum(-1)).max() <= 1e-6
+
+
+def _runner(nt, pt, ct, precision):
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    runner, _, _ = disp._prepare(nt, pt, ct, PARAM, "d4", None, None, None, None, None,
+                                 None, None, None, precision)
+    return runner
+
+
+@pytest.mark.parametrize("sizes,pad", [((330, 380), 400), ((700,), 700)],
+                         ids=["two-structures-N400", "one-structure-N700"])
+def test_multi_cta_eeq_and_atm_match_fp64_path(d4, sizes, pad):
+    """Structures padded beyond the one-CTA EEQ limit (N > 290) take the
+    multi-CTA factorisation (128-column panels, SYRK trailing updates, block
+    sweeps) and the task-parallel global ATM; charges, energies and forces
+    match the plain FP64 path within the precision bar, and the charges
+    match an FP64 solve of the same EEQ system (the precision form's own
+    coordination numbers) to 1e-9."""
+    wl = package().workloads
+    structs = [wl.structure(310 + k, n) for k, n in enumerate(sizes)]
+    B = len(sizes)
+    numbers = np.zeros((B, pad), dtype=np.int64)
+    positions = np.zeros((B, pad, 3))
+    for k, (z, r) in enumerate(structs):
+        numbers[k, :len(z)] = z
+        positions[k, :len(z)] = r
+    charge = np.array([1.0, -1.0][:B])
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (numbers, positions, charge))
+    mixed = _runner(nt, pt, ct, "mixed").run(pt, gradient=True, charges_out=True,
+                                             cn_eeq_out=True)
+    plain = _runner(nt, pt, ct, "fp64").run(pt, gradient=True, charges_out=True)
+    e, g, q, cnq = mixed[0], mixed[1], mixed[3].cpu(), mixed[5].cpu()
+    _check(e.cpu().numpy(), g.cpu().numpy(), plain[0].cpu().numpy(), plain[1].cpu().numpy())
+    # the precision form's FP32 coordination numbers move q by ~1e-7
+    assert (q - plain[3].cpu()).abs().max().item() < 1e-6
+    tables = oracle.load_tables()
+    for k in range(B):
+        q_ref = _eeq_fp64(torch.from_numpy(numbers[k]), torch.from_numpy(positions[k]),
+                          float(charge[k]), cnq[k], tables)
+        n = len(q_ref)
+        assert (q[k, :n] - q_ref).abs().max().item() < 1e-9
