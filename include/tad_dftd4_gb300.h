@@ -25,10 +25,15 @@
  * that can only be seen on the device (atomic number outside the tables,
  * a non-positive EEQ pivot, non-finite input) are reported through the
  * ``status`` word of the workspace; read it with ``d4_read_status`` after
- * the stream has been synchronised.
+ * the stream has been synchronised.  The status word is the first int32 of
+ * the workspace (byte offset D4_STATUS_OFFSET), so a caller that cannot
+ * synchronise (a captured CUDA graph) may copy it asynchronously instead; it
+ * is cleared at the start of every call.
  */
 #ifndef TAD_DFTD4_GB300_H
 #define TAD_DFTD4_GB300_H
+
+#define D4_STATUS_OFFSET 0 /* byte offset of the device status word in a workspace */
 
 #include <stddef.h>
 #include <stdint.h>

@@ -37,6 +37,7 @@ FLAG_GRADIENT = 1
 FLAG_CHARGES_IN = 2
 FLAG_MIXED = 4
 FLAG_PARAM_GRAD = 8
+STATUS_OFFSET = 0  # D4_STATUS_OFFSET: byte offset of the device status word in a workspace
 
 
 class Tables(ctypes.Structure):

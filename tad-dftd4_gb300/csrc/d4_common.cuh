@@ -102,7 +102,12 @@ struct Workspace {
   float *A32;       // [B*S*23*N] (transposed: atoms contiguous per frequency)
   float *A032;      // [B*S*23*N]
   float *dA32;      // [B*N*S*23*3] (dA/dCN, dA/dq, dA0/dCN) per atom, slot, frequency
-  float *alpha32;   // [MAX_ELEM_ID*7*23] reference polarisabilities
+  float *alpha32;   // [MAX_ELEM_ID*7*23] reference polarisabilities (double-float hi
+  float *alpha32lo; //                     and lo parts)
+  float *z0lo;      // [MAX_ELEM_ID*7] low part of zeta at q = 0 (hi in ref32.w)
+  float2 *sfw;      // [32] sqrt((3/pi) w) of the Casimir-Polder weights, double-float
+  float4 *pairA;    // [MAX_ELEM_ID^2] (R0, qq) per element pair, double-floats (hi, lo, hi, lo)
+  float4 *pairB;    // [MAX_ELEM_ID^2] (R0^6, R0^8) per element pair, double-floats
   float4 *ref32;    // [MAX_ELEM_ID*7] (refcovcn, refq + zeff, Gaussians, zeta at q = 0)
   float2 *el32;     // [MAX_ELEM_ID] (zeff, gam * gc)
   float *G32;       // [B*N*S*23] dE/dA
@@ -192,6 +197,11 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.A032 = (float *)take(4 * BNS23);
     w.dA32 = grad ? (float *)take(4 * 3 * BNS23) : nullptr;
     w.alpha32 = (float *)take(4 * (size_t)MAX_ELEM_ID * NREF * NFREQ);
+    w.alpha32lo = (float *)take(4 * (size_t)MAX_ELEM_ID * NREF * NFREQ);
+    w.z0lo = (float *)take(4 * (size_t)MAX_ELEM_ID * NREF);
+    w.sfw = (float2 *)take(8 * 32);
+    w.pairA = (float4 *)take(16 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
+    w.pairB = (float4 *)take(16 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
     w.ref32 = (float4 *)take(16 * (size_t)MAX_ELEM_ID * NREF);
     w.el32 = (float2 *)take(8 * (size_t)MAX_ELEM_ID);
     w.G32 = grad ? (float *)take(4 * BNS23) : nullptr;
@@ -295,6 +305,16 @@ __device__ __forceinline__ void zeta_and_deriv(double gam, double qref, double q
 
 __host__ __device__ inline size_t tri_index(int i, int j) {  // packed lower, j <= i
   return (size_t)i * (i + 1) / 2 + j;
+}
+
+// r_i - r_j from the FP32 positions relative to the structure's first atom
+// (pos32) and their low parts (pos32lo): the high parts of nearby atoms
+// subtract exactly, the low parts restore what rounding the absolute
+// positions to FP32 lost (about 4e-6 Bohr at 60 Bohr from the origin).
+__device__ __forceinline__ float3 pos_diff(const float4 &pi, const float4 &li, const float4 &pj,
+                                          const float4 &lj) {
+  return make_float3((pi.x - pj.x) + (li.x - lj.x), (pi.y - pj.y) + (li.y - lj.y),
+                     (pi.z - pj.z) + (li.z - lj.z));
 }
 
 __device__ __forceinline__ float warp_sumf(float v) {

@@ -86,11 +86,13 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
     if (ok) {
       const double *p = c.positions + 3 * a;
       const double dx = p[0] - p0[0], dy = p[1] - p0[1], dz = p[2] - p0[2];
-      c.w.pos32[a] = make_float4((float)dx, (float)dy, (float)dz, (float)sqrt(atom_r4r2(c, a, z)));
-      if (c.w.pos32lo)
+      const double sr = sqrt(atom_r4r2(c, a, z));
+      c.w.pos32[a] = make_float4((float)dx, (float)dy, (float)dz, (float)sr);
+      if (c.w.pos32lo)  // low parts (positions and sqrt(r4r2)) of the double-float copies
         c.w.pos32lo[a] = make_float4((float)(dx - (double)(float)dx),
                                      (float)(dy - (double)(float)dy),
-                                     (float)(dz - (double)(float)dz), 0.f);
+                                     (float)(dz - (double)(float)dz),
+                                     (float)(sr - (double)(float)sr));
       c.w.aux32[a] = make_float4((float)c.tab.cov_d3[z], (float)c.tab.en[z],
                                  (float)c.tab.eeq_rad[z], 0.f);
     } else {

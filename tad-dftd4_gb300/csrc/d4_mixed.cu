@@ -38,19 +38,29 @@ __global__ void tables32_kernel(Ctx c) {
   const int nz = c.tab.n_ref_elem < MAX_ELEM_ID ? c.tab.n_ref_elem : MAX_ELEM_ID;
   if (t < MAX_ELEM_ID * NREF * NFREQ) {
     const int z = t / (NREF * NFREQ);
-    c.w.alpha32[t] = z < nz ? (float)c.tab.alpha[t] : 0.f;
+    const dfl a = z < nz ? df_from(c.tab.alpha[t]) : dfl{0.f, 0.f};
+    c.w.alpha32[t] = a.hi;
+    c.w.alpha32lo[t] = a.lo;
+  }
+  if (t < NFREQ) {
+    const dfl f = df_from(sqrt(THOPI * c.tab.freq_weights[t]));
+    c.w.sfw[t] = make_float2(f.hi, f.lo);
   }
   if (t < MAX_ELEM_ID * NREF) {
     const int z = t / NREF;
     float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    float z0lo = 0.f;
     if (z < nz && z < c.tab.n_elem) {
       const double zeff = (double)c.tab.zeff[z];
       const double qref = c.tab.refq[t] + zeff;
       double z0, dz0;
       zeta_and_deriv(c.tab.gam[z] * c.cfg.gc, qref, zeff, c.cfg.ga, DBL_EPSILON, &z0, &dz0);
-      v = make_float4((float)c.tab.refcovcn[t], (float)qref, (float)c.tab.refc[t], (float)z0);
+      const dfl zz = df_from(z0);
+      v = make_float4((float)c.tab.refcovcn[t], (float)qref, (float)c.tab.refc[t], zz.hi);
+      z0lo = zz.lo;
     }
     c.w.ref32[t] = v;
+    c.w.z0lo[t] = z0lo;
   }
   if (t < MAX_ELEM_ID) {
     float2 e = make_float2(0.f, 0.f);
@@ -65,6 +75,20 @@ __global__ void tables32_kernel(Ctx c) {
     const double x0 = (double)t / (double)ERF_SCALE;
     const dfl e = df_from(erf(x0)), d = df_from(2.0 / sqrt(M_PI) * exp(-x0 * x0));
     c.w.erf_tab[t] = make_float4(e.hi, e.lo, d.hi, d.lo);
+  }
+  if (t < MAX_ELEM_ID * MAX_ELEM_ID) {  // R0, qq, R0^6, R0^8 of the table r4r2 values
+    const int za = t / MAX_ELEM_ID, zb = t % MAX_ELEM_ID;
+    float4 A = make_float4(0.f, 0.f, 0.f, 0.f), Bq = A;
+    if (za < c.tab.n_elem && zb < c.tab.n_elem) {
+      const double qq = 3.0 * c.tab.r4r2[za] * c.tab.r4r2[zb];
+      const double R0 = c.par.a1 * sqrt(qq) + c.par.a2;
+      const double R02 = R0 * R0, R06 = R02 * R02 * R02;
+      const dfl r0 = df_from(R0), q = df_from(qq), r6 = df_from(R06), r8 = df_from(R06 * R02);
+      A = make_float4(r0.hi, r0.lo, q.hi, q.lo);
+      Bq = make_float4(r6.hi, r6.lo, r8.hi, r8.lo);
+    }
+    c.w.pairA[t] = A;
+    c.w.pairB[t] = Bq;
   }
   if (t < MAX_ELEM_ID * MAX_ELEM_ID) {  // 1 / sqrt(rad_a^2 + rad_b^2)
     const int za = t / MAX_ELEM_ID, zb = t % MAX_ELEM_ID;
@@ -118,6 +142,7 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
     const double wf = d4s ? c.tab.wfpair[zi * c.tab.n_elem + c.w.slot_elem[b * MAX_ELEM_ID + s]]
                           : c.cfg.wf;
     const float4 *R = c.w.ref32 + zi * NREF;
+    const float *Z0L = c.w.z0lo + zi * NREF;
     float4 rv[NREF];
     float dcn[NREF], cf[NREF], dq[NREF];
     double y64[NREF];
@@ -176,35 +201,44 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
           z = expf(ga);
           dz = 0.f;
         }
-        const float z0 = rv[r].w;
+        const float z0 = rv[r].w, z0l = Z0L[r];  // zeta(q = 0) as a double-float
         gq[r] = z * gw;
-        g0[r] = z0 * gw;
+        g0[r] = fmaf(z0l, gw, z0 * gw);
         dgc[r] = z * dgw;
         dgq[r] = dz * gw;
-        dg0[r] = z0 * dgw;
+        dg0[r] = fmaf(z0l, dgw, z0 * dgw);
       }
     }
   }
+  // A'(w) = sqrt((3/pi) w_w) sum_r g_r alpha_r(w): the Casimir-Polder weight
+  // is folded into A so that C6 = sum_w A'_i A'_j carries no rounded weight;
+  // alpha and the scale are double-floats, so the only roundings are the
+  // FP32 sums of each atom (no bias shared by all atoms of an element)
   const float *al = c.w.alpha32 + (size_t)zi * NREF * NFREQ;
+  const float *all = c.w.alpha32lo + (size_t)zi * NREF * NFREQ;
   for (int w = 0; w < NFREQ; ++w) {
     float a = 0.f, a0 = 0.f, da_dcn = 0.f, da_dq = 0.f, da0_dcn = 0.f;
+    float al_ = 0.f, al0 = 0.f;
 #pragma unroll
     for (int r = 0; r < NREF; ++r) {
-      const float v = al[r * NFREQ + w];
+      const float v = al[r * NFREQ + w], vl = all[r * NFREQ + w];
       a = fmaf(gq[r], v, a);
+      al_ = fmaf(gq[r], vl, al_);
       a0 = fmaf(g0[r], v, a0);
+      al0 = fmaf(g0[r], vl, al0);
       da_dcn = fmaf(dgc[r], v, da_dcn);
       da_dq = fmaf(dgq[r], v, da_dq);
       da0_dcn = fmaf(dg0[r], v, da0_dcn);
     }
+    const float2 f = c.w.sfw[w];
     const size_t t = a32_index(b, i, s, w, N, S);
-    c.w.A32[t] = a;
-    c.w.A032[t] = a0;
+    c.w.A32[t] = fmaf(a, f.x, fmaf(a, f.y, al_ * f.x));
+    c.w.A032[t] = fmaf(a0, f.x, fmaf(a0, f.y, al0 * f.x));
     if (grad) {
       float *d = c.w.dA32 + 3 * ((ai * S + s) * NFREQ + w);
-      d[0] = da_dcn;
-      d[1] = da_dq;
-      d[2] = da0_dcn;
+      d[0] = da_dcn * f.x;
+      d[1] = da_dq * f.x;
+      d[2] = da0_dcn * f.x;
     }
   }
 }
@@ -234,15 +268,17 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
     return;
   }
   const float4 *P = c.w.pos32 + (size_t)b * N;
+  const float4 *PL = c.w.pos32lo + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
-  const float4 pi = P[i], xi = X[i];
+  const float4 pi = P[i], li = PL[i], xi = X[i];
   const float kcn = c.pf.kcn, k4 = c.pf.k4, k5 = c.pf.k5, k6 = c.pf.k6;
   const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
   Acc32 s_d4, s_q;
   for (int j = lane; j < n; j += 32) {
     if (j == i || c.w.z[(size_t)b * N + j] == 0) continue;
     const float4 pj = P[j], xj = X[j];
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float3 d = pos_diff(pi, li, pj, PL[j]);
+    const float dx = d.x, dy = d.y, dz = d.z;
     const float r = sqrtf(dx * dx + dy * dy + dz * dz);
     const float x = kcn * (r / (xi.x + xj.x) - 1.0f);
     if (x > 9.0f) continue;  // erfc(9) / 2 < 1e-36
@@ -276,7 +312,7 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
 // r, 1/r, log(R0/r), sqrt(C6(q=0))), the direct gradient and the C6
 // adjoint.  One warp per atom i, lanes over partners j.
 template <bool GRAD, bool PGRAD>
-__global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
+__global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   const int b = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + warp;
@@ -304,21 +340,33 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
   const float s6 = c.pf.s6, s8 = c.pf.s8, s10 = c.pf.s10;
   const float a1 = c.pf.a1, a2 = c.pf.a2, cut2 = c.pf.cut2;
   const float4 *P = c.w.pos32 + (size_t)b * N;
-  const float4 pi = P[i];
+  const float4 *PL = c.w.pos32lo + (size_t)b * N;
+  const float4 pi = P[i], li = PL[i];
   const float wi = c.w.w32[ai];
   const int nslot = c.w.n_slots[b];
   const int slot_i = c.w.slot[ai];
   float4 *T = c.w.ptf + (size_t)ai * N;
   float4 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
   const float alp3_log2e = c.pf.alp3 * 1.4426950408889634f;
-  Acc32 e_acc, gx, gy, gz;
+  // R0 = a1 sqrt(qq) + a2, qq = 3 r4r2_i r4r2_j, R0^6 and R0^8 as
+  // double-floats, so that no FP32 rounding of a per-element-pair constant
+  // biases every pair of that element pair the same way: from the per-call
+  // element-pair table, or (per-atom r4r2 given) per pair from u_i = a1
+  // sqrt(3) s_i, v_i = sqrt(3) s_i (FP64 per atom) and s_j = pos32.w + pos32lo.w
+  const bool tabled = c.r4r2_in == nullptr;
+  // compensated sums of c6 t6 (with (s10/s6) c10 t10 folded in) and of
+  // c8 t8; s6 and s8 are applied in FP64 at the end (one FP32 sum of both
+  // orders, with s8/s6 as a double-float, measured 4x less accurate)
+  const double sref = p.s6 != 0.0 ? p.s6 : 1.0;
+  const dfl rho10 = df_from(p.has_s10 ? p.s10 / sref : 0.0);
+  const float rho6 = p.s6 != 0.0 ? 1.f : 0.f;
+  Acc32 e_acc, e8_acc, gx, gy, gz;
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  const float fw_l = lane < NFREQ ? c.w.fw32[lane] : 0.f;  // (3/pi) w_lane
   for (int s = 0; s < nslot; ++s) {
-    if (lane < NFREQ) {
+    if (lane < NFREQ) {  // A' already carries sqrt((3/pi) w): C6 = sum_w A'_i A'_j
       const size_t o = a32_index(b, i, s, lane, N, c.S);
-      s_wa[warp][lane] = fw_l * c.w.A32[o];
-      s_wa0[warp][lane] = fw_l * c.w.A032[o];
+      s_wa[warp][lane] = c.w.A32[o];
+      s_wa0[warp][lane] = c.w.A032[o];
     }
     __syncwarp();
     float gacc[NFREQ];
@@ -329,7 +377,8 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       const int zj = c.w.z[aj];
       if (j == i || zj == 0 || c.w.slot[aj] != s) continue;
       const float4 pj = P[j];
-      const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+      const float3 d = pos_diff(pi, li, pj, PL[j]);
+      const float dx = d.x, dy = d.y, dz = d.z;
       const float r2 = dx * dx + dy * dy + dz * dz;
       const float ir = rsqrtf(r2);
       const float r = r2 * ir;
@@ -341,42 +390,60 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
         c6 = fmaf(s_wa[warp][w], Aj[(size_t)w * N], c6);
         c60 = fmaf(s_wa0[warp][w], A0j[(size_t)w * N], c60);
       }
-      const float sqq = SQRT3_F * pi.w * pj.w;  // sqrt(3 r4r2_i r4r2_j)
-      const float qq = sqq * sqq;
-      const float R0 = fmaf(a1, sqq, a2);
-      const float lnR0r = logf(R0 * ir);
+      dfl R0d, qqd, R06d, R08d;
+      if (tabled) {  // per element pair, from the table r4r2 values
+        const float4 A = c.w.pairA[zi * MAX_ELEM_ID + zj], Bq = c.w.pairB[zi * MAX_ELEM_ID + zj];
+        R0d = {A.x, A.y};
+        qqd = {A.z, A.w};
+        R06d = {Bq.x, Bq.y};
+        R08d = {Bq.z, Bq.w};
+      } else {  // per-atom r4r2 given (rare): FP64 per pair
+        const double si = (double)pi.w + (double)li.w, sj = (double)pj.w + (double)PL[j].w;
+        const double qq = 3.0 * si * si * sj * sj;
+        const double R0 = p.a1 * sqrt(qq) + p.a2;
+        const double R02 = R0 * R0, R06 = R02 * R02 * R02;
+        R0d = df_from(R0);
+        qqd = df_from(qq);
+        R06d = df_from(R06);
+        R08d = df_from(R06 * R02);
+      }
+      const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
+      const float lnR0r = logf(R0 * ir) + R0d.lo / R0;
       T[j] = make_float4(r2, ir, alp3_log2e * lnR0r, sqrtf(c60));
       if (PGRAD) Tda[j] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
       if (r <= cut2) {
-        const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R02 * R02 * R02;
-        const float t6 = 1.0f / (r6 + R06);
-        float e = s6 * c6 * t6;
+        const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R06d.hi;
+        const float t6 = 1.0f / ((r6 + R06) + R06d.lo);
+        float eterm = rho6 * c6 * t6;
         float dEdr = 6.0f * s6 * c6 * (r6 * ir) * t6 * t6;
         float K = -s6 * t6;
         float dE_dR0 = 6.0f * s6 * c6 * (R06 / R0) * t6 * t6;
         pg[0] -= wi * c6 * t6;
         if (p.has_s8) {
-          const float r8 = r6 * r2, R08 = R06 * R02;
-          const float t8 = 1.0f / (r8 + R08);
-          const float c8 = c6 * qq;
-          e += s8 * c8 * t8;
+          const float r8 = r6 * r2, R08 = R08d.hi, qq = qqd.hi;
+          const float t8 = 1.0f / ((r8 + R08) + R08d.lo);
+          const float c8 = fmaf(c6, qqd.hi, c6 * qqd.lo);
+          const float e8 = c8 * t8;
+          e8_acc.add(e8);
           dEdr += 8.0f * s8 * c8 * (r8 * ir) * t8 * t8;
           K -= s8 * qq * t8;
           dE_dR0 += 8.0f * s8 * c8 * (R08 / R0) * t8 * t8;
           pg[1] -= wi * c8 * t8;
         }
-        if (p.has_s10) {
+        if (p.has_s10) {  // rare: FP32 powers
+          const float qq = sqq * sqq;
           const float r10 = r6 * r2 * r2, R010 = R06 * R02 * R02;
           const float t10 = 1.0f / (r10 + R010);
           const float q2 = qq * qq * (49.0f / 40.0f);
           const float c10 = c6 * q2;
-          e += s10 * c10 * t10;
+          const float e10 = c10 * t10;
+          eterm = fmaf(rho10.hi, e10, fmaf(rho10.lo, e10, eterm));
           dEdr += 10.0f * s10 * c10 * (r10 * ir) * t10 * t10;
           K -= s10 * q2 * t10;
           dE_dR0 += 10.0f * s10 * c10 * (R010 / R0) * t10 * t10;
           pg[2] -= wi * c10 * t10;
         }
-        e_acc.add(-0.5f * e);
+        e_acc.add(eterm);
         const float phi = 0.5f * (wi + c.w.w32[aj]);
         dEdr *= phi;
         K *= phi;
@@ -399,13 +466,13 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
         const float g = warp_sumf(gacc[w]);
         if (lane == w) mine = g;
       }
-      if (lane < NFREQ) c.w.G32[(ai * c.S + s) * NFREQ + lane] = fw_l * mine;
+      if (lane < NFREQ) c.w.G32[(ai * c.S + s) * NFREQ + lane] = mine;  // dE/dA'_i
     }
     __syncwarp();
   }
   if (GRAD && lane < NFREQ)
     for (int s = nslot; s < c.S; ++s) c.w.G32[(ai * c.S + s) * NFREQ + lane] = 0.f;
-  const Acc32 ea = warp_sum_acc(e_acc);
+  const Acc32 ea = warp_sum_acc(e_acc), ea8 = warp_sum_acc(e8_acc);
   if (PGRAD) {
     float v[5];
 #pragma unroll
@@ -426,7 +493,8 @@ __global__ void __launch_bounds__(256) pair_fwd_mixed_kernel(Ctx c) {
       c.out.d_gradient[3 * ai + 2] = g2.value();
     }
   }
-  if (lane == 0) c.out.d_energy[ai] = ea.value();
+  if (lane == 0)
+    c.out.d_energy[ai] = -0.5 * (sref * ea.value() + (p.has_s8 ? p.s8 * ea8.value() : 0.0));
 }
 
 // ---------------------------------------------------------------- ATM
@@ -452,6 +520,7 @@ struct AtmAcc {
   float *sS, *sP, *sE;  // shared (SMEM): upper triangle and atoms
   float *gS, *gP;       // global pair blocks [N][N]
   double *gE;           // atom energies
+  double escale;        // s9 / 6: energies arrive in units of (triple energy without s9) / 6
   int n, N;
   __device__ __forceinline__ void pair(int j, int k, float S, float P) const {
     if (SMEM) {
@@ -467,7 +536,7 @@ struct AtmAcc {
     if (SMEM)
       atomicAdd(&sE[x], e);
     else
-      atomicAdd(&gE[x], (double)e);
+      atomicAdd(&gE[x], (double)e * escale);
   }
 };
 
@@ -532,19 +601,20 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
         const float eu = c9 * fd * ang;  // triple energy without s9
         const float e = s9m * eu;
         float wgt;
+        // atom energies in units of e/6 (exact multiples; s9/6 is applied in
+        // FP64 when they leave the kernel, so no rounded 1/3 biases them)
         if (mij & mik & mjk) {
-          const float third = e * (1.0f / 3.0f);
-          ei = third;
-          Ej += third;
-          Ek += third;
+          const float e2 = eu + eu;
+          ei = e2;
+          Ej += e2;
+          Ek += e2;
           wgt = ((in.weighted ? W[i] : 1.f) + wj + wk) * (1.0f / 3.0f);
         } else {
           const float fij = mij, fik = mik, fjk = mjk;
           const float mi = fjk * (fij + fik), mj = fik * (fij + fjk), mk = fij * (fik + fjk);
-          const float sixth = e * (1.0f / 6.0f);
-          ei = sixth * mi;
-          Ej += sixth * mj;
-          Ek += sixth * mk;
+          ei = eu * mi;
+          Ej += eu * mj;
+          Ek += eu * mk;
           wgt = ((in.weighted ? W[i] : 1.f) * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
         }
         if (GRAD) {
@@ -640,6 +710,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   acc.gS = GRAD ? c.w.prS32 + (size_t)b * N * N : nullptr;
   acc.gP = GRAD ? c.w.prP32 + (size_t)b * N * N : nullptr;
   acc.gE = c.w.e3 + (size_t)b * N;
+  acc.escale = c.par.s9 / 6.0;
   if (SMEM) {
     for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
     __syncthreads();
@@ -706,8 +777,8 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
       }
     }
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
-      const float ev = acc.sE[x] * s9;
-      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev);  // once per atom
+      const float ev = acc.sE[x];
+      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev * acc.escale);
     }
   }
 }
@@ -759,12 +830,12 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
     return;
   }
   const float4 *P = c.w.pos32 + (size_t)b * N;
-  const float4 px = P[x];
+  const float4 *PL = c.w.pos32lo + (size_t)b * N;
+  const float4 px = P[x], lx = PL[x];
   const int nslot = c.w.n_slots[b];
   const int slot_x = c.w.slot[ax];
   const size_t base = (size_t)b * N * N;
   const float4 *T = c.w.ptf + base + (size_t)x * N;
-  const float fw_l = lane < NFREQ ? c.w.fw32[lane] : 0.f;  // (3/pi) w_lane
   Acc32 gx, gy, gz;
   Acc32 dcn_acc, dq_acc;
   for (int s = 0; s < nslot; ++s) {
@@ -777,10 +848,10 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
       const size_t o = base + (size_t)x * N + y;
       const float S = c.w.prS32[o];
       const float Pv = c.w.prP32[o];
-      const float4 py = P[y];
-      gx.add(2.0f * S * (px.x - py.x));
-      gy.add(2.0f * S * (px.y - py.y));
-      gz.add(2.0f * S * (px.z - py.z));
+      const float3 d = pos_diff(px, lx, P[y], PL[y]);
+      gx.add(2.0f * S * d.x);
+      gy.add(2.0f * S * d.y);
+      gz.add(2.0f * S * d.z);
       if (Pv != 0.f) {
         const float cc = T[y].w;
         const float D = Pv / (2.0f * cc * cc);
@@ -798,7 +869,7 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
     // chain rule to CN and q for this slot (lane = frequency)
     if (lane < NFREQ) {
       const size_t o = (ax * c.S + s) * NFREQ + lane;
-      const float g0w = fw_l * mine;
+      const float g0w = mine;  // dE/dA'0_x
       const float gw = c.w.G32[o];
       const float *d = c.w.dA32 + 3 * o;
       dcn_acc.add(gw * d[0]);
@@ -836,13 +907,15 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
   const float4 *D = c.w.adj32 + (size_t)b * N;
-  const float4 pi = P[i], xi = X[i], di = D[i];
+  const float4 *PL = c.w.pos32lo + (size_t)b * N;
+  const float4 pi = P[i], li = PL[i], xi = X[i], di = D[i];
   Acc32 gx, gy, gz;
   for (int j = lane; j < n; j += 32) {
     const size_t aj = (size_t)b * N + j;
     if (j == i || c.w.z[aj] == 0) continue;
     const float4 pj = P[j], xj = X[j], dj = D[j];
-    const float dx = pi.x - pj.x, dy = pi.y - pj.y, dz = pi.z - pj.z;
+    const float3 d = pos_diff(pi, li, pj, PL[j]);
+    const float dx = d.x, dy = d.y, dz = d.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
     const float ir = rsqrtf(r2);
     const float r = r2 * ir;
