@@ -44,6 +44,19 @@ __host__ __device__ inline size_t eeq_small_bytes(int N) {
 __host__ __device__ inline bool eeq_small_fits(int N) { return eeq_small_bytes(N) <= 220 * 1024; }
 constexpr int EEQ_BIG_REFINE = 4;  // refinement iterations of the multi-CTA path at most
 
+// ---------------------------------------------------------------- ATM sizes
+
+// The precision-form ATM accumulates a structure's pair adjoints in shared
+// memory (upper triangle + atoms, FP32) when the padded size allows it
+// (N <= 234); larger structures accumulate in global memory and get
+// neighbour lists for the neighbour-triple variant.
+__host__ __device__ inline size_t atm_smem_bytes(int N) {
+  return (size_t)4 * ((size_t)N * (N - 1) + N);
+}
+__host__ __device__ inline bool atm_smem_fits(int N) { return atm_smem_bytes(N) <= 220 * 1024; }
+// Largest neighbour count of a centre atom in the neighbour-triple ATM.
+constexpr int ATM_SPARSE_DMAX = 2048;
+
 
 struct Workspace {
   int *status;      // [1]
@@ -120,6 +133,9 @@ struct Workspace {
   float2 *eeq_X;    // [B*2*N] double-float solution (multi-CTA)
   float2 *eeq_B;    // [B*2*N] double-float right-hand sides (multi-CTA)
   unsigned *eeq_res;  // [B*EEQ_BIG_REFINE] max |residual| per iteration (float bits)
+  int *nbr;         // [B*N*N] ATM neighbour lists: row j = atoms within disp3 of j, ascending
+  int *nbr_deg;     // [B*N] neighbours per atom
+  unsigned long long *atm_cnt;  // [B*2] (sum_j deg_j (deg_j - 1) / 2, max_j deg_j)
   size_t bytes;
 };
 
@@ -216,6 +232,11 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
       w.eeq_X = (float2 *)take(8 * 2 * BN);
       w.eeq_B = (float2 *)take(8 * 2 * BN);
       w.eeq_res = (unsigned *)take(4 * (size_t)B * EEQ_BIG_REFINE);
+    }
+    if (!atm_smem_fits(N)) {
+      w.nbr = (int *)take(sizeof(int) * BNN);
+      w.nbr_deg = (int *)take(sizeof(int) * BN);
+      w.atm_cnt = (unsigned long long *)take(8 * 2 * (size_t)B);
     }
   }
   w.bytes = align_up(off, 256);

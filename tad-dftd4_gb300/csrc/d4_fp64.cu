@@ -1172,6 +1172,7 @@ void launch_prep(const Ctx &c, cudaStream_t st) {
     if (c.w.prS32) cudaMemsetAsync(c.w.prS32, 0, 4 * bnn, st);
     if (c.w.prP32) cudaMemsetAsync(c.w.prP32, 0, 4 * bnn, st);
   }
+  if (c.w.atm_cnt) cudaMemsetAsync(c.w.atm_cnt, 0, 8 * 2 * (size_t)c.B, st);
   prep_kernel<<<c.B, 256, 0, st>>>(c);
 }
 

@@ -664,6 +664,20 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
   if (kok && Ek != 0.f) acc.energy(k, Ek);
 }
 
+// Whether the ATM of structure b runs over neighbour triples (centre-atom
+// enumeration, atm_sparse_kernel) instead of all triples i < j < k: when
+// every centre's neighbour list fits the kernel's shared memory and the
+// centre-pair visits, sum_j deg_j (deg_j - 1) / 2, are fewer than half the
+// n (n - 1) (n - 2) / 6 triples.  Counts come from atm_nbr_kernel; only
+// structures of the global-accumulation path (N > 234) have them.
+__device__ __forceinline__ bool atm_sparse_mode(const Ctx &c, int b, int n) {
+  if (c.w.atm_cnt == nullptr) return false;
+  const unsigned long long visits = c.w.atm_cnt[2 * b], dmax = c.w.atm_cnt[2 * b + 1];
+  const unsigned long long nn = (unsigned long long)n;
+  const unsigned long long all = nn * (nn - 1) * (nn - 2) / 6;
+  return dmax <= (unsigned long long)ATM_SPARSE_DMAX && 2 * visits < all;
+}
+
 // CTAs per structure of the global-accumulation ATM (large structures):
 // about ATM_BIG_TRIPLES triples each, at most ATM_BIG_KMAX.
 constexpr long long ATM_BIG_TRIPLES = 250000;
@@ -698,6 +712,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   if (n < 3) return;
   const int K = SMEM ? atm_ctas(n) : atm_ctas_big(n);
   if (cta >= K) return;
+  if (!SMEM && atm_sparse_mode(c, b, n)) return;  // the neighbour-triple kernel takes it
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
   const int P = n * (n - 1) / 2;
@@ -807,6 +822,217 @@ __global__ void atm_mirror_kernel(Ctx c) {
     if (i < n && j < n && i > j) {
       S[(size_t)i * N + j] = sS[tx][r];
       P[(size_t)i * N + j] = sP[tx][r];
+    }
+  }
+}
+
+// ---------------------------------------------------------------- ATM over neighbour triples
+
+// Neighbour lists of the ATM (global-accumulation structures): for every
+// real atom j the real atoms k != j with r_jk <= disp3, ascending, taken
+// from the r^2 of the pair records; the per-structure counts decide between
+// the two ATM variants (atm_sparse_mode).  One warp per atom, ballot
+// compaction.
+__global__ void __launch_bounds__(256) atm_nbr_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int j = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  if (j >= N) return;
+  const size_t bN = (size_t)b * N;
+  if (j >= n || c.w.z[bN + j] == 0) {
+    if (lane == 0) c.w.nbr_deg[bN + j] = 0;
+    return;
+  }
+  const float cut2 = c.pf.cut3 * c.pf.cut3;
+  const float4 *T = c.w.ptf + (bN + j) * N;
+  int *L = c.w.nbr + (bN + j) * N;
+  const int *Z = c.w.z + bN;
+  int base = 0;
+  for (int k0 = 0; k0 < n; k0 += 32) {
+    const int k = k0 + lane;
+    bool ok = false;
+    if (k < n && k != j && Z[k] != 0) ok = T[k].x <= cut2;
+    const unsigned m = __ballot_sync(0xffffffffu, ok);
+    if (ok) L[base + __popc(m & ((1u << lane) - 1u))] = k;
+    base += __popc(m);
+  }
+  if (lane == 0) {
+    c.w.nbr_deg[bN + j] = base;
+    const unsigned long long d = (unsigned long long)base;
+    atomicAdd(&c.w.atm_cnt[2 * b], d * (d > 0 ? d - 1 : 0) / 2);
+    atomicMax(&c.w.atm_cnt[2 * b + 1], d);
+  }
+}
+
+constexpr int ATM_SPARSE_THREADS = 512;
+
+// ATM energy and adjoint over the neighbour triples of one centre atom j
+// (one CTA): every pair (i, k), i < k, of atoms within disp3 of j is a triple
+// whose sides r_ij and r_jk are inside the cutoff.  Each unordered triple is
+// taken once: with r_ik > disp3 its centre is unique; with all three sides
+// inside, only at the centre of smallest index (j < i).  The arithmetic, the
+// reference's per-atom attribution (threebody.py:153-163; here [ij] = [jk]
+// = 1) and the adjoint are those of atm_task.
+// Shared memory per list entry a (atom L[a]): the (j, L[a]) pair record, the
+// entry's dE/d(r^2) and weighted-energy sums of the pair (j, L[a]) and its
+// energy (units of e/6, s9 applied at the flush).  The (i, k) pair sums go
+// to the global upper-half accumulators directly; atm_mirror_kernel fills
+// the lower half afterwards.
+template <bool GRAD, bool PGRAD>
+__global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c) {
+  extern __shared__ float4 s_rec[];  // [ATM_SPARSE_DMAX] records, then L, S, P, E
+  int *s_L = reinterpret_cast<int *>(s_rec + ATM_SPARSE_DMAX);
+  float *s_S = reinterpret_cast<float *>(s_L + ATM_SPARSE_DMAX);
+  float *s_P = s_S + ATM_SPARSE_DMAX;
+  float *s_E = s_P + ATM_SPARSE_DMAX;
+  __shared__ float s_red[ATM_SPARSE_THREADS / 32];
+  const int b = blockIdx.y, j = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  if (j >= n || n < 3 || !atm_sparse_mode(c, b, n)) return;
+  const size_t bN = (size_t)b * N;
+  if (c.w.z[bN + j] == 0) return;
+  const int d = c.w.nbr_deg[bN + j];  // <= ATM_SPARSE_DMAX in sparse mode
+  if (d < 2) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const float4 *T = c.w.ptf + bN * N;
+  const float4 *Tda = PGRAD ? c.w.ptf_da + bN * N : nullptr;
+  const int *L = c.w.nbr + (bN + j) * N;
+  for (int t = threadIdx.x; t < d; t += blockDim.x) {
+    const int k = L[t];
+    s_L[t] = k;
+    s_rec[t] = T[(size_t)j * N + k];
+    s_S[t] = 0.f;
+    s_P[t] = 0.f;
+    s_E[t] = 0.f;
+  }
+  __syncthreads();
+  const float *W = c.w.w32 + bN;
+  const bool weighted = c.weights != nullptr;
+  const float cut2 = c.pf.cut3 * c.pf.cut3, alp3 = c.pf.alp3, s9 = c.pf.s9;
+  float *gS = GRAD ? c.w.prS32 + bN * N : nullptr;
+  float *gP = GRAD ? c.w.prP32 + bN * N : nullptr;
+  const float wj = W[j];
+  float Ej = 0.f;
+  AtmPg pg;
+  for (int a = warp; a < d - 1; a += nwarps) {
+    const int i = s_L[a];
+    const float4 pij = s_rec[a];
+    const float wi = weighted ? W[i] : 1.f;
+    const float4 *Ti = T + (size_t)i * N;
+    const bool later = j < i;  // j is the smallest atom of every triple of this row
+    float sij = 0.f, pe = 0.f, ei = 0.f;
+    float4 daij = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (PGRAD) daij = Tda[(size_t)j * N + i];
+    for (int e = a + 1 + lane; e < d; e += 32) {
+      const int k = s_L[e];
+      const float4 pik = Ti[k];
+      const bool mik = pik.x <= cut2;
+      if (mik && !later) continue;  // counted at its smallest atom
+      const float4 pjk = s_rec[e];
+      const float x = pij.x, y = pik.x, z = pjk.x;
+      const float ir1 = pij.y * pjk.y * pik.y;
+      const float ir2 = ir1 * ir1;
+      const float ir3 = ir1 * ir2;
+      const float u = x - y, v = x + y;
+      const float A = u + z, Bv = v - z, Cv = z - u;
+      const float sfac = A * Bv * Cv;
+      const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
+      const float ta = exp2f(pij.z + pik.z + pjk.z);
+      const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
+      const float c9 = pij.w * pik.w * pjk.w;
+      const float eu = c9 * fd * ang;  // triple energy without s9
+      const float wk = weighted ? W[k] : 1.f;
+      float wgt;
+      if (mik) {  // all sides inside: e/3 to each atom
+        const float e2 = eu + eu;
+        ei += e2;
+        Ej += e2;
+        atomicAdd(&s_E[e], e2);
+        wgt = (wi + wj + wk) * (1.0f / 3.0f);
+      } else {  // r_ik outside: e/6 to i and to k, nothing to the centre
+        ei += eu;
+        atomicAdd(&s_E[e], eu);
+        wgt = (wi + wk) * (1.0f / 6.0f);
+      }
+      if (GRAD) {
+        const float kc9 = s9 * c9;
+        const float dfl = alp3 * fd * (1.0f - fd);
+        const float Q = 2.0f * ir3 - 5.0f * ang;
+        const float U = 0.375f * kc9 * fd * ir2 * ir3;
+        const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
+        const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
+        const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
+        const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
+        const float dez = fmaf(U, BC + AB - AC, V * pjk.y * pjk.y);
+        const float we = wgt * s9 * eu;
+        sij = fmaf(wgt, dex, sij);
+        pe += we;
+        atomicAdd(&s_S[e], wgt * dez);
+        atomicAdd(&s_P[e], we);
+        atomicAdd(&gS[(size_t)i * N + k], wgt * dey);  // i < k: upper half
+        atomicAdd(&gP[(size_t)i * N + k], we);
+        if (PGRAD) {
+          const float4 daik = Tda[(size_t)i * N + k];
+          const float4 dajk = Tda[(size_t)j * N + k];
+          const float lsum = daij.z + daik.z + dajk.z;
+          const float dfd = -fd * (1.0f - fd);
+          pg.s9 += wgt * eu;
+          pg.alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
+          const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
+          pg.a1 += dfa * (daij.x + daik.x + dajk.x);
+          pg.a2 += dfa * (daij.y + daik.y + dajk.y);
+        }
+      }
+    }
+    ei = warp_sumf(ei);
+    if (GRAD) {
+      sij = warp_sumf(sij);
+      pe = warp_sumf(pe);
+    }
+    if (lane == 0) {
+      if (ei != 0.f) atomicAdd(&s_E[a], ei);
+      if (GRAD && (sij != 0.f || pe != 0.f)) {
+        atomicAdd(&s_S[a], sij);
+        atomicAdd(&s_P[a], pe);
+      }
+    }
+  }
+  if (PGRAD) {
+    pg.s9 = warp_sumf(pg.s9);
+    pg.alp = warp_sumf(pg.alp);
+    pg.a1 = warp_sumf(pg.a1);
+    pg.a2 = warp_sumf(pg.a2);
+    if (lane == 0) {
+      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)pg.a1);
+      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)pg.a2);
+      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)pg.s9);
+      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)pg.alp);
+    }
+  }
+  Ej = warp_sumf(Ej);
+  if (lane == 0) s_red[warp] = Ej;
+  __syncthreads();
+  const double escale = c.par.s9 / 6.0;
+  if (threadIdx.x == 0) {
+    float t = 0.f;
+    for (int w = 0; w < nwarps; ++w) t += s_red[w];
+    if (t != 0.f) atomicAdd(&c.w.e3[bN + j], (double)t * escale);
+  }
+  for (int t = threadIdx.x; t < d; t += blockDim.x) {
+    const int k = s_L[t];
+    const float ev = s_E[t];
+    if (ev != 0.f) atomicAdd(&c.w.e3[bN + k], (double)ev * escale);
+    if (GRAD) {
+      const float sv = s_S[t], pv = s_P[t];
+      if (sv != 0.f || pv != 0.f) {
+        const size_t o = j < k ? (size_t)j * N + k : (size_t)k * N + j;  // upper half
+        atomicAdd(&gS[o], sv);
+        atomicAdd(&gP[o], pv);
+      }
     }
   }
 }
@@ -1319,7 +1545,14 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int threads = PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS;
   const int K = SMEM ? ATM_KMAX : atm_ctas_big(c.N);
+  if (!SMEM) atm_nbr_kernel<<<dim3((c.N + 7) / 8, c.B), 256, 0, st>>>(c);
   atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(K, c.B), threads, smem, st>>>(c);
+  if (!SMEM) {  // neighbour-triple variant; returns at once for dense structures
+    const int sp = ATM_SPARSE_DMAX * (16 + 4 * 4);
+    cudaFuncSetAttribute(atm_sparse_kernel<GRAD, PGRAD>,
+                         cudaFuncAttributeMaxDynamicSharedMemorySize, sp);
+    atm_sparse_kernel<GRAD, PGRAD><<<dim3(c.N, c.B), ATM_SPARSE_THREADS, sp, st>>>(c);
+  }
   if (!SMEM && GRAD) {
     const int T = (c.N + 31) / 32;
     atm_mirror_kernel<<<dim3(T, T, c.B), 256, 0, st>>>(c);
@@ -1370,8 +1603,8 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
     pair_fwd_mixed_kernel<false, false><<<atoms, 256, 0, st>>>(c);
   stage_end(ST_PAIR_FWD, st);
   // ATM: shared-memory accumulation when the largest structure fits
-  const size_t atm_smem = (size_t)4 * ((size_t)N * (N - 1) + N);
-  const bool atm_sm = atm_smem <= 220 * 1024;
+  const size_t atm_smem = atm_smem_bytes(N);
+  const bool atm_sm = atm_smem_fits(N);
   stage_begin(ST_ATM, st);
   if (atm_sm) {
     if (pgrad)

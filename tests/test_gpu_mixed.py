@@ -193,3 +193,60 @@ def test_multi_cta_eeq_and_atm_match_fp64_path(d4, sizes, pad):
                           float(charge[k]), cnq[k], tables)
         n = len(q_ref)
         assert (q[k, :n] - q_ref).abs().max().item() < 1e-9
+
+
+def _sparse_counts(z, r, cut3):
+    """Centre-pair visits and largest neighbour count of the neighbour-triple ATM."""
+    d2 = ((r[:, None, :] - r[None, :, :]) ** 2).sum(-1)
+    np.fill_diagonal(d2, np.inf)
+    deg = (d2 <= cut3 * cut3).sum(1).astype(np.int64)
+    return int((deg * (deg - 1) // 2).sum()), int(deg.max())
+
+
+def test_neighbour_triple_atm_matches_dense_fp64_path(d4):
+    """Structures whose disp3 sphere holds few of their atoms take the
+    neighbour-triple ATM (centre-atom enumeration; each triple once, with the
+    reference's per-atom attribution); a smaller, denser structure in the same
+    batch keeps the all-triples kernel.  Energies, forces, parameter gradients
+    and a non-uniform energy weighting match the plain FP64 path (all
+    triples, FP64) within the precision bar."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    cut3 = 15.0
+    structs = [wl.structure(320, 1100), wl.structure(321, 300, density=0.03)]
+    sparse = []
+    for z, r in structs:
+        n = len(z)
+        visits, dmax = _sparse_counts(z, r, cut3)
+        sparse.append(dmax <= 2048 and 2 * visits < n * (n - 1) * (n - 2) // 6)
+    assert sparse == [True, False]
+    pad = 1100
+    B = len(structs)
+    numbers = np.zeros((B, pad), dtype=np.int64)
+    positions = np.zeros((B, pad, 3))
+    for k, (z, r) in enumerate(structs):
+        numbers[k, :len(z)] = z
+        positions[k, :len(z)] = r
+    charge = np.array([0.0, 1.0])
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (numbers, positions, charge))
+    cutoff = d4.Cutoff(disp2=50.0, disp3=cut3)
+    param = dict(PARAM, alp=14.0)
+
+    def run(precision, **kw):
+        runner, _, _ = disp._prepare(nt, pt, ct, param, "d4", None, None, None, None, cutoff,
+                                     None, None, None, precision)
+        return runner.run(pt, **kw)
+
+    mixed = run("mixed", gradient=True, param_grad=True)
+    plain = run("fp64", gradient=True, param_grad=True)
+    _check(mixed[0].cpu().numpy(), mixed[1].cpu().numpy(), plain[0].cpu().numpy(),
+           plain[1].cpu().numpy())
+    pm, pp = mixed[2].cpu().numpy(), plain[2].cpu().numpy()
+    assert np.abs(pm - pp).max() <= 1e-6 * max(1.0, np.abs(pp).max()), (pm, pp)
+    w = torch.rand(nt.shape, dtype=torch.float64, generator=torch.Generator().manual_seed(7))
+    w = (w * (nt.cpu() != 0)).to(dev)
+    gm = run("mixed", gradient=True, weights=w)[1]
+    gp = run("fp64", gradient=True, weights=w)[1]
+    assert (gm - gp).abs().max().item() <= F_TOL
