@@ -54,7 +54,8 @@ typedef enum d4_status {
   D4_ERR_ELEMENT = 4,          /* atomic number outside the element tables */
   D4_ERR_EEQ_SINGULAR = 5,     /* EEQ matrix not positive definite */
   D4_ERR_NONFINITE = 6,        /* non-finite position or charge */
-  D4_ERR_TOO_MANY_ELEMENTS = 7 /* D4S: more distinct elements than slots */
+  D4_ERR_TOO_MANY_ELEMENTS = 7, /* D4S: more distinct elements than slots */
+  D4_ERR_DEVICE_TIMEOUT = 8     /* an on-device wait for the tensor cores ran out */
 } d4_status;
 
 /* Model variants (tad_dftd4.model): D4Model and D4SModel. */

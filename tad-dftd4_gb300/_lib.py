@@ -28,6 +28,7 @@ STATUS_NAMES = {
     5: "D4_ERR_EEQ_SINGULAR",
     6: "D4_ERR_NONFINITE",
     7: "D4_ERR_TOO_MANY_ELEMENTS",
+    8: "D4_ERR_DEVICE_TIMEOUT",
 }
 
 MODEL_D4 = 0

@@ -37,6 +37,7 @@ const char *d4_status_string(int status) {
     case D4_ERR_EEQ_SINGULAR: return "EEQ matrix is not positive definite";
     case D4_ERR_NONFINITE: return "non-finite position or charge";
     case D4_ERR_TOO_MANY_ELEMENTS: return "more distinct elements than D4S slots";
+    case D4_ERR_DEVICE_TIMEOUT: return "on-device wait for the tensor cores timed out";
     default: return "unknown status";
   }
 }

@@ -27,6 +27,7 @@ void timing_next_call();
 int launch_fp64(const Ctx &c, cudaStream_t st);
 int launch_mixed(const Ctx &c, cudaStream_t st);
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint);
+void launch_pair_fwd_tc(const Ctx &c, cudaStream_t st);  // D4, precision form (d4_c6tc.cu)
 
 // stages shared by the FP64 method and the precision form (d4_fp64.cu)
 void launch_prep(const Ctx &c, cudaStream_t st);

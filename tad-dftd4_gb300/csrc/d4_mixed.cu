@@ -1595,7 +1595,9 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   weights_mixed_kernel<<<dim3((unsigned)(((N + 127) / 128) * c.S), B), 128, 0, st>>>(c);
   stage_end(ST_WEIGHTS, st);
   stage_begin(ST_PAIR_FWD, st);
-  if (pgrad)
+  if (c.cfg.kind == D4_MODEL_D4)  // C6 on the tensor cores
+    launch_pair_fwd_tc(c, st);
+  else if (pgrad)
     pair_fwd_mixed_kernel<true, true><<<atoms, 256, 0, st>>>(c);
   else if (grad)
     pair_fwd_mixed_kernel<true, false><<<atoms, 256, 0, st>>>(c);
