@@ -19,7 +19,14 @@ Lines printed by rank 0 (one JSON line):
 * ``roofline``: the dominant kernel (ATM), algorithmic flops per launch
   divided by its CUDA-event duration in the timed steps, against the FP32
   FMA peak measured in this run;
-* ``cpu_baseline``: the float64 CPU oracle on a bounded sample.
+* ``cpu_baseline``: the float64 CPU oracle on a bounded sample;
+* ``large16k``: one 16000-atom structure in the precision form (pair / ATM
+  cutoffs 50 / 25 Bohr), seconds per energy + force evaluation and stage
+  times (``--no-large`` skips it).
+* ``serving``: the 20000-request stream through the continuous-batching
+  server in real time (structures/s, p50 / p99 latency) and saturated, for
+  the precision form and the plain FP64 kernels (``--serve-requests 0``
+  skips it).
 
 ``--impl reference`` times the CPU restatement of tad-dftd4 (the oracle) on
 the host cores for the same workload and metric.
@@ -59,6 +66,12 @@ def parse_args():
     ap.add_argument("--e2e-steps", type=int, default=None)
     ap.add_argument("--cpu-seconds", type=float, default=15.0)
     ap.add_argument("--no-cpu-baseline", action="store_true")
+    ap.add_argument("--no-large", action="store_true",
+                    help="skip the one-structure 16000-atom measurement")
+    ap.add_argument("--serve-requests", type=int, default=20000,
+                    help="requests of the serving stream (0 skips it)")
+    ap.add_argument("--serve-plain-requests", type=int, default=3000,
+                    help="requests of the saturated plain-FP64 serving run")
     return ap.parse_args()
 
 
@@ -292,6 +305,113 @@ def probe_peak(lib, pkg, dev, fp64: bool) -> float:
     return best
 
 
+# Kernels of one precision-form energy + gradient call of the D4 model with
+# EEQ charges on structures that fit the one-CTA EEQ / shared-memory ATM
+# (N <= 234): prep, element tables, CN, EEQ matrix, EEQ solve, weights,
+# pair (tensor-core C6), ATM, ATM / C6 adjoint, EEQ adjoint, CN adjoint,
+# finish.
+KERNELS_PER_CALL = 12
+
+
+def run_large(pkg, disp, lib, dev, steps: int = 3):
+    """One 16000-atom structure (H/C/N/O/S, density 0.01, neutral, pair and
+    ATM cutoffs 50 / 25 Bohr), precision form, energy + forces: seconds per
+    structure and per-stage times.  The inputs (10 GB of workspace) are far
+    larger than L2."""
+    import torch
+
+    batch = pkg.workloads.large16k(2)
+    n = batch.numbers.shape[1]
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (batch.numbers, batch.positions,
+                                                        batch.charge))
+    cutoff = pkg.Cutoff(disp2=50.0, disp3=25.0)
+    param = dict(pkg.workloads.BJ_PARAMS)
+    runner, _, _ = disp._prepare(nt, pt, ct, param, "d4", None, None, None, None, cutoff,
+                                 None, None, None, "mixed")
+    runner.run(pt, gradient=True)
+    torch.cuda.synchronize()
+    nstage = lib.d4_stage_count()
+    pkg._lib.check(lib.d4_timing_begin(steps), "timing")
+    ev = [torch.cuda.Event(enable_timing=True) for _ in range(steps + 1)]
+    ev[0].record()
+    for k in range(steps):
+        e, g, _, _, _ = runner.run(pt, gradient=True)
+        ev[k + 1].record()
+    torch.cuda.synchronize()
+    ms_stage = (ctypes.c_float * nstage)()
+    ncalls = ctypes.c_int32(0)
+    pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
+    ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
+    fsum = g[0].sum(0).abs().max().item()
+    out = {
+        "workload": "large16k: 1 structure, N=16000 H/C/N/O/S (0.45/0.3/0.1/0.1/0.05), "
+                    "density 0.01/Bohr^3, neutral, seed 2, cutoffs disp2=50 disp3=25",
+        "method": "precision form, energy + forces",
+        "ms_per_structure": float(np.median(ms)), "structures_per_s": 1e3 / float(np.median(ms)),
+        "atom_pairs_per_s": n * (n - 1) / 2 / (float(np.median(ms)) * 1e-3),
+        "stage_ms": {lib.d4_stage_name(i).decode(): ms_stage[i] / max(1, ncalls.value)
+                     for i in range(nstage)},
+        "energy_eh": float(e.sum()),
+        "max_abs_sum_of_forces_eh_bohr": fsum,
+        "peak_device_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
+        "fp64_check": "no FP64 result at this size (the CPU oracle and the plain FP64 "
+                      "kernels are dense O(N^3)); the same kernels are checked against the "
+                      "plain FP64 path on 1100-atom structures in the GPU tests",
+    }
+    del runner, e, g
+    torch.cuda.empty_cache()
+    return out
+
+
+def run_serving(pkg, param, nreq: int, plain_nreq: int):
+    """The serving form: a Poisson stream of ``nreq`` single-structure
+    energy + force requests at 2000 req/s, log-normal sizes (median 60 atoms,
+    sigma 1.0) clipped to [5, 4000], 12 elements, charges in {-1, 0, 1},
+    through the continuous-batching server (CUDA graphs per size bucket,
+    40 GB HBM budget).  Every request of a given size uses the one seeded
+    structure generated for that size.  Reported: the real-time stream
+    (structures/s, p50 / p99 latency) and the saturated throughput of the
+    precision form and of the plain FP64 kernels on the same requests."""
+    import torch
+
+    sv = importlib.import_module("tad-dftd4_gb300.serving")
+    wl = pkg.workloads
+    sizes, arrivals = wl.stream_sizes(4, nreq)
+    rng = np.random.default_rng(5)
+    charges = rng.integers(-1, 2, size=nreq).astype(np.float64)
+    pool = {int(n): wl.structure(40000 + int(n), int(n)) for n in np.unique(sizes)}
+    reqs = [sv.Request(k, pool[int(n)][0], pool[int(n)][1], float(charges[k]), float(t))
+            for k, (n, t) in enumerate(zip(sizes, arrivals))]
+    out = {"workload": f"stream: {nreq} requests, Poisson at 2000 req/s, log-normal sizes "
+                       "(median 60, sigma 1.0) in [5, 4000], 12 elements, seed 4",
+           "server": "continuous batching, CUDA graph per (bucket, batch size), "
+                     "max_wait 1 ms, HBM budget 40 GB"}
+    res = {}
+    for precision, count, realtime in (("mixed", nreq, True), ("mixed", nreq, False),
+                                       ("fp64", plain_nreq, False)):
+        srv = sv.Server(param, precision=precision, max_wait=1e-3, hbm_budget=40e9)
+        srv.warmup()
+        torch.cuda.synchronize()
+        sub = reqs[:count]
+        if not realtime:
+            sub = [sv.Request(r.rid, r.numbers, r.positions, r.charge, 0.0) for r in sub]
+        results, stats = sv.serve_stream(srv, sub, realtime=realtime)
+        key = ("realtime_" if realtime else "saturated_") + precision
+        out[key] = {k: stats[k] for k in ("requests", "structures_per_s", "atoms_per_s",
+                                          "p50_ms", "p99_ms", "max_ms", "batches", "failed")}
+        res[key] = results
+        del srv
+        torch.cuda.empty_cache()
+    m, f = res["saturated_mixed"], res["saturated_fp64"]
+    out["precision_vs_plain_max_abs_dE_eh"] = max(abs(m[k].energy - f[k].energy)
+                                                  for k in range(plain_nreq))
+    out["precision_vs_plain_max_abs_dF_eh_bohr"] = max(
+        float(np.abs(m[k].gradient - f[k].gradient).max()) for k in range(plain_nreq))
+    out["speedup_saturated_precision_vs_plain"] = (out["saturated_mixed"]["structures_per_s"] /
+                                                   out["saturated_fp64"]["structures_per_s"])
+    return out
+
+
 def run_ours(args, world, rank, local):
     import torch
 
@@ -406,6 +526,14 @@ def run_ours(args, world, rank, local):
                "sample": f"{n} structures of the batch (mean N {np.mean(sizes):.0f}), "
                          f"energy + autograd forces, float64 torch CPU oracle, {dt:.1f} s"}
 
+    large = None
+    if rank == 0 and not args.no_large:
+        large = run_large(pkg, disp, lib, dev)
+    serve = None
+    if rank == 0 and args.serve_requests > 0:
+        serve = run_serving(pkg, param, args.serve_requests,
+                            min(args.serve_plain_requests, args.serve_requests))
+
     clk = clocks.summary()
     if rank == 0:
         line = {
@@ -452,9 +580,11 @@ def run_ours(args, world, rank, local):
                 "hbm_peak_gbs": peaks.get("hbm_gbs"),
             },
             "stage_ms": stages, "top_stage": top,
-            "gpu_launches": 11 * args.steps,
+            "gpu_launches": KERNELS_PER_CALL * args.steps,
             "clocks": {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
             "cpu_baseline": cpu,
+            "large16k": large,
+            "serving": serve,
         }
         print(json.dumps(line), flush=True)
 
