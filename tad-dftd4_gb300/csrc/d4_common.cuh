@@ -43,6 +43,8 @@ __host__ __device__ inline size_t eeq_small_bytes(int N) {
 // shared memory (N <= 290), else by the multi-CTA path.
 __host__ __device__ inline bool eeq_small_fits(int N) { return eeq_small_bytes(N) <= 220 * 1024; }
 constexpr int EEQ_BIG_REFINE = 4;  // refinement iterations of the multi-CTA path at most
+constexpr int EEQ_SB = 512;        // diagonal blocks inverted for the multi-CTA solves
+__host__ __device__ inline int eeq_nsb(int N) { return (N + EEQ_SB - 1) / EEQ_SB; }
 
 // ---------------------------------------------------------------- ATM sizes
 
@@ -56,6 +58,9 @@ __host__ __device__ inline size_t atm_smem_bytes(int N) {
 __host__ __device__ inline bool atm_smem_fits(int N) { return atm_smem_bytes(N) <= 220 * 1024; }
 // Largest neighbour count of a centre atom in the neighbour-triple ATM.
 constexpr int ATM_SPARSE_DMAX = 2048;
+// Structures up to this size get their ATM centres in spatial (Z-) order
+// (one shared-memory sort per structure); larger ones keep index order.
+constexpr int ATM_ORDER_MAX = 16384;
 
 
 struct Workspace {
@@ -133,9 +138,13 @@ struct Workspace {
   float2 *eeq_X;    // [B*2*N] double-float solution (multi-CTA)
   float2 *eeq_B;    // [B*2*N] double-float right-hand sides (multi-CTA)
   unsigned *eeq_res;  // [B*EEQ_BIG_REFINE] max |residual| per iteration (float bits)
+  float *eeq_Y;     // [B*2*N] FP32 intermediate of the triangular sweeps (multi-CTA)
+  float *eeq_Xd;    // [B*nsb*512*512] inverses of the 512-diagonal blocks of the factor
   int *nbr;         // [B*N*N] ATM neighbour lists: row j = atoms within disp3 of j, ascending
   int *nbr_deg;     // [B*N] neighbours per atom
   unsigned long long *atm_cnt;  // [B*2] (sum_j deg_j (deg_j - 1) / 2, max_j deg_j)
+  int *atm_order;   // [B*N] atoms in Z-order of their positions (centre order of the
+                    // neighbour-triple ATM)
   size_t bytes;
 };
 
@@ -232,11 +241,14 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
       w.eeq_X = (float2 *)take(8 * 2 * BN);
       w.eeq_B = (float2 *)take(8 * 2 * BN);
       w.eeq_res = (unsigned *)take(4 * (size_t)B * EEQ_BIG_REFINE);
+      w.eeq_Y = (float *)take(4 * 2 * BN);
+      w.eeq_Xd = (float *)take(4 * (size_t)B * eeq_nsb(N) * EEQ_SB * EEQ_SB);
     }
     if (!atm_smem_fits(N)) {
       w.nbr = (int *)take(sizeof(int) * BNN);
       w.nbr_deg = (int *)take(sizeof(int) * BN);
       w.atm_cnt = (unsigned long long *)take(8 * 2 * (size_t)B);
+      w.atm_order = (int *)take(sizeof(int) * BN);
     }
   }
   w.bytes = align_up(off, 256);

@@ -10,11 +10,15 @@
 //                          panel   L21 = A21 X^T, 64-row tiles
 //                          syrk    A22 -= L21 L21^T, 128 x 128 lower tiles,
 //                                  8 x 8 register tiles (an FP32 SGEMM)
-//   solve  (per iteration): forward and backward block sweeps (X products
-//                          on the diagonal blocks, GEMV updates off them),
-//                          then x += v and the double-float residual of
-//                          (hi + lo) x, whose max |r| per structure decides
-//                          (on the device) whether later iterations run.
+//   inverse (once):         the 512 x 512 diagonal blocks of the factor
+//                          are inverted (block forward substitution over
+//                          their panels, 128 x 128 products)
+//   solve  (per iteration): forward and backward sweeps in 512-row steps
+//                          (products with the block inverses, GEMV updates
+//                          off the diagonal), then x += v and the
+//                          double-float residual of (hi + lo) x, whose max
+//                          |r| per structure decides (on the device) whether
+//                          later iterations run.
 //
 // Rows and columns are in compact order (real atoms only, ``ridx``); the
 // structures of a batch are processed together (grid y), each up to its own
@@ -256,78 +260,239 @@ __global__ void eeq_big_rhs_kernel(Ctx c, int adjoint) {
   c.w.eeq_V[o] = v.hi;
 }
 
-// Diagonal block of a sweep: v_blk <- X v_blk (forward) or X^T v_blk
-// (backward), for nr right-hand sides.
-__global__ void __launch_bounds__(BNB) eeq_big_trsv_kernel(Ctx c, int k0, int it, int trans,
-                                                           int nr) {
-  __shared__ float s_v[2][BNB];
-  const int b = blockIdx.x;
+// ---------------------------------------------------------------- block inverses
+
+// Inverses of the 512 x 512 diagonal blocks of the factor (four panels
+// each), so that the triangular sweeps advance 512 rows per step with plain
+// matrix-vector products.  Xd[b][s] (row-major, lower) is built by block
+// forward substitution over the panels of block s:
+//   W_rr = X_rr (the panel inverses the factorisation left on F's diagonal),
+//   W_rc = -X_rr sum_{j=c}^{r-1} L_rj W_jc   (r = 1..3, c < r).
+// Rows and columns beyond the structure's size are zero.
+constexpr int SBP = EEQ_SB / BNB;  // panels per block
+
+__device__ __forceinline__ float *xd_block(const Ctx &c, int b, int sblk) {
+  return c.w.eeq_Xd + ((size_t)b * eeq_nsb(c.N) + sblk) * EEQ_SB * EEQ_SB;
+}
+
+__global__ void __launch_bounds__(256) eeq_blkinv_init_kernel(Ctx c) {
+  const int sblk = blockIdx.x, b = blockIdx.y;
   const int m = c.w.n_real[b];
-  if (k0 >= m || big_skip(c, b, it)) return;
-  const int kb = min(BNB, m - k0);
+  const int s0 = sblk * EEQ_SB;
+  if (s0 >= m) return;
   const int N = c.N;
   const float *F = c.w.eeq_F + (size_t)b * N * N;
-  float *V = c.w.eeq_V + (size_t)b * 2 * N;
-  const int i = threadIdx.x;
-  for (int r = 0; r < nr; ++r) s_v[r][i] = i < kb ? V[r * N + k0 + i] : 0.f;
-  __syncthreads();
-  if (i >= kb) return;
-  for (int r = 0; r < nr; ++r) {
-    float z = 0.f;
-    if (trans) {
-      for (int cc = i; cc < kb; ++cc) z = fmaf(F[(size_t)(k0 + cc) * N + k0 + i], s_v[r][cc], z);
-    } else {
-      const float *row = F + (size_t)(k0 + i) * N + k0;
-      for (int cc = 0; cc <= i; ++cc) z = fmaf(row[cc], s_v[r][cc], z);
-    }
-    V[r * N + k0 + i] = z;
+  float *X = xd_block(c, b, sblk);
+  for (int t = threadIdx.x; t < EEQ_SB * EEQ_SB; t += blockDim.x) {
+    const int i = t / EEQ_SB, j = t % EEQ_SB;
+    const int gi = s0 + i, gj = s0 + j;
+    const bool diag = (i / BNB) == (j / BNB) && j <= i && gi < m;
+    X[t] = diag ? F[(size_t)gi * N + gj] : 0.f;
   }
 }
 
-// Forward sweep update below the block: v_i -= F[i][blk] . v_blk, warp per row.
-__global__ void __launch_bounds__(256) eeq_big_below_kernel(Ctx c, int k0, int it, int nr) {
+// Sub-block row r of every block: one CTA per (block, column sub-block cc < r)
+// forms T = sum_j L_rj W_jc (K = 128 (r - cc)) and then W_rc = -X_rr T, both
+// as 128 x 128 products with 8 x 8 register tiles (256 threads).
+constexpr int IK = 16;
+__global__ void __launch_bounds__(256) eeq_blkinv_step_kernel(Ctx c, int r) {
+  extern __shared__ float4 s_dyn4[];
+  float *As = reinterpret_cast<float *>(s_dyn4);  // [IK][BNB + 4]: A^T chunk
+  float *Bs = As + IK * (BNB + 4);                 // [IK][BNB + 4]: B chunk
+  float *Ts = Bs + IK * (BNB + 4);                 // [BNB][BNB + 4]: T
+  constexpr int LD = BNB + 4;
+  const int b = blockIdx.y;
+  const int sblk = blockIdx.x / r, cc = blockIdx.x % r;
+  const int m = c.w.n_real[b];
+  const int s0 = sblk * EEQ_SB;
+  if (s0 + r * BNB >= m) return;  // sub-block row r does not exist
+  const int N = c.N;
+  const float *F = c.w.eeq_F + (size_t)b * N * N;
+  float *X = xd_block(c, b, sblk);
+  const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
+  const int lrow = tid >> 1, lcol = (tid & 1) * 8;
+  const int gr0 = s0 + r * BNB;  // first global row of sub-block row r
+  float acc[8][8];
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
+  // T = sum_j L[r][j] W[j][cc]: A = L rows gr0.., columns s0 + 128 j ..; B = W rows 128 j..
+  for (int j = cc; j < r; ++j) {
+    for (int k0 = 0; k0 < BNB; k0 += IK) {
+#pragma unroll
+      for (int q = 0; q < 8; ++q) {
+        const int kk = lcol + q;
+        const int gi = gr0 + lrow, gk = s0 + j * BNB + k0 + kk;
+        As[kk * LD + lrow] = (gi < m && gk < m) ? F[(size_t)gi * N + gk] : 0.f;
+        Bs[kk * LD + lrow] = X[(size_t)(j * BNB + k0 + kk) * EEQ_SB + cc * BNB + lrow];
+      }
+      __syncthreads();
+#pragma unroll 4
+      for (int kk = 0; kk < IK; ++kk) {
+        const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk * LD + 8 * ty]);
+        const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk * LD + 8 * ty + 4]);
+        const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk * LD + 8 * tx]);
+        const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk * LD + 8 * tx + 4]);
+        const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+        const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+        for (int q = 0; q < 8; ++q)
+#pragma unroll
+          for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], bv[u], acc[q][u]);
+      }
+      __syncthreads();
+    }
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q)
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      Ts[(8 * ty + q) * LD + 8 * tx + u] = acc[q][u];
+      acc[q][u] = 0.f;
+    }
+  __syncthreads();
+  // W[r][cc] = -X_rr T (X_rr: Xd's diagonal sub-block r)
+  for (int k0 = 0; k0 < BNB; k0 += IK) {
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      const int kk = lcol + q;
+      As[kk * LD + lrow] = X[(size_t)(r * BNB + lrow) * EEQ_SB + r * BNB + k0 + kk];
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int kk = 0; kk < IK; ++kk) {
+      const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk * LD + 8 * ty]);
+      const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk * LD + 8 * ty + 4]);
+      const float4 b0 = *reinterpret_cast<const float4 *>(&Ts[(k0 + kk) * LD + 8 * tx]);
+      const float4 b1 = *reinterpret_cast<const float4 *>(&Ts[(k0 + kk) * LD + 8 * tx + 4]);
+      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
+      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+#pragma unroll
+      for (int q = 0; q < 8; ++q)
+#pragma unroll
+        for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], bv[u], acc[q][u]);
+    }
+    __syncthreads();
+  }
+#pragma unroll
+  for (int q = 0; q < 8; ++q) {
+    const int i = r * BNB + 8 * ty + q;
+    const bool rok = s0 + i < m;
+#pragma unroll
+    for (int u = 0; u < 8; ++u) {
+      const int j = cc * BNB + 8 * tx + u;
+      X[(size_t)i * EEQ_SB + j] = (rok && s0 + j < m) ? -acc[q][u] : 0.f;
+    }
+  }
+}
+
+size_t eeq_blkinv_smem() { return 4 * ((size_t)2 * IK * (BNB + 4) + (size_t)BNB * (BNB + 4)); }
+
+// ---------------------------------------------------------------- sweeps
+
+// Diagonal block s of a sweep, nr right-hand sides: dst_blk = X_s src_blk
+// (forward: warp per row, coalesced) or X_s^T src_blk (backward: warp per
+// column, lanes over the rows below the diagonal).
+__global__ void __launch_bounds__(256) eeq_sweep_diag_kernel(Ctx c, int sblk, int it, int trans,
+                                                             int nr, int src_y) {
+  __shared__ float s_v[2][EEQ_SB];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
-  if (k0 >= m || big_skip(c, b, it)) return;
-  const int kb = min(BNB, m - k0);
-  const int i = k0 + kb + blockIdx.x * 8 + (threadIdx.x >> 5);
+  const int s0 = sblk * EEQ_SB;
+  if (s0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(EEQ_SB, m - s0);
+  const int N = c.N;
+  const float *src = (src_y ? c.w.eeq_Y : c.w.eeq_V) + (size_t)b * 2 * N;
+  float *dst = (src_y ? c.w.eeq_V : c.w.eeq_Y) + (size_t)b * 2 * N;
+  const float *X = xd_block(c, b, sblk);
+  for (int t = threadIdx.x; t < nr * EEQ_SB; t += blockDim.x) {
+    const int r = t / EEQ_SB, k = t % EEQ_SB;
+    s_v[r][k] = k < kb ? src[(size_t)r * N + s0 + k] : 0.f;
+  }
+  __syncthreads();
+  const int lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + (threadIdx.x >> 5);  // output index
+  if (i >= kb) return;
+  float a0 = 0.f, a1 = 0.f;
+  if (!trans) {
+    const float *row = X + (size_t)i * EEQ_SB;
+    for (int k = lane; k <= i; k += 32) {
+      const float x = row[k];
+      a0 = fmaf(x, s_v[0][k], a0);
+      if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
+    }
+  } else {
+    for (int k = i + lane; k < kb; k += 32) {
+      const float x = X[(size_t)k * EEQ_SB + i];
+      a0 = fmaf(x, s_v[0][k], a0);
+      if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
+    }
+  }
+  a0 = warp_sumf(a0);
+  if (nr == 2) a1 = warp_sumf(a1);
+  if (lane == 0) {
+    dst[s0 + i] = a0;
+    if (nr == 2) dst[N + s0 + i] = a1;
+  }
+}
+
+// Forward sweep update below block s: V_i -= F[i][blk] . Y_blk, warp per row.
+__global__ void __launch_bounds__(256) eeq_sweep_below_kernel(Ctx c, int sblk, int it, int nr) {
+  const int b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  const int s0 = sblk * EEQ_SB;
+  if (s0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(EEQ_SB, m - s0);
+  const int i = s0 + kb + blockIdx.x * 8 + (threadIdx.x >> 5);
   if (i >= m) return;
   const int lane = threadIdx.x & 31;
   const int N = c.N;
-  const float *row = c.w.eeq_F + (size_t)b * N * N + (size_t)i * N + k0;
+  const float *row = c.w.eeq_F + (size_t)b * N * N + (size_t)i * N + s0;
+  const float *Y = c.w.eeq_Y + (size_t)b * 2 * N + s0;
   float *V = c.w.eeq_V + (size_t)b * 2 * N;
-  for (int r = 0; r < nr; ++r) {
-    const float *z = V + r * N + k0;
-    float acc = 0.f;
-    for (int cc = lane; cc < kb; cc += 32) acc = fmaf(row[cc], z[cc], acc);
-    acc = warp_sumf(acc);
-    if (lane == 0) V[r * N + i] -= acc;
+  float a0 = 0.f, a1 = 0.f;
+  for (int k = lane; k < kb; k += 32) {
+    const float x = row[k];
+    a0 = fmaf(x, Y[k], a0);
+    if (nr == 2) a1 = fmaf(x, Y[N + k], a1);
+  }
+  a0 = warp_sumf(a0);
+  if (nr == 2) a1 = warp_sumf(a1);
+  if (lane == 0) {
+    V[i] -= a0;
+    if (nr == 2) V[N + i] -= a1;
   }
 }
 
-// Backward sweep update above the block: v_i -= F[blk][i] . v_blk, thread per
-// row (coalesced over i).
-__global__ void __launch_bounds__(256) eeq_big_above_kernel(Ctx c, int k0, int it, int nr) {
-  __shared__ float s_v[2][BNB];
+// Backward sweep update above block s: Y_i -= F[blk][i] . V_blk, thread per
+// row (coalesced over i), the block's V in shared memory.
+__global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
+  __shared__ float s_v[2][EEQ_SB];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
-  if (k0 >= m || big_skip(c, b, it)) return;
-  const int kb = min(BNB, m - k0);
+  const int s0 = sblk * EEQ_SB;
+  if (s0 >= m || big_skip(c, b, it)) return;
+  const int kb = min(EEQ_SB, m - s0);
   const int N = c.N;
-  float *V = c.w.eeq_V + (size_t)b * 2 * N;
-  for (int t = threadIdx.x; t < nr * BNB; t += blockDim.x) {
-    const int r = t / BNB, cc = t % BNB;
-    s_v[r][cc] = cc < kb ? V[r * N + k0 + cc] : 0.f;
+  const float *V = c.w.eeq_V + (size_t)b * 2 * N;
+  float *Y = c.w.eeq_Y + (size_t)b * 2 * N;
+  for (int t = threadIdx.x; t < nr * EEQ_SB; t += blockDim.x) {
+    const int r = t / EEQ_SB, k = t % EEQ_SB;
+    s_v[r][k] = k < kb ? V[(size_t)r * N + s0 + k] : 0.f;
   }
   __syncthreads();
   const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= k0) return;
-  const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)k0 * N + i;
-  for (int r = 0; r < nr; ++r) {
-    float acc = 0.f;
-    for (int cc = 0; cc < kb; ++cc) acc = fmaf(F[(size_t)cc * N], s_v[r][cc], acc);
-    V[r * N + i] -= acc;
+  if (i >= s0) return;
+  const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)s0 * N + i;
+  float a0 = 0.f, a1 = 0.f;
+  for (int k = 0; k < kb; ++k) {
+    const float x = F[(size_t)k * N];
+    a0 = fmaf(x, s_v[0][k], a0);
+    if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
   }
+  Y[i] -= a0;
+  if (nr == 2) Y[N + i] -= a1;
 }
 
 // x += v (double-float).
@@ -500,19 +665,29 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
       eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), 256, 0, st>>>(c, k0);
     }
   }
+  const int nsb = eeq_nsb(N);
+  if (!adjoint) {  // inverses of the 512-blocks, kept for the adjoint solve
+    eeq_blkinv_init_kernel<<<dim3(nsb, B), 256, 0, st>>>(c);
+    cudaFuncSetAttribute(eeq_blkinv_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)eeq_blkinv_smem());
+    for (int r = 1; r < SBP; ++r)
+      eeq_blkinv_step_kernel<<<dim3(nsb * r, B), 256, eeq_blkinv_smem(), st>>>(c, r);
+  }
   const int nr = adjoint ? 1 : 2;
   eeq_big_rhs_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, adjoint ? 1 : 0);
   for (int it = 0; it < EEQ_BIG_REFINE; ++it) {
-    for (int p = 0; p < npan; ++p) {
-      const int k0 = p * BNB;
-      eeq_big_trsv_kernel<<<B, BNB, 0, st>>>(c, k0, it, 0, nr);
-      const int rest = N - k0 - BNB;
-      if (rest > 0) eeq_big_below_kernel<<<dim3((rest + 7) / 8, B), 256, 0, st>>>(c, k0, it, nr);
+    // V = L^-T L^-1 V: forward sweep into Y, backward sweep into V
+    for (int sb = 0; sb < nsb; ++sb) {
+      eeq_sweep_diag_kernel<<<dim3(EEQ_SB / 8, B), 256, 0, st>>>(c, sb, it, 0, nr, 0);
+      const int rest = N - (sb + 1) * EEQ_SB;
+      if (rest > 0)
+        eeq_sweep_below_kernel<<<dim3((rest + 7) / 8, B), 256, 0, st>>>(c, sb, it, nr);
     }
-    for (int p = npan - 1; p >= 0; --p) {
-      const int k0 = p * BNB;
-      eeq_big_trsv_kernel<<<B, BNB, 0, st>>>(c, k0, it, 1, nr);
-      if (k0 > 0) eeq_big_above_kernel<<<dim3((k0 + 255) / 256, B), 256, 0, st>>>(c, k0, it, nr);
+    for (int sb = nsb - 1; sb >= 0; --sb) {
+      eeq_sweep_diag_kernel<<<dim3(EEQ_SB / 8, B), 256, 0, st>>>(c, sb, it, 1, nr, 1);
+      const int s0 = sb * EEQ_SB;
+      if (s0 > 0)
+        eeq_sweep_above_kernel<<<dim3((s0 + 255) / 256, B), 256, 0, st>>>(c, sb, it, nr);
     }
     eeq_big_update_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, it, nr);
     eeq_big_residual_kernel<<<dim3((N + 7) / 8, B), 256, 0, st>>>(c, it, nr);

@@ -866,6 +866,104 @@ __global__ void __launch_bounds__(256) atm_nbr_kernel(Ctx c) {
   }
 }
 
+// Centre order of the neighbour-triple ATM: the real atoms of a structure
+// sorted by the Z-order (Morton) code of their positions on a 1024^3 grid
+// over the structure's bounding box, so that CTAs running at the same time
+// work on nearby centres and share their neighbourhoods' pair records in L2.
+// One CTA per structure: bitonic sort of (code << 32 | atom) keys in shared
+// memory (padding last); n <= ATM_ORDER_MAX, else index order.
+__device__ __forceinline__ unsigned spread_bits10(unsigned v) {  // 10 bits -> every third bit
+  v &= 0x3FFu;
+  v = (v | (v << 16)) & 0x030000FFu;
+  v = (v | (v << 8)) & 0x0300F00Fu;
+  v = (v | (v << 4)) & 0x030C30C3u;
+  v = (v | (v << 2)) & 0x09249249u;
+  return v;
+}
+
+__global__ void __launch_bounds__(1024) atm_order_kernel(Ctx c) {
+  extern __shared__ unsigned long long s_key[];
+  __shared__ float s_lo[3][32], s_hi[3][32];
+  const int b = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  const size_t bN = (size_t)b * N;
+  const int tid = threadIdx.x, lane = tid & 31, warp = tid >> 5;
+  if (n > ATM_ORDER_MAX) {
+    for (int t = tid; t < n; t += blockDim.x) c.w.atm_order[bN + t] = t;
+    return;
+  }
+  int P = 1;
+  while (P < n) P <<= 1;
+  float lo[3] = {FLT_MAX, FLT_MAX, FLT_MAX}, hi[3] = {-FLT_MAX, -FLT_MAX, -FLT_MAX};
+  for (int t = tid; t < n; t += blockDim.x) {
+    if (c.w.z[bN + t] == 0) continue;
+    const float4 p = c.w.pos32[bN + t];
+    const float v[3] = {p.x, p.y, p.z};
+#pragma unroll
+    for (int d = 0; d < 3; ++d) {
+      lo[d] = fminf(lo[d], v[d]);
+      hi[d] = fmaxf(hi[d], v[d]);
+    }
+  }
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+#pragma unroll
+    for (int o = 16; o > 0; o >>= 1) {
+      lo[d] = fminf(lo[d], __shfl_xor_sync(0xffffffffu, lo[d], o));
+      hi[d] = fmaxf(hi[d], __shfl_xor_sync(0xffffffffu, hi[d], o));
+    }
+    if (lane == 0) {
+      s_lo[d][warp] = lo[d];
+      s_hi[d][warp] = hi[d];
+    }
+  }
+  __syncthreads();
+  const int nw = blockDim.x >> 5;
+#pragma unroll
+  for (int d = 0; d < 3; ++d) {
+    lo[d] = FLT_MAX;
+    hi[d] = -FLT_MAX;
+    for (int w = 0; w < nw; ++w) {
+      lo[d] = fminf(lo[d], s_lo[d][w]);
+      hi[d] = fmaxf(hi[d], s_hi[d][w]);
+    }
+  }
+  for (int t = tid; t < P; t += blockDim.x) {
+    unsigned code = 0xFFFFFFFFu;  // padding and beyond n: last
+    if (t < n && c.w.z[bN + t] != 0) {
+      const float4 p = c.w.pos32[bN + t];
+      const float v[3] = {p.x, p.y, p.z};
+      unsigned q[3];
+#pragma unroll
+      for (int d = 0; d < 3; ++d) {
+        const float ext = hi[d] - lo[d];
+        const float f = ext > 0.f ? (v[d] - lo[d]) / ext : 0.f;
+        q[d] = (unsigned)fminf(fmaxf(f * 1024.f, 0.f), 1023.f);
+      }
+      code = (spread_bits10(q[0]) << 2) | (spread_bits10(q[1]) << 1) | spread_bits10(q[2]);
+    }
+    s_key[t] = ((unsigned long long)code << 32) | (unsigned)t;
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = tid; t < P; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const unsigned long long a = s_key[t], bb = s_key[u];
+          if ((a > bb) == ((t & k) == 0)) {
+            s_key[t] = bb;
+            s_key[u] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = tid; t < n; t += blockDim.x) c.w.atm_order[bN + t] = (int)(s_key[t] & 0xFFFFFFFFu);
+}
+
 constexpr int ATM_SPARSE_THREADS = 512;
 
 // ATM energy and adjoint over the neighbour triples of one centre atom j
@@ -888,11 +986,12 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
   float *s_P = s_S + ATM_SPARSE_DMAX;
   float *s_E = s_P + ATM_SPARSE_DMAX;
   __shared__ float s_red[ATM_SPARSE_THREADS / 32];
-  const int b = blockIdx.y, j = blockIdx.x;
+  const int b = blockIdx.y;
   const int N = c.N;
   const int n = c.w.n_eff[b];
-  if (j >= n || n < 3 || !atm_sparse_mode(c, b, n)) return;
+  if ((int)blockIdx.x >= n || n < 3 || !atm_sparse_mode(c, b, n)) return;
   const size_t bN = (size_t)b * N;
+  const int j = c.w.atm_order[bN + blockIdx.x];  // centres in spatial order
   if (c.w.z[bN + j] == 0) return;
   const int d = c.w.nbr_deg[bN + j];  // <= ATM_SPARSE_DMAX in sparse mode
   if (d < 2) return;
@@ -1545,7 +1644,14 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
                          cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
   const int threads = PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS;
   const int K = SMEM ? ATM_KMAX : atm_ctas_big(c.N);
-  if (!SMEM) atm_nbr_kernel<<<dim3((c.N + 7) / 8, c.B), 256, 0, st>>>(c);
+  if (!SMEM) {
+    atm_nbr_kernel<<<dim3((c.N + 7) / 8, c.B), 256, 0, st>>>(c);
+    int P = 1;
+    while (P < c.N && P < ATM_ORDER_MAX) P <<= 1;
+    const int osm = 8 * P;
+    cudaFuncSetAttribute(atm_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, osm);
+    atm_order_kernel<<<c.B, 1024, osm, st>>>(c);
+  }
   atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(K, c.B), threads, smem, st>>>(c);
   if (!SMEM) {  // neighbour-triple variant; returns at once for dense structures
     const int sp = ATM_SPARSE_DMAX * (16 + 4 * 4);

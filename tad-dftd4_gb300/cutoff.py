@@ -25,7 +25,7 @@ D4_K6 = 2 * 11.28174**2
 class Cutoff:
     """Collection of real-space cutoffs (Bohr)."""
 
-    __slots__ = ("disp2", "disp3", "cn", "cn_eeq", "device", "dtype")
+    __slots__ = ("disp2", "disp3", "cn", "cn_eeq", "device", "dtype", "values")
 
     def __init__(self, disp2=D4_DISP2_CUTOFF, disp3=D4_DISP3_CUTOFF, cn=D4_CN_CUTOFF,
                  cn_eeq=D4_CN_EEQ_CUTOFF, device=None, dtype=None):
@@ -36,7 +36,20 @@ class Cutoff:
         self.disp3 = as_t(disp3)
         self.cn = as_t(cn)
         self.cn_eeq = as_t(cn_eeq)
+        # the same values as host floats: reading them back from a device
+        # tensor would synchronise the stream on every call
+        self.values = {k: float(v) for k, v in
+                       (("disp2", disp2), ("disp3", disp3), ("cn", cn), ("cn_eeq", cn_eeq))}
+
+    def host_values(self) -> dict:
+        """The cutoffs as Python floats (disp2, disp3, cn, cn_eeq)."""
+        return dict(self.values)
 
     def __repr__(self) -> str:
         return (f"Cutoff(disp2={float(self.disp2)}, disp3={float(self.disp3)}, "
                 f"cn={float(self.cn)}, cn_eeq={float(self.cn_eeq)})")
+
+
+# host values of the default cutoffs (``dftd4(cutoff=None)``)
+Cutoff.DEFAULTS = {"disp2": D4_DISP2_CUTOFF, "disp3": D4_DISP3_CUTOFF, "cn": D4_CN_CUTOFF,
+                   "cn_eeq": D4_CN_EEQ_CUTOFF}

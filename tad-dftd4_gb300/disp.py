@@ -157,11 +157,17 @@ class _D4Function(torch.autograd.Function):
     def backward(ctx, go):
         grad, pgrad = ctx.saved_tensors
         runner: Runner = ctx.runner
-        go = go.to(torch.float64)
-        real = runner.numbers != 0
-        first = torch.argmax(real.to(torch.int8), dim=-1, keepdim=True)
-        w0 = torch.gather(go, -1, first)  # (B, 1)
-        uniform = bool((((go - w0) * real).abs().amax() == 0).item())
+        if go.numel() > 0 and all(st == 0 for st in go.stride()):
+            # one value broadcast over all atoms (the gradient of energy.sum()):
+            # uniform, no need to look at it on the host
+            w0 = go.reshape(-1)[:1].to(torch.float64).reshape(1, 1)
+            uniform = True
+        else:
+            go = go.to(torch.float64)
+            real = runner.numbers != 0
+            first = torch.argmax(real.to(torch.int8), dim=-1, keepdim=True)
+            w0 = torch.gather(go, -1, first)  # (B, 1)
+            uniform = bool((((go - w0) * real).abs().amax() == 0).item())
         if not uniform:
             _, grad, pgrad, _, _ = runner.run(ctx.positions, gradient=True,
                                               param_grad=ctx.needs_input_grad[1],
@@ -176,6 +182,7 @@ class _D4Function(torch.autograd.Function):
 
 
 PRECISIONS = ("fp64", "mixed")
+_PVEC: dict = {}
 
 
 def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
@@ -188,8 +195,9 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
             f"Shape of positions ({positions.shape}) is not consistent with atomic "
             f"numbers ({numbers.shape})."
         )
-    if cutoff is None:
-        cutoff = Cutoff(device=device, dtype=dtype)
+    cut_host = (Cutoff.DEFAULTS if cutoff is None else
+                cutoff.host_values() if isinstance(cutoff, Cutoff) else
+                {k: float(getattr(cutoff, k)) for k in ("disp2", "disp3", "cn", "cn_eeq")})
     mdl = _resolve_model(model, numbers)
     if rcov is not None and numbers.shape != rcov.shape:
         raise ValueError(f"Shape of covalent radii ({rcov.shape}) is not consistent with "
@@ -236,8 +244,8 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
         present[:, 0] = 0
         n_slots = max(1, int(present.sum(1).max().item()))
     cut = {
-        "disp2": float(cutoff.disp2), "disp3": float(cutoff.disp3),
-        "cn": D4_CN_CUTOFF, "cn_eeq": float(cutoff.cn_eeq),
+        "disp2": cut_host["disp2"], "disp3": cut_host["disp3"],
+        "cn": D4_CN_CUTOFF, "cn_eeq": cut_host["cn_eeq"],
     }
     runner = Runner(
         numbers=nums, charge=chg, tables=tab, model=mdl, params=resolved, cut=cut,
@@ -245,14 +253,24 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
         r4r2=None if r4r2 is None else r4r2.reshape(-1, N).to(torch.float64).contiguous(),
         n_slots=n_slots, mixed=precision == "mixed",
     )
-    pvec = []
-    for key in PARAM_ORDER:
-        v = param.get(key)
-        if isinstance(v, torch.Tensor):
-            pvec.append(v.reshape(()).to(device=device, dtype=torch.float64))
-        else:
-            pvec.append(torch.tensor(resolved[key], dtype=torch.float64, device=device))
-    return runner, torch.stack(pvec), shape
+    if any(isinstance(param.get(k), torch.Tensor) for k in PARAM_ORDER):
+        pvec = []
+        for key in PARAM_ORDER:
+            v = param.get(key)
+            if isinstance(v, torch.Tensor):
+                pvec.append(v.reshape(()).to(device=device, dtype=torch.float64))
+            else:
+                pvec.append(torch.tensor(resolved[key], dtype=torch.float64, device=device))
+        pvec = torch.stack(pvec)
+    else:  # plain numbers: a cached constant vector (no copy per call)
+        key = (device, tuple(float(resolved[k]) for k in PARAM_ORDER))
+        pvec = _PVEC.get(key)
+        if pvec is None:
+            pvec = torch.tensor(key[1], dtype=torch.float64, device=device)
+            if len(_PVEC) > 64:
+                _PVEC.clear()
+            _PVEC[key] = pvec
+    return runner, pvec, shape
 
 
 def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, *,
