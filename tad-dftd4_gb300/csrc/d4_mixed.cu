@@ -538,7 +538,37 @@ struct AtmAcc {
     else
       atomicAdd(&gE[x], (double)e * escale);
   }
+  // what = 0: dE/d(r^2) of the pair (j, k), 1: its weighted energy, 2:
+  // energy of atom j
+  __device__ __forceinline__ void one(int j, int k, int what, float v) const {
+    if (SMEM) {
+      float *dst = what == 2 ? &sE[j] : (what == 1 ? sP : sS) + tri_u(j, k, n);
+      atomicAdd(dst, v);
+    } else if (what == 2) {
+      atomicAdd(&gE[j], (double)v * escale);
+    } else {
+      atomicAdd((what == 1 ? gP : gS) + (size_t)j * N + k, v);
+    }
+  }
 };
+
+// Warp sums of three values, scattered: lanes 0-7 receive the sum of a,
+// lanes 8-15 of b, lanes 16-23 of c (24-31: 0).  Two halving exchanges
+// (xor 16, xor 8) and three butterfly steps: 6 shuffles instead of 15.
+__device__ __forceinline__ float warp_sum3_scatter(float a, float b, float c) {
+  const int lane = threadIdx.x & 31;
+  const bool up16 = (lane & 16) != 0, up8 = (lane & 8) != 0;
+  float k0 = up16 ? c : a, k1 = up16 ? 0.f : b;
+  const float s0 = up16 ? a : c, s1 = up16 ? b : 0.f;
+  k0 += __shfl_xor_sync(0xffffffffu, s0, 16);
+  k1 += __shfl_xor_sync(0xffffffffu, s1, 16);
+  float k = up8 ? k1 : k0;
+  k += __shfl_xor_sync(0xffffffffu, up8 ? k0 : k1, 8);
+  k += __shfl_xor_sync(0xffffffffu, k, 4);
+  k += __shfl_xor_sync(0xffffffffu, k, 2);
+  k += __shfl_xor_sync(0xffffffffu, k, 1);
+  return k;
+}
 
 // Constant inputs of the ATM triple loop of one structure.
 struct AtmIn {
@@ -576,6 +606,8 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
   const float wj = W[j];
   const float wk = kok ? W[k] : 0.f;
   float Sjk = 0.f, Pjk = 0.f, Ej = 0.f, Ek = 0.f;
+  float kept = 0.f;  // pending (i, j) / E_i value of this lane
+  int kept_i = -1, nred = 0;
   const size_t step = (size_t)istep * N;
   const float4 *Tij = T + (size_t)i0 * N + j;
   const float4 *Tik = T + (size_t)i0 * N + (kok ? k : j);
@@ -647,17 +679,26 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
         }
       }
     }
-    // (i, j) and E_i: one value per warp
+    // (i, j) and E_i: the three warp sums in one reduce-scatter (lanes
+    // 0-7: dE/d(r_ij^2), 8-15: weighted energy of (i, j), 16-23: E_i); lane
+    // u % 8 of each group keeps the value of the u-th reduction, and the 24
+    // kept values are accumulated together every 8 reductions
     if (GRAD) {
-      sij = warp_sumf(sij);
-      pe = warp_sumf(pe);
-    }
-    ei = warp_sumf(ei);
-    if (lane == 0) {
-      if (ei != 0.f) acc.energy(i, ei);
-      if (GRAD && (sij != 0.f || pe != 0.f)) acc.pair(i, j, sij, pe);
+      const float v = warp_sum3_scatter(sij, pe, ei);
+      if ((lane & 7) == (nred & 7)) {
+        kept = v;
+        kept_i = i;
+      }
+      if ((++nred & 7) == 0) {
+        if (lane < 24 && kept_i >= 0 && kept != 0.f) acc.one(kept_i, j, lane >> 3, kept);
+        kept_i = -1;
+      }
+    } else {
+      ei = warp_sumf(ei);
+      if (lane == 0 && ei != 0.f) acc.energy(i, ei);
     }
   }
+  if (GRAD && lane < 24 && kept_i >= 0 && kept != 0.f) acc.one(kept_i, j, lane >> 3, kept);
   if (GRAD && kok && (Sjk != 0.f || Pjk != 0.f)) acc.pair(j, k, Sjk, Pjk);
   const float ej = warp_sumf(Ej);
   if (lane == 0 && ej != 0.f) acc.energy(j, ej);
