@@ -186,6 +186,27 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
                   uint32_t flags, int32_t n_slots, void *d_workspace,
                   size_t workspace_bytes, const d4_outputs_t *out, void *stream);
 
+/* Outputs of d4_properties (device pointers; any may be NULL). */
+typedef struct d4_properties {
+  double *d_cn;      /* [B][N] D4 coordination numbers */
+  double *d_charges; /* [B][N] EEQ charges */
+  double *d_c6;      /* [B][N][N] atom-resolved C6 at the charges, padding rows/columns 0 */
+  double *d_alpha;   /* [B][N] static polarisabilities */
+} d4_properties_t;
+
+/*
+ * Properties of the D4 model for a padded batch, plain FP64 method: the D4
+ * coordination numbers, the EEQ charges, the atom-resolved C6 coefficients
+ * at those charges and the static polarisabilities.  Replaces
+ * ``tad_dftd4.get_properties`` (disp.py:149-197: cn_d4, get_eeq_charges,
+ * D4Model.weight_references / get_atomic_c6 (model/d4.py:103-289) /
+ * get_polarizabilities (model/base.py:286-302)).  ``cfg->kind`` must be
+ * D4_MODEL_D4; the workspace is d4_workspace_size(B, N, 1, 0) bytes.
+ */
+int d4_properties(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                  const d4_batch_t *batch, const d4_params_t *params, void *d_workspace,
+                  size_t workspace_bytes, const d4_properties_t *out, void *stream);
+
 /*
  * Copy the device status word of a workspace to the host (synchronous on
  * ``stream``) and clear it.  Returns a d4_status.

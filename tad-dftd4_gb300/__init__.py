@@ -8,7 +8,11 @@ name carries a hyphen).  Public API, mirroring ``tad_dftd4``:
 * ``dftd4(numbers, positions, charge, param, *, model=..., cutoff=...)``
 * ``Cutoff``, ``D4Model``, ``D4SModel``, ``Param``, ``RationalDamping``,
   ``ZeroDamping``
+* ``get_properties(numbers, positions, charge=None, cutoff=None)`` -- CN,
+  EEQ charges, atom-resolved C6 and static polarisabilities
 * ``dispersion_energy_gradient`` -- energies and forces in one fused call
+* ``get_params(method=..., functional=..., variant=None)`` -- damping
+  parameters per density functional
 """
 
 from __future__ import annotations
@@ -16,8 +20,9 @@ from __future__ import annotations
 from . import _lib, tables, workloads  # noqa: F401
 from .cutoff import Cutoff
 from .damping import Damping, Param, RationalDamping, ZeroDamping
-from .disp import dftd4, dispersion_energy_gradient
+from .disp import dftd4, dispersion_energy_gradient, get_properties
 from .model import D4Model, D4SModel
+from .parameters import DispersionMethod, get_params
 
 __version__ = "0.1.0"
 
@@ -31,5 +36,8 @@ __all__ = [
     "ZeroDamping",
     "dftd4",
     "dispersion_energy_gradient",
+    "get_properties",
+    "get_params",
+    "DispersionMethod",
     "__version__",
 ]

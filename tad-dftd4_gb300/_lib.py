@@ -114,6 +114,15 @@ class Outputs(ctypes.Structure):
     ]
 
 
+class Properties(ctypes.Structure):
+    _fields_ = [
+        ("d_cn", c_void_p),
+        ("d_charges", c_void_p),
+        ("d_c6", c_void_p),
+        ("d_alpha", c_void_p),
+    ]
+
+
 # name -> (restype, argtypes) of every exported function
 SIGNATURES = {
     "d4_abi_version": (c_int, []),
@@ -139,6 +148,11 @@ SIGNATURES = {
     "d4_stage_name": (c_char_p, [c_int32]),
     "d4_probe_fma": (c_int, [c_int32, c_int32, c_int32, c_void_p,
                              ctypes.POINTER(ctypes.c_float), c_void_p]),
+    "d4_properties": (
+        c_int,
+        [ctypes.POINTER(Tables), ctypes.POINTER(ModelCfg), ctypes.POINTER(Batch),
+         ctypes.POINTER(Params), c_void_p, c_size_t, ctypes.POINTER(Properties), c_void_p],
+    ),
     "d4_dispersion_noalloc": (
         c_int,
         [ctypes.POINTER(Tables), ctypes.POINTER(ModelCfg), ctypes.POINTER(Batch),

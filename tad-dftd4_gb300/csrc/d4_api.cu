@@ -114,6 +114,42 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   return check_cuda(cudaGetLastError());
 }
 
+int d4_properties(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
+                  const d4_batch_t *batch, const d4_params_t *params, void *d_workspace,
+                  size_t workspace_bytes, const d4_properties_t *out, void *stream) {
+  if (!tables_ok(tables) || !cfg || !batch || !params || !out || !d_workspace)
+    return D4_ERR_ARGUMENT;
+  if (batch->n_struct <= 0 || batch->n_pad <= 0 || batch->n_struct > 65535) return D4_ERR_ARGUMENT;
+  if (!batch->d_numbers || !batch->d_positions || !batch->d_charge) return D4_ERR_ARGUMENT;
+  if (cfg->kind != D4_MODEL_D4) return D4_ERR_ARGUMENT;
+  d4::Workspace w = d4::carve_workspace(d_workspace, batch->n_struct, batch->n_pad, 1, 0);
+  if (workspace_bytes < w.bytes) return D4_ERR_WORKSPACE;
+  d4::Ctx c{};
+  c.tab = *tables;
+  c.cfg = *cfg;
+  c.par = *params;
+  c.numbers = batch->d_numbers;
+  c.positions = batch->d_positions;
+  c.charge = batch->d_charge;
+  c.r4r2_in = batch->d_r4r2_in;
+  c.B = batch->n_struct;
+  c.N = batch->n_pad;
+  c.S = 1;
+  c.flags = 0;
+  c.w = w;
+  c.out = d4_outputs_t{};
+  c.out.d_cn = out->d_cn;
+  const d4_params_t &pp = *params;
+  c.pf = {(float)pp.s6,        (float)pp.s8,         (float)pp.s10,    (float)pp.a1,
+          (float)pp.a2,        (float)pp.s9,         (float)(pp.alp / 3.0),
+          (float)pp.cut_disp2, (float)pp.cut_disp3,  (float)pp.cut_cn, (float)pp.cut_cn_eeq,
+          (float)pp.kcn,       (float)pp.k4,         (float)pp.k5,     (float)pp.k6,
+          (float)pp.cn_eeq_max, (float)cfg->wf,        (float)cfg->ga};
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  d4::launch_properties(c, out->d_c6, out->d_alpha, out->d_charges, st);
+  return check_cuda(cudaGetLastError());
+}
+
 int d4_read_status(void *d_workspace, void *stream) {
   if (!d_workspace) return D4_ERR_ARGUMENT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

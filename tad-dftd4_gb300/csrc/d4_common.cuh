@@ -356,6 +356,28 @@ __device__ __forceinline__ float warp_sumf(float v) {
   return v;
 }
 
+// Warp sums of up to 32 per-lane values, scattered: lane L receives the
+// sum over the warp of in[L] (0 for L >= NV).  Five halving exchanges
+// (16 + 8 + 4 + 2 + 1 shuffles) instead of NV full butterflies (5 NV).
+template <int NV>
+__device__ __forceinline__ float warp_reduce_scatter32(const float (&in)[NV]) {
+  const int lane = threadIdx.x & 31;
+  float v[32];
+#pragma unroll
+  for (int q = 0; q < 32; ++q) v[q] = q < NV ? in[q] : 0.f;
+#pragma unroll
+  for (int h = 16; h >= 1; h >>= 1) {
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int q = 0; q < h; ++q) {
+      const float keep = up ? v[q + h] : v[q];
+      const float send = up ? v[q] : v[q + h];
+      v[q] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+  return v[0];
+}
+
 // Compensated FP32 accumulator (Knuth two-sum): value = hi + lo.
 struct Acc32 {
   float hi = 0.0f, lo = 0.0f;

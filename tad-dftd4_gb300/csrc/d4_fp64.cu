@@ -1163,6 +1163,67 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   return 0;
 }
 
+// get_properties (disp.py:149-197) of the D4 model: the atom-resolved C6 at
+// the EEQ charges for every pair including i = j (model/d4.py:268-289; rows
+// and columns of padding atoms 0), the static polarisabilities
+// alpha_i = sum_r w_ir alpha_ir(0) (model/base.py:286-302), i.e. A_i at the
+// first frequency, and the charges.  Warp per row i, lanes over j; the C6
+// sums run in the order of pair_fwd_kernel.
+__global__ void __launch_bounds__(256) props_kernel(Ctx c, double *c6out, double *alpha_out,
+                                                    double *q_out) {
+  const int b = blockIdx.y;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int i = blockIdx.x * 8 + warp;
+  const int N = c.N;
+  __shared__ double s_wa[8][NFREQ];
+  if (i >= N) return;
+  const size_t ai = (size_t)b * N + i;
+  const int n = c.w.n_eff[b];
+  const bool ri = i < n && c.w.z[ai] != 0;
+  if (lane < NFREQ)
+    s_wa[warp][lane] = ri ? THOPI * c.tab.freq_weights[lane] * c.w.A[ai * NFREQ + lane] : 0.0;
+  __syncwarp();
+  if (c6out) {
+    double *row = c6out + ai * N;
+    for (int j = lane; j < N; j += 32) {
+      const size_t aj = (size_t)b * N + j;
+      double v = 0.0;
+      if (ri && j < n && c.w.z[aj] != 0) {
+        const double *Aj = c.w.A + aj * NFREQ;
+#pragma unroll
+        for (int w = 0; w < NFREQ; ++w) v += s_wa[warp][w] * Aj[w];
+      }
+      row[j] = v;
+    }
+  }
+  if (lane == 0) {
+    if (alpha_out) alpha_out[ai] = ri ? c.w.A[ai * NFREQ] : 0.0;
+    if (q_out) q_out[ai] = c.w.q[ai];
+  }
+}
+
+int launch_properties(const Ctx &c, double *c6out, double *alpha_out, double *q_out,
+                      cudaStream_t st) {
+  const int B = c.B, N = c.N;
+  const dim3 atoms((N + 7) / 8, B);
+  launch_prep(c, st);
+  cn_kernel<<<atoms, 256, 0, st>>>(c);
+  const size_t vec_bytes = (size_t)8 * ((N + 1) / 2 + 1 + 2 * N);
+  const size_t tri_bytes = (size_t)8 * ((size_t)N * (N + 1) / 2);
+  if (vec_bytes + tri_bytes <= 220 * 1024) {
+    cudaFuncSetAttribute(eeq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)(vec_bytes + tri_bytes));
+    eeq_kernel<true><<<B, 256, vec_bytes + tri_bytes, st>>>(c);
+  } else {
+    cudaFuncSetAttribute(eeq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)vec_bytes);
+    eeq_kernel<false><<<B, 256, vec_bytes, st>>>(c);
+  }
+  launch_weights(c, st);
+  props_kernel<<<atoms, 256, 0, st>>>(c, c6out, alpha_out, q_out);
+  return 0;
+}
+
 void launch_prep(const Ctx &c, cudaStream_t st) {
   cudaMemsetAsync(c.w.status, 0, sizeof(int), st);
   if (c.N > PREP_ZERO_MAX_N) {  // the pair accumulators of large structures: plain memsets

@@ -28,6 +28,8 @@ int launch_fp64(const Ctx &c, cudaStream_t st);
 int launch_mixed(const Ctx &c, cudaStream_t st);
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint);
 void launch_pair_fwd_tc(const Ctx &c, cudaStream_t st);  // D4, precision form (d4_c6tc.cu)
+int launch_properties(const Ctx &c, double *c6out, double *alpha_out, double *q_out,
+                      cudaStream_t st);
 
 // stages shared by the FP64 method and the precision form (d4_fp64.cu)
 void launch_prep(const Ctx &c, cudaStream_t st);

@@ -460,12 +460,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
       }
     }
     if (GRAD) {
-      float mine = 0.f;
-#pragma unroll
-      for (int w = 0; w < NFREQ; ++w) {
-        const float g = warp_sumf(gacc[w]);
-        if (lane == w) mine = g;
-      }
+      const float mine = warp_reduce_scatter32(gacc);  // lane w: sum of gacc[w]
       if (lane < NFREQ) c.w.G32[(ai * c.S + s) * NFREQ + lane] = mine;  // dE/dA'_i
     }
     __syncwarp();
@@ -1226,12 +1221,7 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
         for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[(size_t)w * N], gacc[w]);
       }
     }
-    float mine = 0.f;
-#pragma unroll
-    for (int w = 0; w < NFREQ; ++w) {
-      const float g = warp_sumf(gacc[w]);
-      if (lane == w) mine = g;
-    }
+    const float mine = warp_reduce_scatter32(gacc);  // lane w: sum of gacc[w]
     // chain rule to CN and q for this slot (lane = frequency)
     if (lane < NFREQ) {
       const size_t o = (ax * c.S + s) * NFREQ + lane;

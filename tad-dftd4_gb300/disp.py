@@ -25,7 +25,7 @@ from .cutoff import (D4_CN_CUTOFF, D4_CN_EEQ_MAX, D4_K4, D4_K5, D4_K6, D4_KCN, C
 from .damping import PARAM_ORDER, Damping, Param, RationalDamping, ZeroDamping, resolve
 from .model import BaseModel, D4Model, D4SModel
 
-__all__ = ["dftd4", "dispersion_energy_gradient", "Runner"]
+__all__ = ["dftd4", "dispersion_energy_gradient", "get_properties", "Runner"]
 
 _ALLOWED_MODELS = ("d3", "d4", "d4s", "d5")
 CHECK_STATUS = True
@@ -318,3 +318,66 @@ def dispersion_energy_gradient(numbers, positions, charge, param, **kw):
     energy, grad, _, _, _ = runner.run(pos, gradient=True)
     return (energy.reshape(shape).to(positions.dtype),
             grad.reshape(*shape, 3).to(positions.dtype))
+
+
+def get_properties(numbers: torch.Tensor, positions: torch.Tensor, charge=None,
+                   cutoff: Cutoff | None = None):
+    """
+    Properties of the D4 model, the drop-in for ``tad_dftd4.get_properties``
+    (``disp.py:149-197``): D4 coordination numbers (..., N), EEQ charges
+    (..., N), atom-resolved C6 coefficients at those charges (..., N, N) and
+    static polarisabilities (..., N), in the dtype of ``positions``.  Plain
+    FP64 kernels; padding atoms (atomic number 0) get zeros.
+    """
+    if numbers.shape != positions.shape[:-1]:
+        raise ValueError(
+            f"Shape of positions ({positions.shape}) is not consistent with atomic "
+            f"numbers ({numbers.shape})."
+        )
+    device, dtype = positions.device, positions.dtype
+    if device.type != "cuda":
+        raise RuntimeError("tad-dftd4_gb300 runs on CUDA devices; move the inputs to a GPU")
+    cut_host = (Cutoff.DEFAULTS if cutoff is None else
+                cutoff.host_values() if isinstance(cutoff, Cutoff) else
+                {k: float(getattr(cutoff, k)) for k in ("disp2", "disp3", "cn", "cn_eeq")})
+    shape = numbers.shape
+    N = shape[-1]
+    nums = numbers.reshape(-1, N).to(device=device, dtype=torch.int64).contiguous()
+    B = nums.shape[0]
+    pos = positions.reshape(-1, N, 3).detach().to(torch.float64).contiguous()
+    charge = 0.0 if charge is None else charge
+    chg = _as_tensor(charge, device, torch.float64)
+    chg = (chg.expand(B) if chg.dim() == 0 else chg.reshape(-1)).contiguous()
+    if chg.numel() != B:
+        raise ValueError(f"charge of shape {tuple(chg.shape)} for {B} structures")
+    mdl = D4Model(nums)
+    tab = _tables.device_tables(device, mdl.ref_charges, mdl.ga, mdl.gc)
+    lib = _lib.load()
+    cn = torch.empty((B, N), dtype=torch.float64, device=device)
+    q = torch.empty((B, N), dtype=torch.float64, device=device)
+    c6 = torch.empty((B, N, N), dtype=torch.float64, device=device)
+    alpha = torch.empty((B, N), dtype=torch.float64, device=device)
+    ws_bytes = lib.d4_workspace_size(B, N, 1, 0)
+    work = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+    params = _lib.Params(
+        s6=1.0, s8=1.0, s10=0.0, a1=0.4, a2=5.0, s9=1.0, alp=16.0, has_s8=1, has_s10=0,
+        cut_disp2=cut_host["disp2"], cut_disp3=cut_host["disp3"], cut_cn=D4_CN_CUTOFF,
+        cut_cn_eeq=cut_host["cn_eeq"], cn_eeq_max=D4_CN_EEQ_MAX, kcn=D4_KCN, k4=D4_K4, k5=D4_K5,
+        k6=D4_K6)
+    batch = _lib.Batch(n_struct=B, n_pad=N, d_numbers=nums.data_ptr(), d_positions=pos.data_ptr(),
+                       d_charge=chg.data_ptr())
+    props = _lib.Properties(d_cn=cn.data_ptr(), d_charges=q.data_ptr(), d_c6=c6.data_ptr(),
+                            d_alpha=alpha.data_ptr())
+    cfg = _lib.ModelCfg(kind=_lib.MODEL_D4, ga=mdl.ga, gc=mdl.gc, wf=mdl.wf)
+    stream = torch.cuda.current_stream(device).cuda_stream
+    with torch.cuda.device(device):
+        _lib.check(lib.d4_properties(tab.struct, cfg, batch, params, work.data_ptr(), ws_bytes,
+                                     props, stream), "d4_properties")
+        status = lib.d4_read_status(work.data_ptr(), stream)
+        if status == 4:
+            raise ValueError("atomic number outside the element tables")
+        if status == 6:
+            raise ValueError("non-finite positions or charges")
+        _lib.check(status, "d4_properties (device status)")
+    return (cn.reshape(shape).to(dtype), q.reshape(shape).to(dtype),
+            c6.reshape(*shape, N).to(dtype), alpha.reshape(shape).to(dtype))

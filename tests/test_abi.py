@@ -53,6 +53,8 @@ def test_argument_errors_without_gpu():
     lib = m.load()
     rc = lib.d4_dispersion(None, None, None, None, 0, 1, None, 0, None, None)
     assert rc == 1  # D4_ERR_ARGUMENT, no device touched
+    rc = lib.d4_properties(None, None, None, None, None, 0, None, None)
+    assert rc == 1
 
 
 STRUCTS = {
@@ -67,6 +69,7 @@ STRUCTS = {
                              "d_charges_in", "d_r4r2_in", "d_energy_weights"]),
     "d4_outputs_t": ("Outputs", ["d_energy", "d_gradient", "d_charges", "d_cn",
                                  "d_param_grad", "d_cn_eeq"]),
+    "d4_properties_t": ("Properties", ["d_cn", "d_charges", "d_c6", "d_alpha"]),
 }
 
 

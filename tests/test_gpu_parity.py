@@ -203,3 +203,26 @@ def test_nonfinite_positions_raise(d4):
     pt = torch.tensor([[0.0, 0, 0], [0, 0, float("nan")]], dtype=torch.float64, device=dev)
     with pytest.raises(ValueError):
         d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})
+
+
+@pytest.mark.parametrize("tag,arrays,meta",
+                         [c for c in CASES if c[2]["model"] == "d4"
+                          and c[2]["ref_charges"] == "eeq"],
+                         ids=[c[0] for c in CASES if c[2]["model"] == "d4"
+                              and c[2]["ref_charges"] == "eeq"])
+def test_get_properties_matches_reference(d4, tag, arrays, meta):
+    """get_properties (disp.py:149-197): CN, EEQ charges, C6 at the charges
+    and static polarisabilities sum_r w_r alpha_r(0), against the values the
+    reference's own model code produced (1e-12 relative)."""
+    dev = torch.device("cuda")
+    numbers = torch.from_numpy(arrays["numbers"]).to(dev)
+    positions = torch.from_numpy(arrays["positions"]).to(dev)
+    charge = torch.from_numpy(arrays["charge"]).to(dev)
+    cutoff = d4.Cutoff(**meta["cutoff"]) if meta["cutoff"] else None
+    cn, q, c6, alpha = d4.get_properties(numbers, positions, charge, cutoff=cutoff)
+    assert c6.shape == numbers.shape + numbers.shape[-1:]
+    assert_close(cn.cpu(), arrays["cn"], 1e-12, 1e-14, "cn")
+    assert_close(q.cpu(), arrays["q"], 1e-12, 1e-13, "q")
+    assert_close(c6.cpu(), arrays["c6"], 1e-12, 1e-12, "c6")
+    alpha_ref = np.einsum("...r,...r->...", arrays["gw"], arrays["alpha"][..., 0])
+    assert_close(alpha.cpu(), alpha_ref, 1e-12, 1e-13, "alpha")
