@@ -494,6 +494,15 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
 
 // ---------------------------------------------------------------- ATM
 
+// 2^x on the special-function unit (ex2.approx.ftz: relative error about
+// 2^-22, results below 2^-126 flushed to 0); the ATM damping
+// 1 / (1 + 6 * 2^x) needs no more.
+__device__ __forceinline__ float sfu_exp2(float x) {
+  float y;
+  asm("ex2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ int tri_u(int j, int k, int n) {  // j < k, upper triangle
   return j * n - j * (j + 1) / 2 + (k - j - 1);
 }
@@ -568,6 +577,7 @@ __device__ __forceinline__ float warp_sum3_scatter(float a, float b, float c) {
 // Constant inputs of the ATM triple loop of one structure.
 struct AtmIn {
   const int *Zb;
+  bool gaps;  // padding atoms below the last real one
   const float4 *T, *Tda;
   const float *W;
   float cut2, alp3, s9, s9m;
@@ -607,7 +617,7 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
   const float4 *Tij = T + (size_t)i0 * N + j;
   const float4 *Tik = T + (size_t)i0 * N + (kok ? k : j);
   for (int i = i0; i < j; i += istep, Tij += step, Tik += step) {
-    if (in.Zb[i] == 0) continue;
+    if (in.gaps && in.Zb[i] == 0) continue;
     const float4 pij = *Tij;
     float sij = 0.f, pe = 0.f, ei = 0.f;
     if (kok) {
@@ -622,7 +632,7 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
         const float A = u + z, Bv = v - z, Cv = z - u;
         const float sfac = A * Bv * Cv;
         const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-        const float ta = exp2f(pij.z + pik.z + Ljk);
+        const float ta = sfu_exp2(pij.z + pik.z + Ljk);
         const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
         const float c9 = pij.w * pik.w * cjk;
         const float eu = c9 * fd * ang;  // triple energy without s9
@@ -768,6 +778,7 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   }
   AtmIn in;
   in.Zb = c.w.z + (size_t)b * N;
+  in.gaps = c.w.n_real[b] != n;
   in.T = c.w.ptf + (size_t)b * N * N;
   in.Tda = PGRAD ? c.w.ptf_da + (size_t)b * N * N : nullptr;
   in.W = c.w.w32 + (size_t)b * N;
@@ -1076,7 +1087,7 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
       const float A = u + z, Bv = v - z, Cv = z - u;
       const float sfac = A * Bv * Cv;
       const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-      const float ta = exp2f(pij.z + pik.z + pjk.z);
+      const float ta = sfu_exp2(pij.z + pik.z + pjk.z);
       const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
       const float c9 = pij.w * pik.w * pjk.w;
       const float eu = c9 * fd * ang;  // triple energy without s9
