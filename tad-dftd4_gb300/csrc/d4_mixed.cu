@@ -790,12 +790,18 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
   in.N = N;
   AtmPg pg;
   if (SMEM) {
-    int task = 0;
-    for (int j = 1; j < n - 1; ++j) {
-      for (int kc = j + 1; kc < n; kc += 32, ++task) {
-        if (task % nwarps != warp || in.Zb[j] == 0) continue;
-        atm_task<SMEM, GRAD, PGRAD>(in, acc, n, j, kc, cta, K, pg);
+    // tasks (j, chunk of 32 k > j) in j-major order, dealt round-robin to
+    // the warps; a warp walks straight to its next task (no division)
+    int j = 1, jbase = 0, nch = (n - 2 + 31) >> 5;  // row j: tasks jbase .. jbase + nch
+    for (int t = warp;; t += nwarps) {
+      while (j < n - 1 && t >= jbase + nch) {
+        jbase += nch;
+        ++j;
+        nch = (n - 1 - j + 31) >> 5;
       }
+      if (j >= n - 1) break;
+      if (in.gaps && in.Zb[j] == 0) continue;
+      atm_task<SMEM, GRAD, PGRAD>(in, acc, n, j, j + 1 + 32 * (t - jbase), cta, K, pg);
     }
   } else {
     const int NC = (n + 31) / 32;  // chunk slots per row j
