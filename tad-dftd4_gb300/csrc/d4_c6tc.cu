@@ -504,3 +504,220 @@ void launch_pair_fwd_tc(const Ctx &c, cudaStream_t st) {
 }
 
 }  // namespace d4
+
+namespace d4 {
+
+// ---------------------------------------------------------------- ATM / C6(q=0) adjoint
+
+// ATM forces, the C6(q=0) adjoint and the chain rule to dE/dCN and dE/dq of
+// the D4 precision form (the work of pair_atm_bwd_mixed_kernel), with the
+// C6(q=0) adjoint on the tensor cores:
+//   G0_x(w) = sum_y D_xy A0'_y(w),  D_xy = P_xy / (2 C6(q=0)_xy),
+// P_xy = the weighted triple energies of the pair, C6(q=0)_xy = c_xy^2 from
+// the pair record.  A CTA takes 128 atoms x (thread x) and walks the
+// partners y in chunks of 32: the threads read S_xy, P_xy and c_xy (pair
+// arrays are symmetric, read as row y so that the reads are coalesced over
+// x), add 2 S_xy (r_x - r_y) to the force on x and write D_xy into the MMA's
+// A operand; one thread issues the M=128, N=32 (frequencies, 23 used), K=32
+// products into tensor memory.  Split products hi = tf32(v), lo = tf32(v -
+// hi), three MMAs (lo hi, hi lo, hi hi) per k-step: this adjoint only feeds
+// forces, whose bar (1e-6 Eh/Bohr) the few-1e-7 relative accuracy meets.
+constexpr int BW_THREADS = 128;
+constexpr int BW_K = 32;                      // partners per chunk (MMA K)
+constexpr int BW_SBO = (BW_K / 4) * 128;      // 1024 bytes between groups of 8 rows
+constexpr int BW_COLS = 32;                   // tensor memory: G0 (32 frequencies)
+
+__device__ __forceinline__ int kmaj32_off(int r, int k) {
+  return (r >> 3) * BW_SBO + (k >> 2) * TC_LBO + (r & 7) * 16 + (k & 3) * 4;
+}
+
+struct BwSmem {
+  float a[2][TC_M * BW_K];  // D hi / lo (rows x, K = partners)
+  float bm[2][32 * BW_K];   // A0' hi / lo (rows = frequencies, K = partners)
+  float4 py[BW_K], ly[BW_K];
+  int zy[BW_K];
+  unsigned long long mbar;
+  uint32_t tmem;
+};
+
+__device__ __forceinline__ void split_tf32(float *hi, float *lo, int off, float v) {
+  const float h = tc::to_tf32(v);
+  *reinterpret_cast<float *>(reinterpret_cast<char *>(hi) + off) = h;
+  *reinterpret_cast<float *>(reinterpret_cast<char *>(lo) + off) = tc::to_tf32(v - h);
+}
+
+__global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
+  extern __shared__ __align__(128) unsigned char s_raw[];
+  BwSmem &S = *reinterpret_cast<BwSmem *>(s_raw);
+  const int b = blockIdx.y;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  const int x0 = blockIdx.x * TC_M;
+  const int tid = threadIdx.x, warp = tid >> 5;
+  const int x = x0 + tid;
+  const size_t bN = (size_t)b * N;
+  const size_t ax = bN + x;
+  const bool real = x < n && c.w.z[ax] != 0;
+  if (x0 >= n) {  // a tile of padding only
+    if (x < N) {
+      c.w.dEdcn[ax] = 0.0;
+      c.w.dEdq[ax] = 0.0;
+      c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+    return;
+  }
+  const uint32_t mbar = tc::smem_u32(&S.mbar);
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(&S.tmem), BW_COLS);
+  if (tid == 0) tc::mbar_init(mbar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = S.tmem;
+  const float4 *P = c.w.pos32 + bN;
+  const float4 *PL = c.w.pos32lo + bN;
+  const float4 px = real ? P[x] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float4 lx = real ? PL[x] : make_float4(0.f, 0.f, 0.f, 0.f);
+  const float *Sxy = c.w.prS32 + bN * N;
+  const float *Pxy = c.w.prP32 + bN * N;
+  const float4 *T = c.w.ptf + bN * N;
+  const float *A032 = c.w.A032 + bN * NFREQ;  // [w][N] of structure b
+  constexpr uint32_t IDESC = tc::idesc_tf32(TC_M, 32);
+  const uint32_t a_base = tc::smem_u32(&S.a[0][0]);
+  const uint32_t b_base = tc::smem_u32(&S.bm[0][0]);
+  Acc32 gx, gy, gz;
+  uint32_t parity = 0;
+  bool timed_out = false, issued = false;
+  for (int y0 = 0; y0 < n; y0 += BW_K) {
+    if (tid < BW_K) {
+      const int y = y0 + tid;
+      const bool ok = y < n;
+      S.py[tid] = ok ? P[y] : make_float4(0.f, 0.f, 0.f, 0.f);
+      S.ly[tid] = ok ? PL[y] : make_float4(0.f, 0.f, 0.f, 0.f);
+      S.zy[tid] = ok ? c.w.z[bN + y] : 0;
+    }
+    for (int t = tid; t < 32 * BW_K; t += BW_THREADS) {  // B: A0'_y(w), rows w
+      const int w = t / BW_K, q = t % BW_K;
+      const int y = y0 + q;
+      const float v = (w < NFREQ && y < n && c.w.z[bN + y] != 0) ? A032[(size_t)w * N + y] : 0.f;
+      split_tf32(S.bm[0], S.bm[1], kmaj32_off(w, q), v);
+    }
+    __syncthreads();
+#pragma unroll 4
+    for (int q = 0; q < BW_K; ++q) {
+      const int y = y0 + q;
+      float D = 0.f;
+      if (real && y < n && y != x && S.zy[q] != 0) {
+        const size_t o = (size_t)y * N + x;  // the pair arrays are symmetric
+        const float Sv = Sxy[o], Pv = Pxy[o];
+        const float3 d = pos_diff(px, lx, S.py[q], S.ly[q]);
+        gx.add(2.0f * Sv * d.x);
+        gy.add(2.0f * Sv * d.y);
+        gz.add(2.0f * Sv * d.z);
+        if (Pv != 0.f) {
+          const float cc = T[o].w;
+          D = Pv / (2.0f * cc * cc);
+        }
+      }
+      split_tf32(S.a[0], S.a[1], kmaj32_off(tid, q), D);
+    }
+    tc::fence_async_smem();
+    __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+      constexpr int AP = TC_M * BW_K * 4, BP = 32 * BW_K * 4;
+#pragma unroll
+      for (int pr = 0; pr < 3; ++pr) {
+        const uint32_t ab = a_base + (pr == 0 ? AP : 0), bb = b_base + (pr == 1 ? BP : 0);
+#pragma unroll
+        for (int s = 0; s < BW_K / 8; ++s)
+          tc::mma_tf32(tmem, tc::desc_kmajor(ab + 2 * TC_LBO * s, TC_LBO, BW_SBO),
+                       tc::desc_kmajor(bb + 2 * TC_LBO * s, TC_LBO, BW_SBO), IDESC,
+                       (issued || pr > 0 || s > 0) ? 1u : 0u);
+      }
+      tc::commit(mbar);
+    }
+    issued = true;
+    const bool done = tc::mbar_wait(mbar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(!done)) {
+      timed_out = true;
+      break;
+    }
+  }
+  if (timed_out) {
+    if (tid == 0) set_status(c.w.status, D4_ERR_DEVICE_TIMEOUT);
+    tc::mbar_wait(mbar, parity ^ 1u);
+    tc::fence_before_sync();
+    __syncthreads();
+    if (warp == 0) {
+      tc::fence_after_sync();
+      tc::tmem_free(tmem, BW_COLS);
+    }
+    return;
+  }
+  tc::fence_after_sync();
+  uint32_t g0[32];
+  {
+    uint32_t (&lo16)[16] = *reinterpret_cast<uint32_t(*)[16]>(&g0[0]);
+    uint32_t (&hi16)[16] = *reinterpret_cast<uint32_t(*)[16]>(&g0[16]);
+    const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
+    tc::tmem_ld16(tmem + t_lane, lo16);
+    tc::tmem_ld16(tmem + t_lane + 16, hi16);
+    tc::tmem_ld_wait();
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_free(tmem, BW_COLS);
+  }
+  if (x >= N) return;
+  if (!real) {
+    c.w.dEdcn[ax] = 0.0;
+    c.w.dEdq[ax] = 0.0;
+    c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  if (!issued) {  // a structure with no partners: G0 = 0
+#pragma unroll
+    for (int w = 0; w < 32; ++w) g0[w] = 0u;
+  }
+  // chain rule to CN and q (one slot): dE/dCN = sum_w G dA/dCN + G0 dA0/dCN,
+  // dE/dq = sum_w G dA/dq
+  Acc32 dcn, dq;
+  const float *G = c.w.G32 + ax * NFREQ;
+  const float *dA = c.w.dA32 + ax * NFREQ * 3;
+#pragma unroll
+  for (int w = 0; w < NFREQ; ++w) {
+    const float gw = G[w];
+    dcn.add(gw * dA[3 * w]);
+    dcn.add(__uint_as_float(g0[w]) * dA[3 * w + 2]);
+    dq.add(gw * dA[3 * w + 1]);
+  }
+  c.w.dEdcn[ax] = dcn.value();
+  c.w.dEdq[ax] = dq.value();
+  c.w.adj32[ax] = make_float4(dcn.hi + dcn.lo, 0.f, (float)c.w.q[ax], 0.f);
+  c.out.d_gradient[3 * ax] += gx.value();
+  c.out.d_gradient[3 * ax + 1] += gy.value();
+  c.out.d_gradient[3 * ax + 2] += gz.value();
+  c.out.d_energy[ax] += c.w.e3[ax];
+}
+
+// Whether the tensor-core adjoint runs: D4 (one slot) and at least one
+// 128-atom tile per SM; larger single structures keep the warp-per-atom kernel.
+bool pair_atm_bwd_tc_ok(const Ctx &c) {
+  if (c.cfg.kind != D4_MODEL_D4 || c.S != 1) return false;
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (long long)((c.N + TC_M - 1) / TC_M) * c.B;
+  return tiles >= (nsm > 0 ? nsm : 1);
+}
+
+void launch_pair_atm_bwd_tc(const Ctx &c, cudaStream_t st) {
+  const int smem = (int)sizeof(BwSmem);
+  cudaFuncSetAttribute(pair_atm_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  pair_atm_bwd_tc_kernel<<<dim3((c.N + TC_M - 1) / TC_M, c.B), BW_THREADS, smem, st>>>(c);
+}
+
+}  // namespace d4

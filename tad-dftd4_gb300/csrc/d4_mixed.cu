@@ -1780,7 +1780,10 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   stage_end(ST_ATM, st);
   if (grad) {
     stage_begin(ST_PAIR_ATM_BWD, st);
-    pair_atm_bwd_mixed_kernel<<<atoms, 256, 0, st>>>(c);
+    if (pair_atm_bwd_tc_ok(c))  // C6(q=0) adjoint on the tensor cores
+      launch_pair_atm_bwd_tc(c, st);
+    else
+      pair_atm_bwd_mixed_kernel<<<atoms, 256, 0, st>>>(c);
     stage_end(ST_PAIR_ATM_BWD, st);
     if (eeq) {
       stage_begin(ST_EEQ_ADJ, st);
