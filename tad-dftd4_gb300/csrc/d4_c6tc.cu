@@ -522,7 +522,7 @@ namespace d4 {
 // products into tensor memory.  Split products hi = tf32(v), lo = tf32(v -
 // hi), three MMAs (lo hi, hi lo, hi hi) per k-step: this adjoint only feeds
 // forces, whose bar (1e-6 Eh/Bohr) the few-1e-7 relative accuracy meets.
-constexpr int BW_THREADS = 128;
+constexpr int BW_THREADS = 256;               // two threads per atom (halves of a chunk)
 constexpr int BW_K = 32;                      // partners per chunk (MMA K)
 constexpr int BW_SBO = (BW_K / 4) * 128;      // 1024 bytes between groups of 8 rows
 constexpr int BW_COLS = 32;                   // tensor memory: G0 (32 frequencies)
@@ -554,12 +554,13 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   const int n = c.w.n_eff[b];
   const int x0 = blockIdx.x * TC_M;
   const int tid = threadIdx.x, warp = tid >> 5;
-  const int x = x0 + tid;
+  const int row = tid & (TC_M - 1), half = tid >> 7;
+  const int x = x0 + row;
   const size_t bN = (size_t)b * N;
   const size_t ax = bN + x;
   const bool real = x < n && c.w.z[ax] != 0;
   if (x0 >= n) {  // a tile of padding only
-    if (x < N) {
+    if (half == 0 && x < N) {
       c.w.dEdcn[ax] = 0.0;
       c.w.dEdq[ax] = 0.0;
       c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -602,23 +603,31 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
       split_tf32(S.bm[0], S.bm[1], kmaj32_off(w, q), v);
     }
     __syncthreads();
-#pragma unroll 4
-    for (int q = 0; q < BW_K; ++q) {
-      const int y = y0 + q;
-      float D = 0.f;
-      if (real && y < n && y != x && S.zy[q] != 0) {
-        const size_t o = (size_t)y * N + x;  // the pair arrays are symmetric
-        const float Sv = Sxy[o], Pv = Pxy[o];
-        const float3 d = pos_diff(px, lx, S.py[q], S.ly[q]);
-        gx.add(2.0f * Sv * d.x);
-        gy.add(2.0f * Sv * d.y);
-        gz.add(2.0f * Sv * d.z);
-        if (Pv != 0.f) {
-          const float cc = T[o].w;
-          D = Pv / (2.0f * cc * cc);
-        }
+    {
+      constexpr int QH = BW_K / 2;
+      const int q0 = half * QH;
+      float sv[QH], pv[QH], cv[QH];
+#pragma unroll
+      for (int u = 0; u < QH; ++u) {  // all loads of the half chunk first
+        const int q = q0 + u, y = y0 + q;
+        const bool ok = real && y < n && y != x && S.zy[q] != 0;
+        const size_t o = (size_t)(ok ? y : 0) * N + x;  // the pair arrays are symmetric
+        sv[u] = ok ? Sxy[o] : 0.f;
+        pv[u] = ok ? Pxy[o] : 0.f;
+        cv[u] = ok ? T[o].w : 1.f;
       }
-      split_tf32(S.a[0], S.a[1], kmaj32_off(tid, q), D);
+#pragma unroll
+      for (int u = 0; u < QH; ++u) {
+        const int q = q0 + u;
+        if (sv[u] != 0.f) {
+          const float3 d = pos_diff(px, lx, S.py[q], S.ly[q]);
+          gx.add(2.0f * sv[u] * d.x);
+          gy.add(2.0f * sv[u] * d.y);
+          gz.add(2.0f * sv[u] * d.z);
+        }
+        const float D = pv[u] != 0.f ? pv[u] / (2.0f * cv[u] * cv[u]) : 0.f;
+        split_tf32(S.a[0], S.a[1], kmaj32_off(row, q), D);
+      }
     }
     tc::fence_async_smem();
     __syncthreads();
@@ -657,7 +666,7 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   }
   tc::fence_after_sync();
   uint32_t g0[32];
-  {
+  if (half == 0) {
     uint32_t (&lo16)[16] = *reinterpret_cast<uint32_t(*)[16]>(&g0[0]);
     uint32_t (&hi16)[16] = *reinterpret_cast<uint32_t(*)[16]>(&g0[16]);
     const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
@@ -665,12 +674,29 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
     tc::tmem_ld16(tmem + t_lane + 16, hi16);
     tc::tmem_ld_wait();
   }
+  // the second half's force partial sums, through the (now free) A operand
+  float *red = &S.a[0][0];
+  if (half == 1) {
+    red[0 * TC_M + row] = gx.hi;
+    red[1 * TC_M + row] = gx.lo;
+    red[2 * TC_M + row] = gy.hi;
+    red[3 * TC_M + row] = gy.lo;
+    red[4 * TC_M + row] = gz.hi;
+    red[5 * TC_M + row] = gz.lo;
+  }
   tc::fence_before_sync();
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_free(tmem, BW_COLS);
   }
+  if (half == 1) return;
+  gx.add(red[0 * TC_M + row]);
+  gx.lo += red[1 * TC_M + row];
+  gy.add(red[2 * TC_M + row]);
+  gy.lo += red[3 * TC_M + row];
+  gz.add(red[4 * TC_M + row]);
+  gz.lo += red[5 * TC_M + row];
   if (x >= N) return;
   if (!real) {
     c.w.dEdcn[ax] = 0.0;
