@@ -79,6 +79,14 @@ __device__ __forceinline__ void store_digits(float *p1, float *p2, float *p3, in
 
 size_t pair_fwd_tc_smem() { return sizeof(TcSmem); }
 
+// log2(x) on the special-function unit (lg2.approx.ftz: absolute error about
+// 2^-22 near 1, relative elsewhere).
+__device__ __forceinline__ float sfu_log2(float x) {
+  float y;
+  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 template <bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   extern __shared__ __align__(128) unsigned char s_raw[];
@@ -159,7 +167,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   const float wi = real ? c.w.w32[ai] : 0.f;
   float4 *Tt = c.w.ptf + bN * N;  // written transposed: T[j][i], coalesced over i
   float4 *Tdat = PGRAD ? c.w.ptf_da + bN * N : nullptr;
-  const float alp3_log2e = c.pf.alp3 * 1.4426950408889634f;
+  const float alp3 = c.pf.alp3;
   const bool tabled = c.r4r2_in == nullptr;
   const double sref = p.s6 != 0.0 ? p.s6 : 1.0;
   const dfl rho10 = df_from(p.has_s10 ? p.s10 / sref : 0.0);
@@ -244,7 +252,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
       break;
     }
     tc::fence_after_sync();
-#pragma unroll
+#pragma unroll 1
     for (int u = 0; u < 2; ++u) {
       const int c0 = 16 * half + 8 * u;
       float c6v[8], c60v[8];
@@ -300,38 +308,42 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
           R08d = df_from(R06 * R02);
         }
         const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
-        const float lnR0r = logf(R0 * ir) + R0d.lo / R0;
-        Tt[(size_t)j * N + i] = make_float4(r2, ir, alp3_log2e * lnR0r, sqrtf(fmaxf(c60, 0.f)));
-        if (PGRAD) Tdat[(size_t)j * N + i] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
+        const float iR0 = __frcp_rn(R0);
+        // log2(R0 / r) on the SFU (ATM damping exponent; absolute error ~1e-7)
+        const float l2R0r = sfu_log2(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
+        Tt[(size_t)j * N + i] = make_float4(r2, ir, alp3 * l2R0r, sqrtf(fmaxf(c60, 0.f)));
+        if (PGRAD)
+          Tdat[(size_t)j * N + i] =
+              make_float4(sqq * iR0, iR0, l2R0r * 0.6931471805599453f, 0.f);
         if (rr <= cut2) {
           const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R06d.hi;
-          const float t6 = 1.0f / ((r6 + R06) + R06d.lo);
+          const float t6 = __frcp_rn((r6 + R06) + R06d.lo);
           float eterm = rho6 * c6 * t6;
           float dEdr = 6.0f * s6 * c6 * (r6 * ir) * t6 * t6;
           float K = -s6 * t6;
-          float dE_dR0 = 6.0f * s6 * c6 * (R06 / R0) * t6 * t6;
+          float dE_dR0 = 6.0f * s6 * c6 * (R06 * iR0) * t6 * t6;
           pg[0] -= wi * c6 * t6;
           if (p.has_s8) {
             const float r8 = r6 * r2, R08 = R08d.hi, qq = qqd.hi;
-            const float t8 = 1.0f / ((r8 + R08) + R08d.lo);
+            const float t8 = __frcp_rn((r8 + R08) + R08d.lo);
             const float c8 = fmaf(c6, qqd.hi, c6 * qqd.lo);
             e8_acc.add(c8 * t8);
             dEdr += 8.0f * s8 * c8 * (r8 * ir) * t8 * t8;
             K -= s8 * qq * t8;
-            dE_dR0 += 8.0f * s8 * c8 * (R08 / R0) * t8 * t8;
+            dE_dR0 += 8.0f * s8 * c8 * (R08 * iR0) * t8 * t8;
             pg[1] -= wi * c8 * t8;
           }
           if (p.has_s10) {
             const float qq = sqq * sqq;
             const float r10 = r6 * r2 * r2, R010 = R06 * R02 * R02;
-            const float t10 = 1.0f / (r10 + R010);
+            const float t10 = __frcp_rn(r10 + R010);
             const float q2 = qq * qq * (49.0f / 40.0f);
             const float c10 = c6 * q2;
             const float e10 = c10 * t10;
             eterm = fmaf(rho10.hi, e10, fmaf(rho10.lo, e10, eterm));
             dEdr += 10.0f * s10 * c10 * (r10 * ir) * t10 * t10;
             K -= s10 * q2 * t10;
-            dE_dR0 += 10.0f * s10 * c10 * (R010 / R0) * t10 * t10;
+            dE_dR0 += 10.0f * s10 * c10 * (R010 * iR0) * t10 * t10;
             pg[2] -= wi * c10 * t10;
           }
           e_acc.add(eterm);
