@@ -307,10 +307,10 @@ def probe_peak(lib, pkg, dev, fp64: bool) -> float:
 
 # Kernels of one precision-form energy + gradient call of the D4 model with
 # EEQ charges on structures that fit the one-CTA EEQ / shared-memory ATM
-# (N <= 234): prep, element tables, CN, EEQ matrix, EEQ solve, weights,
-# pair (tensor-core C6), ATM, ATM / C6 adjoint, EEQ adjoint, CN adjoint,
-# finish.
-KERNELS_PER_CALL = 12
+# (N <= 234): prep, element tables, size order, CN, EEQ matrix, EEQ solve,
+# weights, pair (tensor-core C6), ATM, ATM / C6 adjoint (tensor cores), EEQ
+# adjoint, CN adjoint, finish.
+KERNELS_PER_CALL = 13
 
 
 def run_large(pkg, disp, lib, dev, steps: int = 3):

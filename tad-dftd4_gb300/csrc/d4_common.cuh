@@ -56,6 +56,9 @@ __host__ __device__ inline size_t atm_smem_bytes(int N) {
   return (size_t)4 * ((size_t)N * (N - 1) + N);
 }
 __host__ __device__ inline bool atm_smem_fits(int N) { return atm_smem_bytes(N) <= 220 * 1024; }
+// Batches up to this many structures get a size-ordered launch order.
+constexpr int SORDER_MAX = 16384;
+
 // Largest neighbour count of a centre atom in the neighbour-triple ATM.
 constexpr int ATM_SPARSE_DMAX = 2048;
 // Structures up to this size get their ATM centres in spatial (Z-) order
@@ -145,6 +148,8 @@ struct Workspace {
   unsigned long long *atm_cnt;  // [B*2] (sum_j deg_j (deg_j - 1) / 2, max_j deg_j)
   int *atm_order;   // [B*N] atoms in Z-order of their positions (centre order of the
                     // neighbour-triple ATM)
+  int *sorder;      // [B] structures by decreasing n_eff (launch order of the
+                    // per-structure kernels of the precision form)
   size_t bytes;
 };
 
@@ -208,6 +213,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.fw32 = (float *)take(sizeof(float) * 32);
   if (mixed) {
     w.adj32 = (float4 *)take(16 * BN);
+    w.sorder = (int *)take(sizeof(int) * (size_t)B);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.prP32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.eeq_hi = (float *)take(4 * BNN);

@@ -492,6 +492,47 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
     c.out.d_energy[ai] = -0.5 * (sref * ea.value() + (p.has_s8 ? p.s8 * ea8.value() : 0.0));
 }
 
+// ---------------------------------------------------------------- launch order
+
+// Structures by decreasing size (n_eff), ties by index: the per-structure
+// kernels (EEQ solves, shared-memory ATM) take structure sorder[blockIdx],
+// so that the largest structures start first and the small ones fill the
+// last wave (longest-processing-time-first).  One CTA, bitonic sort of
+// (size, index) keys in shared memory; batches above SORDER_MAX keep index
+// order.
+__global__ void __launch_bounds__(1024) size_order_kernel(Ctx c) {
+  extern __shared__ unsigned long long s_ord[];
+  const int B = c.B;
+  const int tid = threadIdx.x;
+  if (B > SORDER_MAX) {
+    for (int t = tid; t < B; t += blockDim.x) c.w.sorder[t] = t;
+    return;
+  }
+  int P = 1;
+  while (P < B) P <<= 1;
+  for (int t = tid; t < P; t += blockDim.x) {
+    const unsigned key = t < B ? 0x7FFFFFFFu - (unsigned)c.w.n_eff[t] : 0xFFFFFFFFu;
+    s_ord[t] = ((unsigned long long)key << 32) | (unsigned)t;
+  }
+  __syncthreads();
+  for (int k = 2; k <= P; k <<= 1) {
+    for (int j = k >> 1; j > 0; j >>= 1) {
+      for (int t = tid; t < P; t += blockDim.x) {
+        const int u = t ^ j;
+        if (u > t) {
+          const unsigned long long a = s_ord[t], bb = s_ord[u];
+          if ((a > bb) == ((t & k) == 0)) {
+            s_ord[t] = bb;
+            s_ord[u] = a;
+          }
+        }
+      }
+      __syncthreads();
+    }
+  }
+  for (int t = tid; t < B; t += blockDim.x) c.w.sorder[t] = (int)(s_ord[t] & 0xFFFFFFFFu);
+}
+
 // ---------------------------------------------------------------- ATM
 
 // 2^x on the special-function unit (ex2.approx.ftz: relative error about
@@ -751,7 +792,7 @@ template <bool SMEM, bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     atm_mixed_kernel(Ctx c) {
   extern __shared__ float s_acc[];
-  const int b = blockIdx.y;
+  const int b = SMEM ? c.w.sorder[blockIdx.y] : (int)blockIdx.y;
   const int cta = blockIdx.x;
   const int N = c.N;
   const int n = c.w.n_eff[b];
@@ -1527,7 +1568,7 @@ template <bool SMEM>
 __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_mixed_kernel(Ctx c) {
   extern __shared__ float4 s_dyn4[];
   float *s_f = reinterpret_cast<float *>(s_dyn4);
-  const int b = blockIdx.x;
+  const int b = c.w.sorder[blockIdx.x];  // largest structures first
   const int N = c.N;
   const int n = c.w.n_eff[b];
   __shared__ int s_m;
@@ -1610,7 +1651,7 @@ template <bool SMEM>
 __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_adjoint_mixed_kernel(Ctx c) {
   extern __shared__ float4 s_dyn4[];
   float *s_f = reinterpret_cast<float *>(s_dyn4);
-  const int b = blockIdx.x;
+  const int b = c.w.sorder[blockIdx.x];  // largest structures first
   const int N = c.N;
   const int n = c.w.n_eff[b];
   __shared__ int s_m;
@@ -1723,6 +1764,14 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   stage_begin(ST_PREP, st);
   launch_prep(c, st);
   tables32_kernel<<<TABLES32_THREADS / 256, 256, 0, st>>>(c);
+  {
+    int P = 1;
+    while (P < B && P < SORDER_MAX) P <<= 1;
+    const int osm = 8 * P;
+    if (osm > 48 * 1024)
+      cudaFuncSetAttribute(size_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, osm);
+    size_order_kernel<<<1, 1024, osm, st>>>(c);
+  }
   stage_end(ST_PREP, st);
   stage_begin(ST_CN, st);
   cn_mixed_kernel<<<atoms, 256, 0, st>>>(c);
