@@ -79,14 +79,6 @@ __device__ __forceinline__ void store_digits(float *p1, float *p2, float *p3, in
 
 size_t pair_fwd_tc_smem() { return sizeof(TcSmem); }
 
-// log2(x) on the special-function unit (lg2.approx.ftz: absolute error about
-// 2^-22 near 1, relative elsewhere).
-__device__ __forceinline__ float sfu_log2(float x) {
-  float y;
-  asm("lg2.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 template <bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   extern __shared__ __align__(128) unsigned char s_raw[];
@@ -309,8 +301,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         }
         const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
         const float iR0 = __frcp_rn(R0);
-        // log2(R0 / r) on the SFU (ATM damping exponent; absolute error ~1e-7)
-        const float l2R0r = sfu_log2(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
+        // log2(R0 / r), the ATM damping exponent (to ~1 ulp: an SFU estimate
+        // biases the three-body energy by ~1e-6 relative)
+        const float l2R0r = log2f(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
         Tt[(size_t)j * N + i] = make_float4(r2, ir, alp3 * l2R0r, sqrtf(fmaxf(c60, 0.f)));
         if (PGRAD)
           Tdat[(size_t)j * N + i] =
@@ -571,6 +564,14 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   const size_t bN = (size_t)b * N;
   const size_t ax = bN + x;
   const bool real = x < n && c.w.z[ax] != 0;
+  // partners of this CTA: chunks [ch0, ch1); with several CTAs per tile
+  // (gridDim.z > 1) they add G0 and the forces atomically and
+  // pair_atm_bwd_finish_kernel applies the chain rule
+  const int nsplit = gridDim.z;
+  const int nch = (n + BW_K - 1) / BW_K;
+  const int ch0 = (int)((long long)blockIdx.z * nch / nsplit);
+  const int ch1 = (int)((long long)(blockIdx.z + 1) * nch / nsplit);
+  if (nsplit > 1 && (x0 >= n || ch0 >= ch1)) return;
   if (x0 >= n) {  // a tile of padding only
     if (half == 0 && x < N) {
       c.w.dEdcn[ax] = 0.0;
@@ -600,7 +601,7 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   Acc32 gx, gy, gz;
   uint32_t parity = 0;
   bool timed_out = false, issued = false;
-  for (int y0 = 0; y0 < n; y0 += BW_K) {
+  for (int y0 = ch0 * BW_K; y0 < ch1 * BW_K; y0 += BW_K) {
     if (tid < BW_K) {
       const int y = y0 + tid;
       const bool ok = y < n;
@@ -710,6 +711,15 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   gz.add(red[4 * TC_M + row]);
   gz.lo += red[5 * TC_M + row];
   if (x >= N) return;
+  if (nsplit > 1) {  // partial sums of this CTA's partners
+    if (!real) return;
+#pragma unroll
+    for (int w = 0; w < NFREQ; ++w) atomicAdd(&c.w.G032[ax * NFREQ + w], __uint_as_float(g0[w]));
+    atomicAdd(&c.out.d_gradient[3 * ax], gx.value());
+    atomicAdd(&c.out.d_gradient[3 * ax + 1], gy.value());
+    atomicAdd(&c.out.d_gradient[3 * ax + 2], gz.value());
+    return;
+  }
   if (!real) {
     c.w.dEdcn[ax] = 0.0;
     c.w.dEdq[ax] = 0.0;
@@ -741,21 +751,64 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
   c.out.d_energy[ax] += c.w.e3[ax];
 }
 
-// Whether the tensor-core adjoint runs: D4 (one slot) and at least one
-// 128-atom tile per SM; larger single structures keep the warp-per-atom kernel.
-bool pair_atm_bwd_tc_ok(const Ctx &c) {
-  if (c.cfg.kind != D4_MODEL_D4 || c.S != 1) return false;
-  int dev = 0, nsm = 0;
-  cudaGetDevice(&dev);
-  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
-  const long long tiles = (long long)((c.N + TC_M - 1) / TC_M) * c.B;
-  return tiles >= (nsm > 0 ? nsm : 1);
+// Chain rule of the split tensor-core adjoint (thread per atom): dE/dCN and
+// dE/dq from G (pair kernel) and the accumulated G0, and E2 + E3.
+__global__ void __launch_bounds__(256) pair_atm_bwd_finish_kernel(Ctx c) {
+  const int b = blockIdx.y;
+  const int N = c.N;
+  const int x = blockIdx.x * blockDim.x + threadIdx.x;
+  if (x >= N) return;
+  const size_t ax = (size_t)b * N + x;
+  const int n = c.w.n_eff[b];
+  if (x >= n || c.w.z[ax] == 0) {
+    c.w.dEdcn[ax] = 0.0;
+    c.w.dEdq[ax] = 0.0;
+    c.w.adj32[ax] = make_float4(0.f, 0.f, 0.f, 0.f);
+    return;
+  }
+  Acc32 dcn, dq;
+  const float *G = c.w.G32 + ax * NFREQ;
+  const float *G0 = c.w.G032 + ax * NFREQ;
+  const float *dA = c.w.dA32 + ax * NFREQ * 3;
+#pragma unroll
+  for (int w = 0; w < NFREQ; ++w) {
+    const float gw = G[w];
+    dcn.add(gw * dA[3 * w]);
+    dcn.add(G0[w] * dA[3 * w + 2]);
+    dq.add(gw * dA[3 * w + 1]);
+  }
+  c.w.dEdcn[ax] = dcn.value();
+  c.w.dEdq[ax] = dq.value();
+  c.w.adj32[ax] = make_float4(dcn.hi + dcn.lo, 0.f, (float)c.w.q[ax], 0.f);
+  c.out.d_energy[ax] += c.w.e3[ax];
 }
+
+// Whether the tensor-core adjoint runs: the D4 model (one slot).
+bool pair_atm_bwd_tc_ok(const Ctx &c) { return c.cfg.kind == D4_MODEL_D4 && c.S == 1; }
 
 void launch_pair_atm_bwd_tc(const Ctx &c, cudaStream_t st) {
   const int smem = (int)sizeof(BwSmem);
   cudaFuncSetAttribute(pair_atm_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
-  pair_atm_bwd_tc_kernel<<<dim3((c.N + TC_M - 1) / TC_M, c.B), BW_THREADS, smem, st>>>(c);
+  // few tiles (large structures): a tile's partners are split over several
+  // CTAs so that every SM gets about four
+  int dev = 0, nsm = 0;
+  cudaGetDevice(&dev);
+  cudaDeviceGetAttribute(&nsm, cudaDevAttrMultiProcessorCount, dev);
+  const long long tiles = (long long)((c.N + TC_M - 1) / TC_M) * c.B;
+  const long long want = 4LL * (nsm > 0 ? nsm : 1);
+  const long long chunks = (c.N + BW_K - 1) / BW_K;
+  int nsplit = 1;
+  if (tiles < want) {
+    const long long sp = (want + tiles - 1) / tiles;
+    nsplit = (int)(sp < chunks ? sp : chunks);
+  }
+  if (nsplit > 1) {
+    cudaMemsetAsync(c.w.G032, 0, (size_t)4 * NFREQ * c.B * c.N, st);
+    pair_atm_bwd_tc_kernel<<<dim3((c.N + TC_M - 1) / TC_M, c.B, nsplit), BW_THREADS, smem, st>>>(c);
+    pair_atm_bwd_finish_kernel<<<dim3((c.N + 255) / 256, c.B), 256, 0, st>>>(c);
+  } else {
+    pair_atm_bwd_tc_kernel<<<dim3((c.N + TC_M - 1) / TC_M, c.B), BW_THREADS, smem, st>>>(c);
+  }
 }
 
 }  // namespace d4
