@@ -8,8 +8,8 @@
 //                                  shared memory) and the full inverse X of
 //                                  its factor, stored over the block
 //                          panel   L21 = A21 X^T, 64-row tiles
-//                          syrk    A22 -= L21 L21^T, 128 x 128 lower tiles,
-//                                  8 x 8 register tiles (an FP32 SGEMM)
+//                          syrk    A22 -= L21 L21^T, 128 x 128 lower tiles
+//                                  on the tensor cores (tcgen05, split TF32)
 //   inverse (once):         the 512 x 512 diagonal blocks of the factor
 //                          are inverted (block forward substitution over
 //                          their panels, 128 x 128 products)
@@ -28,6 +28,7 @@
 #include "d4_chol.cuh"
 #include "d4_common.cuh"
 #include "d4_kernels.cuh"
+#include "d4_tc.cuh"
 
 namespace d4 {
 
@@ -166,12 +167,36 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
 size_t eeq_big_panel_smem() { return 4 * ((size_t)BNB * (BNB + 4) + (size_t)BNB * (64 + 4)); }
 
 // Trailing update A22 -= L21 L21^T of the lower 128 x 128 tiles (ti >= tj)
-// right of the panel.  K = kb in chunks of 16 staged transposed in shared
-// memory; 16 x 16 threads with 8 x 8 register tiles.
-constexpr int SK = 16;
-__global__ void __launch_bounds__(256) eeq_big_syrk_kernel(Ctx c, int k0) {
-  __shared__ __align__(16) float As[SK][BNB + 4];
-  __shared__ __align__(16) float Bs[SK][BNB + 4];
+// right of the panel, on the tensor cores.  One CTA (128 threads) per tile:
+//  - the two 128 x kb row blocks of the panel are staged in chunks of 32
+//    columns, a warp reading one row per step (lanes over columns, 128-byte
+//    coalesced loads), split hi = tf32(v), lo = tf32(v - hi), into the
+//    canonical K-major layout with padded core-matrix strides (LBO = 144
+//    bytes, so the 32 lanes of a row store to 32 different banks);
+//  - one thread issues tcgen05 kind::tf32 MMAs (M = N = 128, lo hi, hi lo,
+//    hi hi per k-step) into a 128-column tensor-memory accumulator;
+//  - the tile goes from tensor memory through shared memory (thread = row)
+//    so that the warps update the matrix row by row with coalesced accesses.
+// The split products keep the update at about FP32 accuracy (a few 1e-7
+// relative), which the FP64 refinement of the solves absorbs.
+constexpr int SY_KC = 32;                    // panel columns per chunk
+constexpr int SY_LBO = 144;                  // bytes between core matrices along K (128 + 16)
+constexpr int SY_SBO = (SY_KC / 4) * SY_LBO; // bytes between groups of 8 rows
+constexpr int SY_PLANE = (BNB / 8) * SY_SBO; // bytes of one 128 x 32 operand
+constexpr int SY_COLS = 128;                 // tensor memory: the 128 x 128 tile
+constexpr int SY_TLD = BNB + 1;              // row stride (floats) of the staged result tile
+
+static_assert(4 * SY_PLANE >= 4 * BNB * SY_TLD, "the result tile reuses the operand planes");
+
+__device__ __forceinline__ int sy_off(int r, int k) {  // bytes
+  return (r >> 3) * SY_SBO + (k >> 2) * SY_LBO + (r & 7) * 16 + (k & 3) * 4;
+}
+
+__global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0) {
+  extern __shared__ __align__(128) unsigned char s_raw[];
+  unsigned char *planes = s_raw;  // A hi, A lo, B hi, B lo
+  __shared__ unsigned long long s_mbar;
+  __shared__ uint32_t s_tmem;
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   if (k0 >= m) return;
@@ -183,53 +208,118 @@ __global__ void __launch_bounds__(256) eeq_big_syrk_kernel(Ctx c, int k0) {
   if (i0 >= m) return;
   const int N = c.N;
   float *F = c.w.eeq_F + (size_t)b * N * N;
-  const int tid = threadIdx.x;
-  const int ty = tid >> 4, tx = tid & 15;
-  float acc[8][8];
+  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const uint32_t mbar = tc::smem_u32(&s_mbar);
+  if (warp == 0) tc::tmem_alloc(tc::smem_u32(&s_tmem), SY_COLS);
+  if (tid == 0) tc::mbar_init(mbar, 1);
+  tc::fence_before_sync();
+  __syncthreads();
+  tc::fence_after_sync();
+  const uint32_t tmem = s_tmem;
+  constexpr uint32_t IDESC = tc::idesc_tf32(BNB, BNB);
+  const uint32_t p_base = tc::smem_u32(planes);
+  uint32_t parity = 0;
+  bool timed_out = false;
+  // a warp stages rows warp, warp + 4, ...; the loads of the next chunk are
+  // issued before the wait for the current chunk's MMAs
+  constexpr int RW = BNB / 4;  // rows per warp
+  float va[RW], vb[RW];
+  auto load_chunk = [&](int kc) {
+    const int k = kc + lane;
+    const bool kok = k < kb;
 #pragma unroll
-  for (int q = 0; q < 8; ++q)
-#pragma unroll
-    for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
-  // loader: thread t stages row t >> 1, columns 8 (t & 1) .. +8 of the chunk
-  const int lrow = tid >> 1, lcol = (tid & 1) * 8;
-  const int ia = i0 + lrow, jb = j0 + lrow;
-  const float *pa = F + (size_t)min(ia, m - 1) * N + k0;
-  const float *pb = F + (size_t)min(jb, m - 1) * N + k0;
-  for (int c0 = 0; c0 < kb; c0 += SK) {
-#pragma unroll
-    for (int q = 0; q < 8; ++q) {
-      const int cc = c0 + lcol + q;
-      As[lcol + q][lrow] = (ia < m && cc < kb) ? pa[cc] : 0.f;
-      Bs[lcol + q][lrow] = (jb < m && cc < kb) ? pb[cc] : 0.f;
+    for (int q = 0; q < RW; ++q) {
+      const int r = warp + 4 * q;
+      const int ia = i0 + r, jb = j0 + r;
+      va[q] = (kok && ia < m) ? F[(size_t)ia * N + k0 + k] : 0.f;
+      vb[q] = (kok && jb < m) ? F[(size_t)jb * N + k0 + k] : 0.f;
     }
-    __syncthreads();
-#pragma unroll 4
-    for (int kk = 0; kk < SK; ++kk) {
-      const float4 a0 = *reinterpret_cast<const float4 *>(&As[kk][8 * ty]);
-      const float4 a1 = *reinterpret_cast<const float4 *>(&As[kk][8 * ty + 4]);
-      const float4 b0 = *reinterpret_cast<const float4 *>(&Bs[kk][8 * tx]);
-      const float4 b1 = *reinterpret_cast<const float4 *>(&Bs[kk][8 * tx + 4]);
-      const float av[8] = {a0.x, a0.y, a0.z, a0.w, a1.x, a1.y, a1.z, a1.w};
-      const float bv[8] = {b0.x, b0.y, b0.z, b0.w, b1.x, b1.y, b1.z, b1.w};
+  };
+  load_chunk(0);
+  for (int kc = 0; kc < kb; kc += SY_KC) {
 #pragma unroll
-      for (int q = 0; q < 8; ++q)
-#pragma unroll
-        for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], bv[u], acc[q][u]);
+    for (int q = 0; q < RW; ++q) {
+      const int off = sy_off(warp + 4 * q, lane);
+      const float ah = tc::to_tf32(va[q]), bh = tc::to_tf32(vb[q]);
+      *reinterpret_cast<float *>(planes + off) = ah;
+      *reinterpret_cast<float *>(planes + SY_PLANE + off) = tc::to_tf32(va[q] - ah);
+      *reinterpret_cast<float *>(planes + 2 * SY_PLANE + off) = bh;
+      *reinterpret_cast<float *>(planes + 3 * SY_PLANE + off) = tc::to_tf32(vb[q] - bh);
     }
+    tc::fence_async_smem();
     __syncthreads();
+    if (tid == 0) {
+      tc::fence_after_sync();
+#pragma unroll
+      for (int pr = 0; pr < 3; ++pr) {  // lo hi, hi lo, hi hi
+        const uint32_t ab = p_base + (pr == 0 ? SY_PLANE : 0);
+        const uint32_t bb = p_base + 2 * SY_PLANE + (pr == 1 ? SY_PLANE : 0);
+#pragma unroll
+        for (int s = 0; s < SY_KC / 8; ++s)
+          tc::mma_tf32(tmem, tc::desc_kmajor(ab + 2 * SY_LBO * s, SY_LBO, SY_SBO),
+                       tc::desc_kmajor(bb + 2 * SY_LBO * s, SY_LBO, SY_SBO), IDESC,
+                       (kc > 0 || pr > 0 || s > 0) ? 1u : 0u);
+      }
+      tc::commit(mbar);
+    }
+    if (kc + SY_KC < kb) load_chunk(kc + SY_KC);
+    const bool done = tc::mbar_wait(mbar, parity);
+    parity ^= 1u;
+    if (__syncthreads_or(!done)) {
+      timed_out = true;
+      break;
+    }
   }
+  if (timed_out) {
+    if (tid == 0) set_status(c.w.status, D4_ERR_DEVICE_TIMEOUT);
+    tc::mbar_wait(mbar, parity ^ 1u);
+  } else {
+    // tensor memory -> shared tile (thread = row) -> row-wise coalesced update
+    tc::fence_after_sync();
+    float *T = reinterpret_cast<float *>(planes);
+    const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
+#pragma unroll 1
+    for (int cc = 0; cc < BNB; cc += 16) {
+      uint32_t v[16];
+      tc::tmem_ld16(tmem + t_lane + cc, v);
+      tc::tmem_ld_wait();
 #pragma unroll
-  for (int q = 0; q < 8; ++q) {
-    const int i = i0 + 8 * ty + q;
-    if (i >= m) continue;
-    float *row = F + (size_t)i * N;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int j = j0 + 8 * tx + u;
-      if (j <= i) row[j] -= acc[q][u];
+      for (int u = 0; u < 16; ++u) T[tid * SY_TLD + cc + u] = __uint_as_float(v[u]);
     }
+    __syncthreads();
+    // 8 rows per step with all their loads in flight before the stores
+#pragma unroll 1
+    for (int r0 = warp; r0 < BNB; r0 += 32) {
+      float cur[8][BNB / 32];
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        const int i = i0 + r0 + 4 * h;
+#pragma unroll
+        for (int q = 0; q < BNB / 32; ++q) {
+          const int j = j0 + q * 32 + lane;
+          cur[h][q] = (i < m && j < m && j <= i) ? F[(size_t)i * N + j] : 0.f;
+        }
+      }
+#pragma unroll
+      for (int h = 0; h < 8; ++h) {
+        const int r = r0 + 4 * h, i = i0 + r;
+#pragma unroll
+        for (int q = 0; q < BNB / 32; ++q) {
+          const int jl = q * 32 + lane, j = j0 + jl;
+          if (i < m && j < m && j <= i) F[(size_t)i * N + j] = cur[h][q] - T[r * SY_TLD + jl];
+        }
+      }
+    }
+  }
+  tc::fence_before_sync();
+  __syncthreads();
+  if (warp == 0) {
+    tc::fence_after_sync();
+    tc::tmem_free(tmem, SY_COLS);
   }
 }
+
+size_t eeq_big_syrk_smem() { return (size_t)4 * SY_PLANE; }
 
 // ---------------------------------------------------------------- solves
 
@@ -655,6 +745,8 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
                          (int)eeq_big_diag_smem());
     cudaFuncSetAttribute(eeq_big_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
                          (int)eeq_big_panel_smem());
+    cudaFuncSetAttribute(eeq_big_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                         (int)eeq_big_syrk_smem());
     for (int p = 0; p < npan; ++p) {
       const int k0 = p * BNB;
       eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), st>>>(c, k0);
@@ -662,7 +754,7 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
       if (rest <= 0) break;
       eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), st>>>(c, k0);
       const int T = (rest + BNB - 1) / BNB;
-      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), 256, 0, st>>>(c, k0);
+      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0);
     }
   }
   const int nsb = eeq_nsb(N);
