@@ -555,10 +555,13 @@ __global__ void __launch_bounds__(256) eeq_sweep_below_kernel(Ctx c, int sblk, i
   }
 }
 
-// Backward sweep update above block s: Y_i -= F[blk][i] . V_blk, thread per
-// row (coalesced over i), the block's V in shared memory.
+// Backward sweep update above block s: Y_i -= F[blk][i] . V_blk.  A CTA
+// takes 64 rows i, four threads per row splitting the block's 512 columns
+// (reads coalesced over i), partial sums combined in shared memory.
+constexpr int AB_ROWS = 64;
 __global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
   __shared__ float s_v[2][EEQ_SB];
+  __shared__ float s_part[2][4][AB_ROWS];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   const int s0 = sblk * EEQ_SB;
@@ -572,17 +575,36 @@ __global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, i
     s_v[r][k] = k < kb ? V[(size_t)r * N + s0 + k] : 0.f;
   }
   __syncthreads();
-  const int i = blockIdx.x * blockDim.x + threadIdx.x;
-  if (i >= s0) return;
-  const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)s0 * N + i;
+  const int rr = threadIdx.x & (AB_ROWS - 1), qk = threadIdx.x / AB_ROWS;
+  const int i = blockIdx.x * AB_ROWS + rr;
   float a0 = 0.f, a1 = 0.f;
-  for (int k = 0; k < kb; ++k) {
-    const float x = F[(size_t)k * N];
-    a0 = fmaf(x, s_v[0][k], a0);
-    if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
+  if (i < s0) {
+    const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)s0 * N + i;
+    const int kq = EEQ_SB / 4;
+    const int k_lo = qk * kq, k_hi = min(kb, k_lo + kq);
+    float b0 = 0.f, b1 = 0.f;
+#pragma unroll 4
+    for (int k = k_lo; k < k_hi; ++k) {
+      const float x = F[(size_t)k * N];
+      if (k & 1) {
+        b0 = fmaf(x, s_v[0][k], b0);
+        if (nr == 2) b1 = fmaf(x, s_v[1][k], b1);
+      } else {
+        a0 = fmaf(x, s_v[0][k], a0);
+        if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
+      }
+    }
+    a0 += b0;
+    a1 += b1;
   }
-  Y[i] -= a0;
-  if (nr == 2) Y[N + i] -= a1;
+  s_part[0][qk][rr] = a0;
+  s_part[1][qk][rr] = a1;
+  __syncthreads();
+  if (qk == 0 && i < s0) {
+    Y[i] -= (s_part[0][0][rr] + s_part[0][1][rr]) + (s_part[0][2][rr] + s_part[0][3][rr]);
+    if (nr == 2)
+      Y[N + i] -= (s_part[1][0][rr] + s_part[1][1][rr]) + (s_part[1][2][rr] + s_part[1][3][rr]);
+  }
 }
 
 // x += v (double-float).
@@ -779,7 +801,7 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
       eeq_sweep_diag_kernel<<<dim3(EEQ_SB / 8, B), 256, 0, st>>>(c, sb, it, 1, nr, 1);
       const int s0 = sb * EEQ_SB;
       if (s0 > 0)
-        eeq_sweep_above_kernel<<<dim3((s0 + 255) / 256, B), 256, 0, st>>>(c, sb, it, nr);
+        eeq_sweep_above_kernel<<<dim3((s0 + AB_ROWS - 1) / AB_ROWS, B), 256, 0, st>>>(c, sb, it, nr);
     }
     eeq_big_update_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, it, nr);
     eeq_big_residual_kernel<<<dim3((N + 7) / 8, B), 256, 0, st>>>(c, it, nr);
