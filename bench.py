@@ -23,6 +23,8 @@ Lines printed by rank 0 (one JSON line):
 * ``large16k``: one 16000-atom structure in the precision form (pair / ATM
   cutoffs 50 / 25 Bohr), seconds per energy + force evaluation and stage
   times (``--no-large`` skips it).
+* ``diff256``: 256 structures with energies, forces and parameter gradients,
+  D4 and D4S, precision form against the plain FP64 kernels;
 * ``serving``: the 20000-request stream through the continuous-batching
   server in real time (structures/s, p50 / p99 latency) and saturated, for
   the precision form and the plain FP64 kernels (``--serve-requests 0``
@@ -363,6 +365,50 @@ def run_large(pkg, disp, lib, dev, steps: int = 3):
     return out
 
 
+def run_diff(pkg, disp, dev, steps: int = 5):
+    """The differentiation form: 256 structures, N ~ U[20, 150] padded to
+    150, 12 elements, neutral, with the damping parameters drawn for the
+    first structure (s8, a1, a2; s6 = s9 = 1), energies + forces + the
+    gradient with respect to (s6, s8, a1, a2, s9) in one call, D4 and D4S,
+    precision form; structures/s and the largest differences to the plain
+    FP64 kernels on the same inputs."""
+    import torch
+
+    batch, params = pkg.workloads.diff256(3)
+    param = params[0]
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (batch.numbers, batch.positions,
+                                                        batch.charge))
+    B = nt.shape[0]
+    out = {"workload": "diff256: 256 structures, N~U[20,150] padded to 150, 12 elements, "
+                       "neutral, seed 3; energy + forces + parameter gradients",
+           "params": param}
+    for model in ("d4", "d4s"):
+        runs = {}
+        for precision in ("mixed", "fp64"):
+            r, _, _ = disp._prepare(nt, pt, ct, param, model, None, None, None, None, None,
+                                    None, None, None, precision)
+            res = r.run(pt, gradient=True, param_grad=True)
+            torch.cuda.synchronize()
+            ev = [torch.cuda.Event(enable_timing=True) for _ in range(2)]
+            ev[0].record()
+            for _ in range(steps):
+                res = r.run(pt, gradient=True, param_grad=True)
+            ev[1].record()
+            torch.cuda.synchronize()
+            ms = ev[0].elapsed_time(ev[1]) / steps
+            runs[precision] = (ms, res)
+        (ms_m, rm), (ms_p, rp) = runs["mixed"], runs["fp64"]
+        out[model] = {
+            "precision_form_structures_per_s": B / (ms_m * 1e-3),
+            "plain_fp64_structures_per_s": B / (ms_p * 1e-3),
+            "max_abs_dE_eh": (rm[0].sum(-1) - rp[0].sum(-1)).abs().max().item(),
+            "max_abs_dF_eh_bohr": (rm[1] - rp[1]).abs().max().item(),
+            "max_rel_dparam": ((rm[2][:, :7].sum(0) - rp[2][:, :7].sum(0)).abs() /
+                               rp[2][:, :7].sum(0).abs().clamp(min=1e-12)).max().item(),
+        }
+    return out
+
+
 def run_serving(pkg, param, nreq: int, plain_nreq: int):
     """The serving form: a Poisson stream of ``nreq`` single-structure
     energy + force requests at 2000 req/s, log-normal sizes (median 60 atoms,
@@ -529,6 +575,7 @@ def run_ours(args, world, rank, local):
     large = None
     if rank == 0 and not args.no_large:
         large = run_large(pkg, disp, lib, dev)
+    diff = run_diff(pkg, disp, dev) if rank == 0 and not args.no_large else None
     serve = None
     if rank == 0 and args.serve_requests > 0:
         serve = run_serving(pkg, param, args.serve_requests,
@@ -584,6 +631,7 @@ def run_ours(args, world, rank, local):
             "clocks": {k: clk[k] for k in ("sm_mhz", "sm_max_mhz", "reasons")},
             "cpu_baseline": cpu,
             "large16k": large,
+            "diff256": diff,
             "serving": serve,
         }
         print(json.dumps(line), flush=True)
