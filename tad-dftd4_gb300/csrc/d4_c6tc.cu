@@ -169,6 +169,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   float gacc[NFREQ];
 #pragma unroll
   for (int w = 0; w < NFREQ; ++w) gacc[w] = 0.f;
+  float r2mx = 0.f;  // largest r^2 of this thread's pairs (the ATM's all-inside test)
 
   constexpr uint32_t IDESC = tc::idesc_tf32(TC_M, TC_NJ);
   const uint32_t a_base = tc::smem_u32(&S.a[0][0]);
@@ -305,6 +306,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         // biases the three-body energy by ~1e-6 relative)
         const float l2R0r = log2f(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
         Tt[(size_t)j * N + i] = make_float4(r2, ir, alp3 * l2R0r, sqrtf(fmaxf(c60, 0.f)));
+        r2mx = fmaxf(r2mx, r2);
         if (PGRAD)
           Tdat[(size_t)j * N + i] =
               make_float4(sqq * iR0, iR0, l2R0r * 0.6931471805599453f, 0.f);
@@ -366,6 +368,8 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
     tc::fence_before_sync();
     __syncthreads();  // chunk buffers and tensor memory are free again
   }
+  r2mx = warp_maxf(r2mx);
+  if ((tid & 31) == 0 && r2mx > 0.f) atomicMax(&c.w.atm_r2max[b], __float_as_uint(r2mx));
   if (timed_out) {
     // an MMA batch did not complete in time: report it, give the tensor
     // cores one more bounded wait, release the tensor memory and leave

@@ -150,6 +150,8 @@ struct Workspace {
                     // neighbour-triple ATM)
   int *sorder;      // [B] structures by decreasing n_eff (launch order of the
                     // per-structure kernels of the precision form)
+  unsigned *atm_r2max;  // [B] largest r^2 over the real pairs of each structure
+                        // (FP32 bits; written by the pair kernels of the precision form)
   size_t bytes;
 };
 
@@ -214,6 +216,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   if (mixed) {
     w.adj32 = (float4 *)take(16 * BN);
     w.sorder = (int *)take(sizeof(int) * (size_t)B);
+    w.atm_r2max = (unsigned *)take(sizeof(unsigned) * (size_t)B);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.prP32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.eeq_hi = (float *)take(4 * BNN);
@@ -359,6 +362,12 @@ __device__ __forceinline__ float3 pos_diff(const float4 &pi, const float4 &li, c
 __device__ __forceinline__ float warp_sumf(float v) {
 #pragma unroll
   for (int o = 16; o > 0; o >>= 1) v += __shfl_xor_sync(0xffffffffu, v, o);
+  return v;
+}
+
+__device__ __forceinline__ float warp_maxf(float v) {
+#pragma unroll
+  for (int o = 16; o > 0; o >>= 1) v = fmaxf(v, __shfl_xor_sync(0xffffffffu, v, o));
   return v;
 }
 

@@ -362,6 +362,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   const float rho6 = p.s6 != 0.0 ? 1.f : 0.f;
   Acc32 e_acc, e8_acc, gx, gy, gz;
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
+  float r2mx = 0.f;  // largest r^2 of this atom's pairs (the ATM's all-inside test)
   for (int s = 0; s < nslot; ++s) {
     if (lane < NFREQ) {  // A' already carries sqrt((3/pi) w): C6 = sum_w A'_i A'_j
       const size_t o = a32_index(b, i, s, lane, N, c.S);
@@ -410,6 +411,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
       const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
       const float lnR0r = logf(R0 * ir) + R0d.lo / R0;
       T[j] = make_float4(r2, ir, alp3_log2e * lnR0r, sqrtf(c60));
+      r2mx = fmaxf(r2mx, r2);
       if (PGRAD) Tda[j] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
       if (r <= cut2) {
         const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R06d.hi;
@@ -468,6 +470,8 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   if (GRAD && lane < NFREQ)
     for (int s = nslot; s < c.S; ++s) c.w.G32[(ai * c.S + s) * NFREQ + lane] = 0.f;
   const Acc32 ea = warp_sum_acc(e_acc), ea8 = warp_sum_acc(e8_acc);
+  r2mx = warp_maxf(r2mx);
+  if (lane == 0) atomicMax(&c.w.atm_r2max[b], __float_as_uint(r2mx));
   if (PGRAD) {
     float v[5];
 #pragma unroll
@@ -504,6 +508,7 @@ __global__ void __launch_bounds__(1024) size_order_kernel(Ctx c) {
   extern __shared__ unsigned long long s_ord[];
   const int B = c.B;
   const int tid = threadIdx.x;
+  for (int t = tid; t < B; t += blockDim.x) c.w.atm_r2max[t] = 0u;  // the pair kernels raise it
   if (B > SORDER_MAX) {
     for (int t = tid; t < B; t += blockDim.x) c.w.sorder[t] = t;
     return;
@@ -890,6 +895,357 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
       if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev * acc.escale);
     }
   }
+}
+
+// ---------------------------------------------------------------- ATM, register-tiled
+
+// Shared-memory ATM (n <= 234) for structures whose real pairs all lie
+// inside the three-body cutoff (the pair kernels record each structure's
+// largest r^2), with no padding below the last real atom and unit atom
+// weights: every triple then carries the full mask, so the attribution
+// weights are 1 and the atom energies follow from the pair sums,
+// E_x = sum_y P(x, y) (each triple reaches x through two pairs; the same
+// total as the per-triple attribution eu / 3 per atom).
+//
+// A warp task is a tile of AT_C = 8 consecutive middle atoms j (j0 .. j0+7)
+// and a chunk of 8 outer atoms k > j.  Lane (q, l) = (lane / 8, lane % 8)
+// takes k = kc + l and keeps the eight (j, k) pair records and their
+// dE/dr^2 and energy sums in registers; the four lane groups q walk the
+// inner atoms i < j in step (group q takes every fourth i of the CTA's
+// sequence).  Per i a lane reads the (i, k) record and the eight (i, j)
+// records (one row segment per group), evaluates eight triples, adds its
+// (i, k) sums to shared memory once, and the group reduce-scatters its
+// sixteen (i, j) sums over its eight lanes.  8 x 8 tiles keep the triples
+// evaluated outside i < j < k at ~22 % for sizes 8..200 (8 x 32: ~50 %).
+// The triple arithmetic is that of atm_task with the weights at 1.
+// Structures outside these conditions run atm_task in the same kernel.
+constexpr int AT_C = 8;             // middle atoms per task (and outer atoms per chunk)
+constexpr int AT_THREADS = 768;     // 24 warps at 80 registers (measured: 512 threads
+                                    // at 128 registers, no spills, 4 % slower)
+constexpr int AT_TASKS_MAX = 900;   // tiles x chunks for n <= 237 (30 x 30)
+constexpr int AT_CTA_TRIPLES = 600000;
+
+__host__ __device__ inline size_t atm_tiled_smem_bytes(int N) {
+  return atm_smem_bytes(N) + sizeof(int) * AT_TASKS_MAX;
+}
+
+__device__ __forceinline__ int atm_tiled_ctas(int n) {
+  const long long work = (long long)n * n * n / 6;
+  const int K = (int)((work + AT_CTA_TRIPLES - 1) / AT_CTA_TRIPLES);
+  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
+}
+
+// tri_u(i, x, n) = tri_row(i, n) + x for x > i
+__device__ __forceinline__ int tri_row(int i, int n) { return i * n - i * (i + 1) / 2 - i - 1; }
+
+// 1 / x to the SFU's ~1 ulp (x >= 1 here)
+__device__ __forceinline__ float sfu_rcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
+// Halving exchanges over the lane bits H, H/2, ... (STEPS of them): v[p]
+// for p < NV >> STEPS ends as the sum over the 2^STEPS lanes that differ in
+// those bits of the value with index p + (NV/2) bit(H) + (NV/4) bit(H/2) + ...
+template <int NV, int H, int STEPS>
+__device__ __forceinline__ void lane_halving(float (&v)[NV]) {
+  const int lane = threadIdx.x & 31;
+#pragma unroll
+  for (int s = 0; s < STEPS; ++s) {
+    const int m = NV >> (s + 1), h = H >> s;
+    const bool up = (lane & h) != 0;
+#pragma unroll
+    for (int q = 0; q < m; ++q) {
+      const float keep = up ? v[q + m] : v[q];
+      const float send = up ? v[q] : v[q + m];
+      v[q] = keep + __shfl_xor_sync(0xffffffffu, send, h);
+    }
+  }
+}
+
+// One step of a tile task: inner atom i of this lane's group.  GUARD: some
+// (i, j) of the step are not pairs (i >= j, j beyond the structure, i
+// beyond the task's range).
+template <bool GRAD, bool GUARD>
+__device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, float *sS, float *sP,
+                                              int n, int N, int j0, int jend, int k, bool kok,
+                                              int i, float alp3h, const float (&zjk)[AT_C],
+                                              const float (&irjk)[AT_C],
+                                              const float (&Ljk)[AT_C],
+                                              const float (&cjk)[AT_C], float (&Sjk)[AT_C],
+                                              float (&Pjk)[AT_C]) {
+  const int l = threadIdx.x & 7;
+  const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
+  const bool iok = !GUARD || i < jend - 1;
+  const float4 *Ti = T + (size_t)(iok ? i : 0) * N;
+  const bool lk = iok && kok && k > i;
+  const float4 pik = lk ? Ti[k] : zero4;
+  const float y = pik.x, iry = pik.y, Ly = pik.z, cy = pik.w;
+  const float y2ik = iry * iry;
+  float Sik = 0.f, Pik = 0.f;
+  constexpr int NV = GRAD ? 2 * AT_C : AT_C;
+  float v[NV];  // (i, j) sums: dE/dr^2 (GRAD) then energies
+#pragma unroll
+  for (int t = 0; t < AT_C; ++t) {
+    float4 pij;
+    if (GUARD) {
+      const int jt = j0 + t;
+      const bool ok = iok && jt > i && jt < jend;
+      pij = ok ? Ti[ok ? jt : 0] : zero4;
+    } else {
+      pij = Ti[j0 + t];
+    }
+    const float x = pij.x, irx = pij.y, z = zjk[t];
+    const float ir1 = irx * (iry * irjk[t]);
+    const float ir2 = ir1 * ir1;
+    const float ir3 = ir1 * ir2;
+    const float u = x - y;
+    const float A = u + z, Bv = (x + y) - z, Cv = z - u;
+    const float AB = A * Bv;
+    const float sfac = AB * Cv;
+    const float h = 0.375f * ir2;
+    const float ang = ir3 * fmaf(sfac, h, 1.0f);
+    const float ta = sfu_exp2(pij.z + Ly + Ljk[t]);
+    const float fd = sfu_rcp(fmaf(6.0f, ta, 1.0f));
+    const float c9 = pij.w * cy * cjk[t];
+    const float cf = c9 * fd;
+    const float eu = cf * ang;  // triple energy without s9
+    Pik += eu;
+    Pjk[t] += eu;
+    if (GRAD) {
+      // U = 3/8 c9 fd r^-10, V = c9 / 2 (fd (2 r^-6 - 5 ang) + ang alp/3 fd (1 - fd))
+      const float U = cf * h * ir3;
+      const float g = fmaf(-fd, fd, fd);
+      const float V = c9 * fmaf(fd, fmaf(-2.5f, ang, ir3), ang * (alp3h * g));
+      const float AC = A * Cv, BC = Bv * Cv;
+      const float Sg = AB + AC + BC;
+      const float dex = fmaf(U, fmaf(-2.0f, AB, Sg), V * (irx * irx));
+      const float dey = fmaf(U, fmaf(-2.0f, BC, Sg), V * y2ik);
+      const float dez = fmaf(U, fmaf(-2.0f, AC, Sg), V * (irjk[t] * irjk[t]));
+      Sik += dey;
+      Sjk[t] += dez;
+      v[t] = dex;
+      v[AT_C + t] = eu;
+    } else {
+      v[t] = eu;
+    }
+  }
+  const int rb = tri_row(i, n);
+  if (lk) {
+    if (GRAD) atomicAdd(&sS[rb + k], Sik);
+    atomicAdd(&sP[rb + k], Pik);
+  }
+  // group sums over the eight lanes: lane l keeps values NV/8 l .. NV/8 l + NV/8 - 1
+  lane_halving<NV, 4, 3>(v);
+#pragma unroll
+  for (int p = 0; p < NV / 8; ++p) {
+    const int idx = (NV / 8) * l + p;
+    const int jt = j0 + idx % AT_C;
+    if (!GUARD || (iok && jt > i && jt < jend && v[p] != 0.f))
+      atomicAdd(&((GRAD && idx < AT_C) ? sS : sP)[rb + jt], v[p]);
+  }
+}
+
+template <bool GRAD>
+__device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, float *sS, float *sP,
+                                              int n, int N, int j0, int kc, int i0, int istep,
+                                              float alp3h) {
+  const int lane = threadIdx.x & 31;
+  const int q = lane >> 3;
+  const int k = kc + (lane & 7);
+  const bool kok = k < n;
+  float zjk[AT_C], irjk[AT_C], Ljk[AT_C], cjk[AT_C], Sjk[AT_C], Pjk[AT_C];
+#pragma unroll
+  for (int t = 0; t < AT_C; ++t) {
+    const int jt = j0 + t;
+    const bool ok = kok && jt < k;  // then also jt <= n - 2
+    const float4 r = ok ? T[(size_t)jt * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    zjk[t] = r.x;
+    irjk[t] = r.y;
+    Ljk[t] = r.z;
+    cjk[t] = r.w;  // 0 also zeroes every product of a (j, k) that is not a pair
+    Sjk[t] = 0.f;
+    Pjk[t] = 0.f;
+  }
+  const int jend = min(j0 + AT_C, n - 1);  // middle atoms j0 .. jend - 1
+  // group q takes i = i0 + (4 s + q) istep, s = 0, 1, ...
+  const int st4 = 4 * istep;
+  int ib = i0;  // i of group 0 in this step
+  if (j0 + AT_C <= n - 1)
+    for (; ib + 3 * istep < j0; ib += st4)
+      atm_tile_step<GRAD, false>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
+                                 irjk, Ljk, cjk, Sjk, Pjk);
+  for (; ib < jend - 1; ib += st4)
+    atm_tile_step<GRAD, true>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
+                              irjk, Ljk, cjk, Sjk, Pjk);
+  // (j, k) sums of the four groups: group q keeps values NV/4 q .. NV/4 q + NV/4 - 1
+  constexpr int NV = GRAD ? 2 * AT_C : AT_C;
+  float v[NV];
+#pragma unroll
+  for (int t = 0; t < AT_C; ++t) {
+    if (GRAD) {
+      v[t] = Sjk[t];
+      v[AT_C + t] = Pjk[t];
+    } else {
+      v[t] = Pjk[t];
+    }
+  }
+  lane_halving<NV, 16, 2>(v);
+#pragma unroll
+  for (int p = 0; p < NV / 4; ++p) {
+    const int idx = (NV / 4) * q + p;
+    const int jt = j0 + idx % AT_C;
+    if (kok && jt < k && v[p] != 0.f)
+      atomicAdd(&((GRAD && idx < AT_C) ? sS : sP)[tri_u(jt, k, n)], v[p]);
+  }
+}
+
+template <bool GRAD>
+__global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
+  extern __shared__ float s_acc[];
+  __shared__ int s_next, s_ntask;
+  const int b = c.w.sorder[blockIdx.y];
+  const int cta = blockIdx.x;
+  const int N = c.N;
+  const int n = c.w.n_eff[b];
+  if (n < 3) return;
+  const int K = atm_tiled_ctas(n);
+  if (cta >= K) return;
+  const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
+  const int nwarps = blockDim.x >> 5;
+  const int P = n * (n - 1) / 2;
+  float *sS = s_acc, *sP = s_acc + P, *sE = s_acc + 2 * P;
+  int *s_task = reinterpret_cast<int *>(s_acc + 2 * P + n);
+  const float cut2 = c.pf.cut3 * c.pf.cut3;
+  const bool fast = c.w.n_real[b] == n && __uint_as_float(c.w.atm_r2max[b]) <= cut2;
+  for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
+  const int NT = (n - 2 + AT_C - 1) / AT_C;  // tiles of middle atoms 1 .. n - 2
+  if (fast && threadIdx.x < NT) {
+    // task table: tiles from the last (longest i range) to the first, the
+    // chunks of eight outer atoms of each in order
+    auto nch = [&](int ti) { return (n - 1 - (1 + AT_C * ti) + AT_C - 1) / AT_C; };
+    const int ti = threadIdx.x;
+    int off = 0;
+    for (int u = NT - 1; u > ti; --u) off += nch(u);
+    for (int ch = 0; ch < nch(ti); ++ch) s_task[off + ch] = (ti << 8) | ch;
+    if (ti == 0) {
+      s_ntask = off + nch(0);
+      s_next = nwarps;
+    }
+  }
+  __syncthreads();
+  const float4 *T = c.w.ptf + (size_t)b * N * N;
+  if (fast) {
+    const float alp3h = 0.5f * c.pf.alp3;
+    const int ntask = s_ntask;
+    for (int task = warp; task < ntask;) {
+      const int e = s_task[task];
+      const int j0 = 1 + AT_C * (e >> 8);
+      atm_tile_task<GRAD>(T, sS, sP, n, N, j0, j0 + 1 + AT_C * (e & 255), cta, K, alp3h);
+      int nx = 0;
+      if (lane == 0) nx = atomicAdd(&s_next, 1);
+      task = __shfl_sync(0xffffffffu, nx, 0);
+    }
+  } else {
+    AtmAcc<true> acc;
+    acc.n = n;
+    acc.N = N;
+    acc.sS = sS;
+    acc.sP = sP;
+    acc.sE = sE;
+    acc.gS = acc.gP = nullptr;
+    acc.gE = nullptr;
+    acc.escale = c.par.s9 / 6.0;
+    AtmIn in;
+    in.Zb = c.w.z + (size_t)b * N;
+    in.gaps = c.w.n_real[b] != n;
+    in.T = T;
+    in.Tda = nullptr;
+    in.W = c.w.w32 + (size_t)b * N;
+    in.cut2 = cut2;
+    in.alp3 = c.pf.alp3;
+    in.s9 = c.pf.s9;
+    in.s9m = 1.f;
+    in.weighted = false;
+    in.N = N;
+    AtmPg pg;
+    int j = 1, jbase = 0, nch = (n - 2 + 31) >> 5;
+    for (int t = warp;; t += nwarps) {
+      while (j < n - 1 && t >= jbase + nch) {
+        jbase += nch;
+        ++j;
+        nch = (n - 1 - j + 31) >> 5;
+      }
+      if (j >= n - 1) break;
+      if (in.gaps && in.Zb[j] == 0) continue;
+      atm_task<true, GRAD, false>(in, acc, n, j, j + 1 + 32 * (t - jbase), cta, K, pg);
+    }
+  }
+  __syncthreads();
+  // Flush: the upper half of the pair sums row by row (lanes over k > j),
+  // then the lower half row by row (lanes over j < k), both coalesced in
+  // global memory; a structure with one CTA stores, several CTAs add.  The
+  // tiled path's atom energies are the row sums of P: the part over y > x
+  // in the first pass (parked in sE), the part over y < x in the second.
+  const float s9 = c.pf.s9;
+  float *gS = GRAD ? c.w.prS32 + (size_t)b * N * N : nullptr;
+  float *gP = GRAD ? c.w.prP32 + (size_t)b * N * N : nullptr;
+  const bool solo = K == 1;
+  const double escale = c.par.s9 / 6.0;
+  for (int j = warp; j < n; j += nwarps) {
+    const int rb = tri_row(j, n);
+    float er = 0.f;
+    for (int k = j + 1 + lane; k < n; k += 32) {
+      const float pv = sP[rb + k];
+      er += pv;
+      if (GRAD) {
+        const float sv = sS[rb + k];
+        float *ds = gS + (size_t)j * N + k, *dp = gP + (size_t)j * N + k;
+        if (solo) {
+          *ds = sv * s9;
+          *dp = pv * s9;
+        } else if (sv != 0.f || pv != 0.f) {
+          atomicAdd(ds, sv * s9);
+          atomicAdd(dp, pv * s9);
+        }
+      }
+    }
+    if (fast) {
+      er = warp_sumf(er);
+      if (lane == 0) sE[j] = er;
+    }
+  }
+  __syncthreads();
+  for (int k = warp; k < n; k += nwarps) {
+    float ec = 0.f;
+    for (int j = lane; j < k; j += 32) {
+      const int t = tri_u(j, k, n);
+      const float pv = sP[t];
+      ec += pv;
+      if (GRAD) {
+        const float sv = sS[t];
+        float *ds = gS + (size_t)k * N + j, *dp = gP + (size_t)k * N + j;
+        if (solo) {
+          *ds = sv * s9;
+          *dp = pv * s9;
+        } else if (sv != 0.f || pv != 0.f) {
+          atomicAdd(ds, sv * s9);
+          atomicAdd(dp, pv * s9);
+        }
+      }
+    }
+    if (fast) {
+      ec = warp_sumf(ec);
+      const float ev = ec + sE[k];  // E_k = sum_y P(k, y)
+      if (lane == 0 && ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + k], (double)ev * escale);
+    }
+  }
+  if (!fast)
+    for (int x = threadIdx.x; x < n; x += blockDim.x) {
+      const float ev = sE[x];
+      if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev * escale);
+    }
 }
 
 // Lower half of the ATM pair accumulators from the upper half (global
@@ -1811,7 +2167,18 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   const size_t atm_smem = atm_smem_bytes(N);
   const bool atm_sm = atm_smem_fits(N);
   stage_begin(ST_ATM, st);
-  if (atm_sm) {
+  if (atm_sm && !pgrad && c.weights == nullptr) {  // register-tiled triples
+    const size_t sm = atm_tiled_smem_bytes(N);
+    if (grad) {
+      cudaFuncSetAttribute(atm_tiled_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+      atm_tiled_kernel<true><<<dim3(ATM_KMAX, B), AT_THREADS, sm, st>>>(c);
+    } else {
+      cudaFuncSetAttribute(atm_tiled_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
+                           (int)sm);
+      atm_tiled_kernel<false><<<dim3(ATM_KMAX, B), AT_THREADS, sm, st>>>(c);
+    }
+  } else if (atm_sm) {
     if (pgrad)
       launch_atm<true, true, true>(c, st, atm_smem);
     else if (grad)

@@ -250,3 +250,37 @@ def test_neighbour_triple_atm_matches_dense_fp64_path(d4):
     gm = run("mixed", gradient=True, weights=w)[1]
     gp = run("fp64", gradient=True, weights=w)[1]
     assert (gm - gp).abs().max().item() <= F_TOL
+
+
+@pytest.mark.parametrize("cut3", [40.0, 12.0])
+@pytest.mark.parametrize("gradient", [True, False])
+def test_atm_tiles_and_per_triple_fallback_match_fp64(d4, cut3, gradient):
+    """The shared-memory ATM evaluates structures whose real pairs all lie
+    inside disp3 with register tiles of eight middle atoms (unit attribution
+    weights, atom energies from the pair sums); structures with a pair beyond
+    disp3 or padding below their last atom take the per-triple masks in the
+    same kernel.  disp3 = 40 Bohr: most structures tiled; 12 Bohr: most per
+    triple.  Energies (per structure and per atom) and forces match the
+    plain FP64 path within the precision bar, with and without gradients."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    b = wl.batch_uniform(303, 12, 5, 200, wl.ELEMENTS_12, True, "t", 200)
+    numbers = b.numbers.copy()
+    numbers[1, 2] = 0   # padding below the last real atom
+    numbers[4, 0] = 0
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (numbers, b.positions, b.charge))
+    cutoff = d4.Cutoff(disp3=cut3)
+
+    def run(precision):
+        runner, _, _ = disp._prepare(nt, pt, ct, PARAM, "d4", None, None, None, None, cutoff,
+                                     None, None, None, precision)
+        return runner.run(pt, gradient=gradient)
+
+    mixed, plain = run("mixed"), run("fp64")
+    em, ep = mixed[0].cpu().numpy(), plain[0].cpu().numpy()
+    assert np.abs(em - ep).max() <= E_TOL
+    assert np.abs(em.sum(-1) - ep.sum(-1)).max() <= E_TOL
+    if gradient:
+        assert (mixed[1] - plain[1]).abs().max().item() <= F_TOL
