@@ -616,7 +616,7 @@ def run_ours(args, world, rank, local):
                                    "p99": 1e3 * float(np.percentile(lat, 99))},
                     "api": "dftd4(precision='mixed') + torch.autograd.grad, pinned host buffers"},
             "roofline": {
-                "kernel": "atm_mixed_kernel<SMEM,GRAD> (FP32 arithmetic)", "bound": "fp32",
+                "kernel": "atm_tiled_kernel<GRAD> (FP32 arithmetic)", "bound": "fp32",
                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak else None,
                 "traffic": traffic.get("atm_mixed_batch512"),

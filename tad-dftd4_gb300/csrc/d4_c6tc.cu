@@ -302,10 +302,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         }
         const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
         const float iR0 = __frcp_rn(R0);
-        // log2(R0 / r), the ATM damping exponent (to ~1 ulp: an SFU estimate
-        // biases the three-body energy by ~1e-6 relative)
+        // log2(R0 / r) and (R0 / r)^(alp/3) of the ATM damping through the
+        // accurate log2f / exp2f (SFU estimates bias the three-body energy by
+        // ~1e-6 relative)
         const float l2R0r = log2f(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
-        Tt[(size_t)j * N + i] = make_float4(r2, ir, alp3 * l2R0r, sqrtf(fmaxf(c60, 0.f)));
+        const float ir2 = __frcp_rn(r2);
+        Tt[(size_t)j * N + i] = make_float4(r2, ir2, exp2f(alp3 * l2R0r),
+                                            sqrtf(fmaxf(c60, 0.f)) * (ir * ir2));
         r2mx = fmaxf(r2mx, r2);
         if (PGRAD)
           Tdat[(size_t)j * N + i] =
@@ -623,7 +626,7 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
     {
       constexpr int QH = BW_K / 2;
       const int q0 = half * QH;
-      float sv[QH], pv[QH], cv[QH];
+      float sv[QH], pv[QH], cv[QH];  // cv: record w = sqrt(C6(q=0)) / r^3
 #pragma unroll
       for (int u = 0; u < QH; ++u) {  // all loads of the half chunk first
         const int q = q0 + u, y = y0 + q;
@@ -631,18 +634,22 @@ __global__ void __launch_bounds__(BW_THREADS) pair_atm_bwd_tc_kernel(Ctx c) {
         const size_t o = (size_t)(ok ? y : 0) * N + x;  // the pair arrays are symmetric
         sv[u] = ok ? Sxy[o] : 0.f;
         pv[u] = ok ? Pxy[o] : 0.f;
-        cv[u] = ok ? T[o].w : 1.f;
+        cv[u] = ok ? T[o].w : 0.f;
       }
 #pragma unroll
       for (int u = 0; u < QH; ++u) {
         const int q = q0 + u;
-        if (sv[u] != 0.f) {
+        float D = 0.f;
+        if (sv[u] != 0.f || pv[u] != 0.f) {
           const float3 d = pos_diff(px, lx, S.py[q], S.ly[q]);
           gx.add(2.0f * sv[u] * d.x);
           gy.add(2.0f * sv[u] * d.y);
           gz.add(2.0f * sv[u] * d.z);
+          if (pv[u] != 0.f) {  // D = P / (2 C6(q=0)), C6(q=0) = w^2 r^6
+            const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+            D = pv[u] / (2.0f * (cv[u] * cv[u]) * (r2 * r2 * r2));
+          }
         }
-        const float D = pv[u] != 0.f ? pv[u] / (2.0f * cv[u] * cv[u]) : 0.f;
         split_tf32(S.a[0], S.a[1], kmaj32_off(row, q), D);
       }
     }

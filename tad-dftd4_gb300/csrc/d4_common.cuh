@@ -133,7 +133,7 @@ struct Workspace {
   float2 *el32;     // [MAX_ELEM_ID] (zeff, gam * gc)
   float *G32;       // [B*N*S*23] dE/dA
   float *G032;      // [B*N*S*23] dE/dA0
-  float4 *ptf;      // [B*N*N] (r^2, 1/r, alp/3 log2(R0/r), sqrt(C6(q=0)))
+  float4 *ptf;      // [B*N*N] (r^2, 1/r^2, (R0/r)^(alp/3), sqrt(C6(q=0)) / r^3)
   float4 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2, log(R0/r), 0)
   float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor (one-CTA path)
   float *eeq_F;     // [B*N*N] dense FP32 factor, block inverses on the diagonal (multi-CTA)

@@ -309,8 +309,8 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
 // ---------------------------------------------------------------- pairs
 
 // Fused C6 + BJ two-body term in FP32, the per-pair ATM table (float4:
-// r, 1/r, log(R0/r), sqrt(C6(q=0))), the direct gradient and the C6
-// adjoint.  One warp per atom i, lanes over partners j.
+// r^2, 1/r^2, (R0/r)^(alp/3), sqrt(C6(q=0)) / r^3), the direct gradient and
+// the C6 adjoint.  One warp per atom i, lanes over partners j.
 template <bool GRAD, bool PGRAD>
 __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   const int b = blockIdx.y;
@@ -410,7 +410,8 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
       }
       const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
       const float lnR0r = logf(R0 * ir) + R0d.lo / R0;
-      T[j] = make_float4(r2, ir, alp3_log2e * lnR0r, sqrtf(c60));
+      const float ir2 = __frcp_rn(r2);
+      T[j] = make_float4(r2, ir2, exp2f(alp3_log2e * lnR0r), sqrtf(c60) * (ir * ir2));
       r2mx = fmaxf(r2mx, r2);
       if (PGRAD) Tda[j] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
       if (r <= cut2) {
@@ -549,6 +550,13 @@ __device__ __forceinline__ float sfu_exp2(float x) {
   return y;
 }
 
+// 1 / x to the SFU's ~1 ulp (x >= 1 here: the ATM damping)
+__device__ __forceinline__ float sfu_rcp(float x) {
+  float y;
+  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
+  return y;
+}
+
 __device__ __forceinline__ int tri_u(int j, int k, int n) {  // j < k, upper triangle
   return j * n - j * (j + 1) / 2 + (k - j - 1);
 }
@@ -620,6 +628,50 @@ __device__ __forceinline__ float warp_sum3_scatter(float a, float b, float c) {
   return k;
 }
 
+// ATM triple (i, j, k) of the precision form from its three pair records
+// (r^2, 1/r^2, (R0/r)^(alp/3), sqrt(C6(q=0)) / r^3) of the pairs ij, ik,
+// jk (x, y, z = their r^2).  With R = r_ij r_ik r_jk, the angular factor is
+// w / R^3, w = 1 + 3/8 (x - y + z)(x + y - z)(y + z - x) / R^2, and C9 / R^3
+// is the product Q of the records' fourth entries, so the energy without s9
+// is eu = Q fd w with fd = 1 / (1 + 6 prod (R0/r)^(alp/3)) (the reference's
+// damping, model/d4.py three-body term through damping/atm.py).  dex, dey,
+// dez: d eu / d(x, y, z); qwg = Q w fd (1 - fd), for the parameter gradients.
+struct AtmTri {
+  float eu, dex, dey, dez, qwg;
+};
+
+template <bool GRAD>
+__device__ __forceinline__ AtmTri atm_triple(float x, float ix2, float ex, float qx, float y,
+                                             float iy2, float ey, float qy, float z, float iz2,
+                                             float ez, float qz, float alp3h) {
+  AtmTri r;
+  const float ir2 = ix2 * (iy2 * iz2);
+  const float h = 0.375f * ir2;
+  const float u = x - y;
+  const float A = u + z, Bv = (x + y) - z, Cv = z - u;
+  const float AB = A * Bv;
+  const float w = fmaf(AB * Cv, h, 1.0f);
+  const float fd = sfu_rcp(fmaf(6.0f, ex * (ey * ez), 1.0f));
+  const float Q = qx * (qy * qz);
+  const float cq = Q * fd;
+  r.eu = cq * w;
+  if (GRAD) {
+    // U = 3/8 C9 fd / R^5, V = C9 / (2 R^3) (fd (2 - 5 w) + w alp/3 fd (1 - fd))
+    const float g = fmaf(-fd, fd, fd);
+    const float U = cq * h;
+    const float V = Q * fmaf(fd, fmaf(-2.5f, w, 1.0f), w * (alp3h * g));
+    const float AC = A * Cv, BC = Bv * Cv;
+    const float Sg = AB + AC + BC;
+    r.dex = fmaf(U, fmaf(-2.0f, AB, Sg), V * ix2);
+    r.dey = fmaf(U, fmaf(-2.0f, BC, Sg), V * iy2);
+    r.dez = fmaf(U, fmaf(-2.0f, AC, Sg), V * iz2);
+    r.qwg = Q * w * g;
+  } else {
+    r.dex = r.dey = r.dez = r.qwg = 0.f;
+  }
+  return r;
+}
+
 // Constant inputs of the ATM triple loop of one structure.
 struct AtmIn {
   const int *Zb;
@@ -650,7 +702,8 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
   const int k = kc + lane;
   const bool kok = k < n && in.Zb[k] != 0;
   const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float zjk = pjk.x, irjk = pjk.y, Ljk = pjk.z, cjk = pjk.w;
+  const float zjk = pjk.x, izjk = pjk.y, ejk = pjk.z, qjk = pjk.w;
+  const float alp3h = 0.5f * alp3;
   const bool mjk = kok && zjk <= cut2;
   float4 dajk = make_float4(0.f, 0.f, 0.f, 0.f);
   if (PGRAD && kok) dajk = in.Tda[(size_t)j * N + k];
@@ -670,18 +723,9 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
       const float4 pik = *Tik;
       const bool mij = pij.x <= cut2, mik = pik.x <= cut2;
       if ((int)mij + (int)mik + (int)mjk >= 2) {
-        const float x = pij.x, y = pik.x, z = zjk;
-        const float ir1 = pij.y * irjk * pik.y;
-        const float ir2 = ir1 * ir1;
-        const float ir3 = ir1 * ir2;
-        const float u = x - y, v = x + y;
-        const float A = u + z, Bv = v - z, Cv = z - u;
-        const float sfac = A * Bv * Cv;
-        const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-        const float ta = sfu_exp2(pij.z + pik.z + Ljk);
-        const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
-        const float c9 = pij.w * pik.w * cjk;
-        const float eu = c9 * fd * ang;  // triple energy without s9
+        const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y, pik.z,
+                                           pik.w, zjk, izjk, ejk, qjk, alp3h);
+        const float eu = tr.eu;  // triple energy without s9
         const float e = s9m * eu;
         float wgt;
         // atom energies in units of e/6 (exact multiples; s9/6 is applied in
@@ -701,29 +745,21 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
           wgt = ((in.weighted ? W[i] : 1.f) * mi + wj * mj + wk * mk) * (1.0f / 6.0f);
         }
         if (GRAD) {
-          const float kc9 = s9m * c9;
-          const float dfl = alp3 * fd * (1.0f - fd);  // = 6 alp/3 ta fd^2
-          const float Q = 2.0f * ir3 - 5.0f * ang;
-          const float U = 0.375f * kc9 * fd * ir2 * ir3;
-          const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
-          const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
-          const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
-          const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
-          const float dez = fmaf(U, BC + AB - AC, V * irjk * irjk);
-          sij = wgt * dex;
-          Sjk = fmaf(wgt, dez, Sjk);
+          const float ws = wgt * s9m;
+          sij = ws * tr.dex;
+          Sjk = fmaf(ws, tr.dez, Sjk);
           const float we = wgt * e;
           pe = we;
           Pjk += we;
-          acc.pair(i, k, wgt * dey, we);
+          acc.pair(i, k, ws * tr.dey, we);
           if (PGRAD) {
             const float4 daij = in.Tda[(size_t)i * N + j];
             const float4 daik = in.Tda[(size_t)i * N + k];
             const float lsum = daij.z + daik.z + dajk.z;
-            const float dfd = -fd * (1.0f - fd);  // d fd / d(alp/3 sum log(R0/r))
+            // d fd / d(alp/3 sum log(R0/r)) = -fd (1 - fd)
             pg.s9 += wgt * eu;
-            pg.alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
-            const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
+            pg.alp -= wgt * s9 * tr.qwg * lsum * (1.0f / 3.0f);
+            const float dfa = -wgt * s9 * tr.qwg * alp3;
             pg.a1 += dfa * (daij.x + daik.x + dajk.x);
             pg.a2 += dfa * (daij.y + daik.y + dajk.y);
           }
@@ -783,9 +819,9 @@ __host__ __device__ inline int atm_ctas_big(int n) {
 // ATM energy and adjoint over triples i < j < k of one structure.  A warp
 // takes a task (j, 32 consecutive k > j) and loops over i: lanes hold the
 // (j, k) pair record in registers and read the (i, j) (broadcast) and (i, k)
-// (coalesced 128-bit) records.  A pair record holds r^2, 1/r,
-// alp/3 log2(R0/r) and sqrt(C6(q=0)), so the damping is one exp2 and C9 two
-// products.
+// (coalesced 128-bit) records.  A pair record holds r^2, 1/r^2,
+// (R0/r)^(alp/3) and sqrt(C6(q=0)) / r^3, so the damping factor and
+// C9 / (r_ij r_ik r_jk)^3 are two products each (atm_triple).
 //   SMEM (n <= 234): K <= 8 CTAs share a structure, interleaving i; per-pair
 //     dE/d(r^2) and mask-weighted triple energies accumulate in shared memory
 //     without the s9 factor, applied when a CTA flushes them (FP32 global
@@ -938,13 +974,6 @@ __device__ __forceinline__ int atm_tiled_ctas(int n) {
 // tri_u(i, x, n) = tri_row(i, n) + x for x > i
 __device__ __forceinline__ int tri_row(int i, int n) { return i * n - i * (i + 1) / 2 - i - 1; }
 
-// 1 / x to the SFU's ~1 ulp (x >= 1 here)
-__device__ __forceinline__ float sfu_rcp(float x) {
-  float y;
-  asm("rcp.approx.ftz.f32 %0, %1;" : "=f"(y) : "f"(x));
-  return y;
-}
-
 // Halving exchanges over the lane bits H, H/2, ... (STEPS of them): v[p]
 // for p < NV >> STEPS ends as the sum over the 2^STEPS lanes that differ in
 // those bits of the value with index p + (NV/2) bit(H) + (NV/4) bit(H/2) + ...
@@ -971,9 +1000,9 @@ template <bool GRAD, bool GUARD>
 __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, float *sS, float *sP,
                                               int n, int N, int j0, int jend, int k, bool kok,
                                               int i, float alp3h, const float (&zjk)[AT_C],
-                                              const float (&irjk)[AT_C],
-                                              const float (&Ljk)[AT_C],
-                                              const float (&cjk)[AT_C], float (&Sjk)[AT_C],
+                                              const float (&izjk)[AT_C],
+                                              const float (&ejk)[AT_C],
+                                              const float (&qjk)[AT_C], float (&Sjk)[AT_C],
                                               float (&Pjk)[AT_C]) {
   const int l = threadIdx.x & 7;
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -981,8 +1010,6 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
   const float4 *Ti = T + (size_t)(iok ? i : 0) * N;
   const bool lk = iok && kok && k > i;
   const float4 pik = lk ? Ti[k] : zero4;
-  const float y = pik.x, iry = pik.y, Ly = pik.z, cy = pik.w;
-  const float y2ik = iry * iry;
   float Sik = 0.f, Pik = 0.f;
   constexpr int NV = GRAD ? 2 * AT_C : AT_C;
   float v[NV];  // (i, j) sums: dE/dr^2 (GRAD) then energies
@@ -996,39 +1023,17 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
     } else {
       pij = Ti[j0 + t];
     }
-    const float x = pij.x, irx = pij.y, z = zjk[t];
-    const float ir1 = irx * (iry * irjk[t]);
-    const float ir2 = ir1 * ir1;
-    const float ir3 = ir1 * ir2;
-    const float u = x - y;
-    const float A = u + z, Bv = (x + y) - z, Cv = z - u;
-    const float AB = A * Bv;
-    const float sfac = AB * Cv;
-    const float h = 0.375f * ir2;
-    const float ang = ir3 * fmaf(sfac, h, 1.0f);
-    const float ta = sfu_exp2(pij.z + Ly + Ljk[t]);
-    const float fd = sfu_rcp(fmaf(6.0f, ta, 1.0f));
-    const float c9 = pij.w * cy * cjk[t];
-    const float cf = c9 * fd;
-    const float eu = cf * ang;  // triple energy without s9
-    Pik += eu;
-    Pjk[t] += eu;
+    const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y, pik.z, pik.w,
+                                       zjk[t], izjk[t], ejk[t], qjk[t], alp3h);
+    Pik += tr.eu;
+    Pjk[t] += tr.eu;
     if (GRAD) {
-      // U = 3/8 c9 fd r^-10, V = c9 / 2 (fd (2 r^-6 - 5 ang) + ang alp/3 fd (1 - fd))
-      const float U = cf * h * ir3;
-      const float g = fmaf(-fd, fd, fd);
-      const float V = c9 * fmaf(fd, fmaf(-2.5f, ang, ir3), ang * (alp3h * g));
-      const float AC = A * Cv, BC = Bv * Cv;
-      const float Sg = AB + AC + BC;
-      const float dex = fmaf(U, fmaf(-2.0f, AB, Sg), V * (irx * irx));
-      const float dey = fmaf(U, fmaf(-2.0f, BC, Sg), V * y2ik);
-      const float dez = fmaf(U, fmaf(-2.0f, AC, Sg), V * (irjk[t] * irjk[t]));
-      Sik += dey;
-      Sjk[t] += dez;
-      v[t] = dex;
-      v[AT_C + t] = eu;
+      Sik += tr.dey;
+      Sjk[t] += tr.dez;
+      v[t] = tr.dex;
+      v[AT_C + t] = tr.eu;
     } else {
-      v[t] = eu;
+      v[t] = tr.eu;
     }
   }
   const int rb = tri_row(i, n);
@@ -1055,16 +1060,16 @@ __device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, floa
   const int q = lane >> 3;
   const int k = kc + (lane & 7);
   const bool kok = k < n;
-  float zjk[AT_C], irjk[AT_C], Ljk[AT_C], cjk[AT_C], Sjk[AT_C], Pjk[AT_C];
+  float zjk[AT_C], izjk[AT_C], ejk[AT_C], qjk[AT_C], Sjk[AT_C], Pjk[AT_C];
 #pragma unroll
   for (int t = 0; t < AT_C; ++t) {
     const int jt = j0 + t;
     const bool ok = kok && jt < k;  // then also jt <= n - 2
     const float4 r = ok ? T[(size_t)jt * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
     zjk[t] = r.x;
-    irjk[t] = r.y;
-    Ljk[t] = r.z;
-    cjk[t] = r.w;  // 0 also zeroes every product of a (j, k) that is not a pair
+    izjk[t] = r.y;
+    ejk[t] = r.z;
+    qjk[t] = r.w;  // 0 also zeroes every product of a (j, k) that is not a pair
     Sjk[t] = 0.f;
     Pjk[t] = 0.f;
   }
@@ -1075,10 +1080,10 @@ __device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, floa
   if (j0 + AT_C <= n - 1)
     for (; ib + 3 * istep < j0; ib += st4)
       atm_tile_step<GRAD, false>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
-                                 irjk, Ljk, cjk, Sjk, Pjk);
+                                 izjk, ejk, qjk, Sjk, Pjk);
   for (; ib < jend - 1; ib += st4)
     atm_tile_step<GRAD, true>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
-                              irjk, Ljk, cjk, Sjk, Pjk);
+                              izjk, ejk, qjk, Sjk, Pjk);
   // (j, k) sums of the four groups: group q keeps values NV/4 q .. NV/4 q + NV/4 - 1
   constexpr int NV = GRAD ? 2 * AT_C : AT_C;
   float v[NV];
@@ -1462,6 +1467,7 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
   const float *W = c.w.w32 + bN;
   const bool weighted = c.weights != nullptr;
   const float cut2 = c.pf.cut3 * c.pf.cut3, alp3 = c.pf.alp3, s9 = c.pf.s9;
+  const float alp3h = 0.5f * alp3;
   float *gS = GRAD ? c.w.prS32 + bN * N : nullptr;
   float *gP = GRAD ? c.w.prP32 + bN * N : nullptr;
   const float wj = W[j];
@@ -1482,18 +1488,9 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
       const bool mik = pik.x <= cut2;
       if (mik && !later) continue;  // counted at its smallest atom
       const float4 pjk = s_rec[e];
-      const float x = pij.x, y = pik.x, z = pjk.x;
-      const float ir1 = pij.y * pjk.y * pik.y;
-      const float ir2 = ir1 * ir1;
-      const float ir3 = ir1 * ir2;
-      const float u = x - y, v = x + y;
-      const float A = u + z, Bv = v - z, Cv = z - u;
-      const float sfac = A * Bv * Cv;
-      const float ang = ir3 * fmaf(0.375f * sfac, ir2, 1.0f);
-      const float ta = sfu_exp2(pij.z + pik.z + pjk.z);
-      const float fd = __fdividef(1.0f, fmaf(6.0f, ta, 1.0f));
-      const float c9 = pij.w * pik.w * pjk.w;
-      const float eu = c9 * fd * ang;  // triple energy without s9
+      const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y, pik.z,
+                                         pik.w, pjk.x, pjk.y, pjk.z, pjk.w, alp3h);
+      const float eu = tr.eu;  // triple energy without s9
       const float wk = weighted ? W[k] : 1.f;
       float wgt;
       if (mik) {  // all sides inside: e/3 to each atom
@@ -1508,30 +1505,21 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
         wgt = (wi + wk) * (1.0f / 6.0f);
       }
       if (GRAD) {
-        const float kc9 = s9 * c9;
-        const float dfl = alp3 * fd * (1.0f - fd);
-        const float Q = 2.0f * ir3 - 5.0f * ang;
-        const float U = 0.375f * kc9 * fd * ir2 * ir3;
-        const float V = 0.5f * kc9 * fmaf(fd, Q, ang * dfl);
-        const float BC = Bv * Cv, AC = A * Cv, AB = A * Bv;
-        const float dex = fmaf(U, BC + AC - AB, V * pij.y * pij.y);
-        const float dey = fmaf(U, AC + AB - BC, V * pik.y * pik.y);
-        const float dez = fmaf(U, BC + AB - AC, V * pjk.y * pjk.y);
-        const float we = wgt * s9 * eu;
-        sij = fmaf(wgt, dex, sij);
+        const float ws = wgt * s9;
+        const float we = ws * eu;
+        sij = fmaf(ws, tr.dex, sij);
         pe += we;
-        atomicAdd(&s_S[e], wgt * dez);
+        atomicAdd(&s_S[e], ws * tr.dez);
         atomicAdd(&s_P[e], we);
-        atomicAdd(&gS[(size_t)i * N + k], wgt * dey);  // i < k: upper half
+        atomicAdd(&gS[(size_t)i * N + k], ws * tr.dey);  // i < k: upper half
         atomicAdd(&gP[(size_t)i * N + k], we);
         if (PGRAD) {
           const float4 daik = Tda[(size_t)i * N + k];
           const float4 dajk = Tda[(size_t)j * N + k];
           const float lsum = daij.z + daik.z + dajk.z;
-          const float dfd = -fd * (1.0f - fd);
           pg.s9 += wgt * eu;
-          pg.alp += wgt * s9 * c9 * ang * dfd * lsum * (1.0f / 3.0f);
-          const float dfa = wgt * s9 * c9 * ang * dfd * alp3;
+          pg.alp -= wgt * s9 * tr.qwg * lsum * (1.0f / 3.0f);
+          const float dfa = -wgt * s9 * tr.qwg * alp3;
           pg.a1 += dfa * (daij.x + daik.x + dajk.x);
           pg.a2 += dfa * (daij.y + daik.y + dajk.y);
         }
@@ -1628,8 +1616,9 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_mixed_kernel(Ctx c) {
       gy.add(2.0f * S * d.y);
       gz.add(2.0f * S * d.z);
       if (Pv != 0.f) {
-        const float cc = T[y].w;
-        const float D = Pv / (2.0f * cc * cc);
+        const float cw = T[y].w;  // sqrt(C6(q=0)) / r^3: C6(q=0) = w^2 r^6
+        const float r2 = d.x * d.x + d.y * d.y + d.z * d.z;
+        const float D = Pv / (2.0f * (cw * cw) * (r2 * r2 * r2));
         const float *A0y = c.w.A032 + a32_index(b, y, slot_x, 0, N, c.S);
 #pragma unroll
         for (int w = 0; w < NFREQ; ++w) gacc[w] = fmaf(D, A0y[(size_t)w * N], gacc[w]);
