@@ -959,16 +959,18 @@ constexpr int AT_C = 8;             // middle atoms per task (and outer atoms pe
 constexpr int AT_THREADS = 768;     // 24 warps at 80 registers (measured: 512 threads
                                     // at 128 registers, no spills, 4 % slower)
 constexpr int AT_TASKS_MAX = 900;   // tiles x chunks for n <= 237 (30 x 30)
-constexpr int AT_CTA_TRIPLES = 600000;
+// Triples per CTA: 600000 for batches of 512 structures and more (measured
+// best for batch512: 300000 -> 4 % slower, 1200000 -> 2x slower from the
+// largest CTAs), fewer for smaller batches so that they still fill the GPU.
+__device__ __forceinline__ int atm_tiled_ctas(int n, int B) {
+  const long long per = B >= 512 ? 600000 : (B <= 64 ? 75000 : 600000LL * B / 512);
+  const long long work = (long long)n * n * n / 6;
+  const int K = (int)((work + per - 1) / per);
+  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
+}
 
 __host__ __device__ inline size_t atm_tiled_smem_bytes(int N) {
   return atm_smem_bytes(N) + sizeof(int) * AT_TASKS_MAX;
-}
-
-__device__ __forceinline__ int atm_tiled_ctas(int n) {
-  const long long work = (long long)n * n * n / 6;
-  const int K = (int)((work + AT_CTA_TRIPLES - 1) / AT_CTA_TRIPLES);
-  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
 }
 
 // tri_u(i, x, n) = tri_row(i, n) + x for x > i
@@ -1115,7 +1117,7 @@ __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
   const int N = c.N;
   const int n = c.w.n_eff[b];
   if (n < 3) return;
-  const int K = atm_tiled_ctas(n);
+  const int K = atm_tiled_ctas(n, c.B);
   if (cta >= K) return;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   const int nwarps = blockDim.x >> 5;
