@@ -90,7 +90,15 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
   const int quad = warp & 3, half = warp >> 2;
   const int row = quad * 32 + lane;  // tensor-memory lane of this thread
-  const int i = i0 + row;
+  // A tile of m <= 64 (32) atoms holds each atom in 2 (4) rows of the MMA's
+  // 128, so that 4 (8) threads share an atom's partners instead of 2 and no
+  // lane idles: copies of MR = 128 / D rows, thread column group cg of 2 D
+  // (warp-uniform: a copy spans whole lane quadrants)
+  const int mt = n - i0;  // atoms of the tile (if fewer than TC_M; <= 0: padding only)
+  const int D = (mt <= 0 || mt > 64) ? 1 : (mt <= 32 ? 4 : 2);
+  const int MR = TC_M / D;
+  const int cg = half * D + row / MR;
+  const int i = i0 + row % MR;
   const size_t bN = (size_t)b * N;
   const size_t ai = bN + i;
   const int zi = (i < n) ? c.w.z[ai] : 0;
@@ -103,7 +111,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   const int ch0 = (int)((long long)blockIdx.z * nch / nsplit);
   const int ch1 = (int)((long long)(blockIdx.z + 1) * nch / nsplit);
   if (nsplit > 1 && (i0 >= n || ch0 >= ch1)) return;
-  if (i0 >= n) {  // a tile of padding only
+  if (i0 >= n) {  // a tile of padding only (D = 1)
     if (half == 0 && i < N) {
       c.out.d_energy[ai] = 0.0;
       if (GRAD) {
@@ -115,6 +123,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
     }
     return;
   }
+  if (nsplit == 1)  // atoms i0 + MR .. i0 + 127 of a duplicated tile: padding
+    for (int a = MR + tid; a < TC_M && i0 + a < N; a += TC_THREADS) {
+      const size_t ap = bN + i0 + a;
+      c.out.d_energy[ap] = 0.0;
+      if (GRAD) {
+        c.out.d_gradient[3 * ap] = 0.0;
+        c.out.d_gradient[3 * ap + 1] = 0.0;
+        c.out.d_gradient[3 * ap + 2] = 0.0;
+        for (int w = 0; w < NFREQ; ++w) c.w.G32[ap * NFREQ + w] = 0.f;
+      }
+    }
   const uint32_t mbar = tc::smem_u32(&S.mbar);
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(&S.tmem), TC_COLS);
   if (tid == 0) tc::mbar_init(mbar, 1);
@@ -125,7 +144,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   __shared__ int s_ea[2][TC_M];
   {
     const int m = tid / TC_M, r = tid % TC_M;  // 256 threads: one per (matrix, row)
-    const int ii = i0 + r;
+    const int ii = i0 + r % MR;
     const float *src = m == 0 ? A32 : A032;
     float mx = 0.f;
     if (ii < n && c.w.z[bN + ii] != 0)
@@ -138,7 +157,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   for (int t = tid; t < 2 * TC_M * TC_K; t += TC_THREADS) {
     const int m = t / (TC_M * TC_K), rk = t % (TC_M * TC_K);
     const int r = rk % TC_M, k = rk / TC_M;
-    const int ii = i0 + r;
+    const int ii = i0 + r % MR;
     float v = 0.f;
     if (k < NFREQ && ii < n && c.w.z[bN + ii] != 0)
       v = (m == 0 ? A32 : A032)[(size_t)k * N + ii];
@@ -245,9 +264,13 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
       break;
     }
     tc::fence_after_sync();
+    // this thread's columns: ncol = 16 / D from cbeg, in blocks of 8 (D = 4:
+    // half of one block)
+    const int ncol = 16 / D, cbeg = cg * ncol;
 #pragma unroll 1
-    for (int u = 0; u < 2; ++u) {
-      const int c0 = 16 * half + 8 * u;
+    for (int u = 0; u < (ncol + 7) / 8; ++u) {
+      const int c0 = (cbeg + 8 * u) & ~7;
+      const int qlo = cbeg + 8 * u - c0, qhi = qlo + (ncol < 8 ? ncol : 8);
       float c6v[8], c60v[8];
 #pragma unroll
       for (int m = 0; m < 2; ++m) {
@@ -273,7 +296,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         const int r = c0 + q;
         const int j = j0 + r;
         const int zj = S.zj[r];
-        if (j >= n || j == i || zj == 0) continue;
+        if (q < qlo || q >= qhi || j >= n || j == i || zj == 0) continue;
         const float4 pj = S.pj[r];
         const float3 dv = pos_diff(pi, li, pj, S.lj[r]);
         const float dx = dv.x, dy = dv.y, dz = dv.z;
@@ -386,28 +409,31 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
     }
     return;
   }
-  // combine the two column halves of every atom (A operand area reused: the
-  // last MMA batch has completed)
+  // combine the 2 D column groups of every atom in the group-0 thread (A
+  // operand area reused: the last MMA batch has completed; (2 D - 1) x 38 x
+  // MR floats <= 8512)
   float *red = &S.a[0][0][0];
-  if (half == 1) {
+  const int ra = row % MR;
+  if (cg != 0) {
     float v[TC_NRED] = {e_acc.hi, e_acc.lo, e8_acc.hi, e8_acc.lo, gx.hi, gx.lo, gy.hi, gy.lo,
                         gz.hi,    gz.lo,    pg[0],     pg[1],     pg[2], pg[3], pg[4]};
 #pragma unroll
     for (int w = 0; w < NFREQ; ++w) v[15 + w] = gacc[w];
+    float *o = red + (size_t)(cg - 1) * TC_NRED * MR + ra;
 #pragma unroll
-    for (int k = 0; k < TC_NRED; ++k) red[k * TC_M + row] = v[k];
+    for (int k = 0; k < TC_NRED; ++k) o[k * MR] = v[k];
   }
   __syncthreads();
   if (warp == 0) {
     tc::fence_after_sync();
     tc::tmem_free(tmem, TC_COLS);
   }
-  if (half == 1) return;
-  {
-    const float *o = red + row;
+  if (cg != 0) return;
+  for (int g = 0; g < 2 * D - 1; ++g) {
+    const float *o = red + (size_t)g * TC_NRED * MR + ra;
     auto merge = [&](Acc32 &a, int k) {
-      a.add(o[k * TC_M]);
-      a.lo += o[(k + 1) * TC_M];
+      a.add(o[k * MR]);
+      a.lo += o[(k + 1) * MR];
     };
     merge(e_acc, 0);
     merge(e8_acc, 2);
@@ -415,9 +441,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
     merge(gy, 6);
     merge(gz, 8);
 #pragma unroll
-    for (int k = 0; k < 5; ++k) pg[k] += o[(10 + k) * TC_M];
+    for (int k = 0; k < 5; ++k) pg[k] += o[(10 + k) * MR];
 #pragma unroll
-    for (int w = 0; w < NFREQ; ++w) gacc[w] += o[(15 + w) * TC_M];
+    for (int w = 0; w < NFREQ; ++w) gacc[w] += o[(15 + w) * MR];
   }
   if (PGRAD) {
     float v[5];

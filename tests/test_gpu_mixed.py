@@ -284,3 +284,28 @@ def test_atm_tiles_and_per_triple_fallback_match_fp64(d4, cut3, gradient):
     assert np.abs(em.sum(-1) - ep.sum(-1)).max() <= E_TOL
     if gradient:
         assert (mixed[1] - plain[1]).abs().max().item() <= F_TOL
+
+
+def test_many_small_structures_padded_wide(d4):
+    """A batch with more tiles of 128 atoms than the GPU has SMs x 4 (one CTA
+    per tile, no partner split), small structures (tiles of <= 32 and <= 64
+    atoms hold every atom in 4 and 2 rows of the tensor-core tile) padded to
+    N = 230 (tiles of padding only): energies per atom, padding included,
+    and forces match the plain FP64 path."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    b = wl.batch_uniform(304, 700, 3, 100, wl.ELEMENTS_12, True, "t", 230)
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (b.numbers, b.positions, b.charge))
+
+    def run(precision):
+        runner, _, _ = disp._prepare(nt, pt, ct, PARAM, "d4", None, None, None, None, None,
+                                     None, None, None, precision)
+        return runner.run(pt, gradient=True)
+
+    mixed, plain = run("mixed"), run("fp64")
+    em, ep = mixed[0].cpu().numpy(), plain[0].cpu().numpy()
+    assert np.abs(em - ep).max() <= E_TOL
+    assert np.all(em[b.numbers == 0] == 0.0)
+    assert (mixed[1] - plain[1]).abs().max().item() <= F_TOL
