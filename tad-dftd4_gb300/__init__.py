@@ -11,6 +11,8 @@ name carries a hyphen).  Public API, mirroring ``tad_dftd4``:
 * ``get_properties(numbers, positions, charge=None, cutoff=None)`` -- CN,
   EEQ charges, atom-resolved C6 and static polarisabilities
 * ``dispersion_energy_gradient`` -- energies and forces in one fused call
+* ``check_status()`` -- raise a pending device error of a forward call with
+  gradients whose backward has not run (the backward raises it otherwise)
 * ``get_params(method=..., functional=..., variant=None)`` -- damping
   parameters per density functional
 """
@@ -20,7 +22,7 @@ from __future__ import annotations
 from . import _lib, tables, workloads  # noqa: F401
 from .cutoff import Cutoff
 from .damping import Damping, Param, RationalDamping, ZeroDamping
-from .disp import dftd4, dispersion_energy_gradient, get_properties
+from .disp import check_status, dftd4, dispersion_energy_gradient, get_properties
 from .model import D4Model, D4SModel
 from .parameters import DispersionMethod, get_params
 
@@ -37,6 +39,7 @@ __all__ = [
     "dftd4",
     "dispersion_energy_gradient",
     "get_properties",
+    "check_status",
     "get_params",
     "DispersionMethod",
     "__version__",

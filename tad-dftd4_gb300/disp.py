@@ -25,10 +25,50 @@ from .cutoff import (D4_CN_CUTOFF, D4_CN_EEQ_MAX, D4_K4, D4_K5, D4_K6, D4_KCN, C
 from .damping import PARAM_ORDER, Damping, Param, RationalDamping, ZeroDamping, resolve
 from .model import BaseModel, D4Model, D4SModel
 
-__all__ = ["dftd4", "dispersion_energy_gradient", "get_properties", "Runner"]
+__all__ = ["dftd4", "dispersion_energy_gradient", "get_properties", "check_status", "Runner"]
 
 _ALLOWED_MODELS = ("d3", "d4", "d4s", "d5")
 CHECK_STATUS = True
+
+# Device status words not read yet: (pinned copy, event after the copy,
+# label).  A forward call whose result feeds autograd leaves its status here
+# and its backward reads it, so the host is not held up between the forward
+# launches and the backward bookkeeping; every public call first reads the
+# words of the calls that have completed, and check_status() waits for all.
+_PENDING: list = []
+_PENDING_MAX = 64
+
+
+def _raise_status(status: int, what: str) -> None:
+    if status == 4:
+        raise ValueError("atomic number outside the element tables")
+    if status == 6:
+        raise ValueError("non-finite positions or charges")
+    _lib.check(status, what)
+
+
+def _read_token(token) -> None:
+    word, ev, what = token
+    ev.synchronize()
+    _raise_status(int(word[0]), what)
+
+
+def check_status() -> None:
+    """Wait for every call whose device status word has not been read (a
+    forward call with gradients leaves it to its backward) and raise the
+    first error among them (``ValueError`` for elements outside the tables
+    or non-finite input)."""
+    pending = list(_PENDING)
+    _PENDING.clear()
+    for token in pending:
+        _read_token(token)
+
+
+def _drain_pending() -> None:
+    """Read the status words of the pending calls that have completed (and
+    of the oldest ones beyond _PENDING_MAX), raising the first error."""
+    while _PENDING and (_PENDING[0][1].query() or len(_PENDING) > _PENDING_MAX):
+        _read_token(_PENDING.pop(0))
 
 
 def _as_tensor(x, device, dtype):
@@ -71,7 +111,7 @@ class Runner:
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
-            cn_out: bool = False, cn_eeq_out: bool = False):
+            cn_out: bool = False, cn_eeq_out: bool = False, defer_status: bool = False):
         lib = _lib.load()
         device = positions.device
         B, N = self.numbers.shape
@@ -128,13 +168,17 @@ class Runner:
             _lib.check(lib.d4_dispersion(self.tables.struct, cfg, batch, params, flags,
                                          self.n_slots, work.data_ptr(), ws_bytes, outs, stream),
                        "d4_dispersion")
-            if CHECK_STATUS:
-                status = lib.d4_read_status(work.data_ptr(), stream)
-                if status == 4:
-                    raise ValueError("atomic number outside the element tables")
-                if status == 6:
-                    raise ValueError("non-finite positions or charges")
-                _lib.check(status, "d4_dispersion (device status)")
+            self.token = None
+            if CHECK_STATUS and defer_status:  # the status word stays in the stream
+                word = torch.empty(1, dtype=torch.int32, pin_memory=True)
+                word.copy_(work[:4].view(torch.int32), non_blocking=True)
+                ev = torch.cuda.Event()
+                ev.record(torch.cuda.current_stream(device))
+                self.token = (word, ev, "d4_dispersion (device status)")
+                _PENDING.append(self.token)
+            elif CHECK_STATUS:
+                _raise_status(lib.d4_read_status(work.data_ptr(), stream),
+                              "d4_dispersion (device status)")
         if cn_eeq_out:
             return energy, grad, pgrad, qout, cnout, cnqout
         return energy, grad, pgrad, qout, cnout
@@ -146,7 +190,9 @@ class _D4Function(torch.autograd.Function):
         need_pos = ctx.needs_input_grad[0]
         need_par = ctx.needs_input_grad[1]
         energy, grad, pgrad, _, _ = runner.run(positions, gradient=need_pos or need_par,
-                                               param_grad=need_par)
+                                               param_grad=need_par,
+                                               defer_status=need_pos or need_par)
+        ctx.token = runner.token
         ctx.runner = runner
         ctx.positions = positions.detach()
         ctx.save_for_backward(grad if grad is not None else torch.empty(0),
@@ -155,6 +201,11 @@ class _D4Function(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, go):
+        for idx, token in enumerate(_PENDING):  # the forward's status word
+            if token is ctx.token:
+                del _PENDING[idx]
+                _read_token(token)
+                break
         grad, pgrad = ctx.saved_tensors
         runner: Runner = ctx.runner
         if go.numel() > 0 and all(st == 0 for st in go.stride()):
@@ -187,6 +238,7 @@ _PVEC: dict = {}
 
 def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
              cn_function, counting_function, damping_function, precision=None):
+    _drain_pending()
     device = positions.device
     dtype = positions.dtype
     charge = _as_tensor(charge, device, dtype)

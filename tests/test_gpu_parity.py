@@ -197,6 +197,27 @@ def test_bad_element_raises(d4):
         d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})
 
 
+def test_bad_element_with_gradient_raises_at_backward(d4):
+    """With positions that require gradients the forward call leaves its
+    device status word to the backward: the error surfaces from
+    autograd.grad, or from check_status() when no backward runs."""
+    dev = torch.device("cuda")
+    nt = torch.tensor([1, 104], device=dev)
+    pt = torch.tensor([[0.0, 0, 0], [0, 0, 2.0]], dtype=torch.float64, device=dev,
+                      requires_grad=True)
+    e = d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})
+    with pytest.raises(ValueError):
+        torch.autograd.grad(e.sum(), pt)
+    d4.dftd4(nt, pt, 0.0, {"a1": 0.4, "a2": 5.0})
+    with pytest.raises(ValueError):
+        d4.check_status()
+    d4.check_status()  # nothing pending any more
+    good = torch.tensor([1, 8], device=dev)
+    e = d4.dftd4(good, pt, 0.0, {"a1": 0.4, "a2": 5.0})
+    (g,) = torch.autograd.grad(e.sum(), pt)
+    assert torch.isfinite(g).all()
+
+
 def test_nonfinite_positions_raise(d4):
     dev = torch.device("cuda")
     nt = torch.tensor([1, 1], device=dev)
