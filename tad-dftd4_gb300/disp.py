@@ -163,7 +163,8 @@ class Runner:
         cfg = _lib.ModelCfg(kind=_lib.MODEL_D4S if self.model.kind == "d4s" else _lib.MODEL_D4,
                             ga=self.model.ga, gc=self.model.gc,
                             wf=self.model.wf if self.model.wf is not None else 6.0)
-        stream = torch.cuda.current_stream(device).cuda_stream
+        cur = torch.cuda.current_stream(device)
+        stream = cur.cuda_stream
         with torch.cuda.device(device):
             _lib.check(lib.d4_dispersion(self.tables.struct, cfg, batch, params, flags,
                                          self.n_slots, work.data_ptr(), ws_bytes, outs, stream),
@@ -173,7 +174,7 @@ class Runner:
                 word = torch.empty(1, dtype=torch.int32, pin_memory=True)
                 word.copy_(work[:4].view(torch.int32), non_blocking=True)
                 ev = torch.cuda.Event()
-                ev.record(torch.cuda.current_stream(device))
+                ev.record(cur)
                 self.token = (word, ev, "d4_dispersion (device status)")
                 _PENDING.append(self.token)
             elif CHECK_STATUS:
@@ -201,11 +202,6 @@ class _D4Function(torch.autograd.Function):
 
     @staticmethod
     def backward(ctx, go):
-        for idx, token in enumerate(_PENDING):  # the forward's status word
-            if token is ctx.token:
-                del _PENDING[idx]
-                _read_token(token)
-                break
         grad, pgrad = ctx.saved_tensors
         runner: Runner = ctx.runner
         if go.numel() > 0 and all(st == 0 for st in go.stride()):
@@ -229,6 +225,13 @@ class _D4Function(torch.autograd.Function):
             gpos = (w0.unsqueeze(-1) * grad).to(ctx.positions.dtype)
         if ctx.needs_input_grad[1]:
             gpar = (w0 * pgrad).sum(0)[: len(PARAM_ORDER)]
+        # the forward's status word, read after the gradient's own launches
+        # so that the GPU does not idle while the host waits for it
+        for idx, token in enumerate(_PENDING):
+            if token is ctx.token:
+                del _PENDING[idx]
+                _read_token(token)
+                break
         return gpos, gpar, None
 
 
