@@ -619,7 +619,7 @@ def run_ours(args, world, rank, local):
                 "kernel": "atm_tiled_kernel<GRAD> (FP32 arithmetic)", "bound": "fp32",
                 "achieved": achieved, "peak": fp32_peak, "unit": "TFLOP/s",
                 "frac": achieved / fp32_peak if fp32_peak else None,
-                "traffic": traffic.get("atm_mixed_batch512"),
+                "traffic": traffic.get("atm_tiled_batch512"),
                 "peak_source": "FP32 FMA-chain probe (d4_probe_fma) measured in this run; "
                                "MEASURED_PEAKS.json holds only HBM and bf16 peaks",
                 "algorithmic": f"{ATM_FLOPS_PER_TRIPLE:.0f} flop x {triples} triples per launch",
