@@ -78,3 +78,53 @@ def test_model_descriptors(d4):
         d4.D4Model(z, ref_charges="xyz")
     with pytest.raises(NotImplementedError):
         d4.D4SModel(z, wf=3.0)
+
+
+class _FakeEvent:
+    """Stands in for torch.cuda.Event: completed or not, synchronize() marks
+    it completed."""
+
+    def __init__(self, done):
+        self.done = done
+        self.waited = False
+
+    def query(self):
+        return self.done
+
+    def synchronize(self):
+        self.waited = True
+        self.done = True
+
+
+def _token(status, done):
+    return (torch.tensor([status], dtype=torch.int32), _FakeEvent(done), "test call")
+
+
+def test_deferred_status_words():
+    """The status words that forward calls with gradients leave pending:
+    a completed word is read by the next call's drain (raising its error),
+    an incomplete one stays until check_status() waits for it; errors map
+    to the same exceptions as the synchronous check."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    disp._PENDING.clear()
+    try:
+        ok_done, bad_busy = _token(0, True), _token(4, False)
+        disp._PENDING.extend([ok_done, bad_busy])
+        disp._drain_pending()  # reads the completed word, keeps the busy one
+        assert len(disp._PENDING) == 1 and disp._PENDING[0] is bad_busy
+        assert not bad_busy[1].waited
+        with pytest.raises(ValueError, match="element tables"):
+            disp.check_status()
+        assert bad_busy[1].waited and not disp._PENDING
+        disp._PENDING.append(_token(6, True))
+        with pytest.raises(ValueError, match="non-finite"):
+            disp._drain_pending()
+        # more pending words than the cap: the oldest are waited for
+        toks = [_token(0, False) for _ in range(disp._PENDING_MAX + 3)]
+        disp._PENDING.extend(toks)
+        disp._drain_pending()
+        assert len(disp._PENDING) == disp._PENDING_MAX
+        assert all(t[1].waited for t in toks[:3])
+    finally:
+        disp._PENDING.clear()
