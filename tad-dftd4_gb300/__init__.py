@@ -11,6 +11,8 @@ name carries a hyphen).  Public API, mirroring ``tad_dftd4``:
 * ``get_properties(numbers, positions, charge=None, cutoff=None)`` -- CN,
   EEQ charges, atom-resolved C6 and static polarisabilities
 * ``dispersion_energy_gradient`` -- energies and forces in one fused call
+* ``hessian`` -- second derivatives of the total energy with respect to the
+  positions (central differences of the fused analytic gradient)
 * ``check_status()`` -- raise a pending device error of a forward call with
   gradients whose backward has not run (the backward raises it otherwise)
 * ``get_params(method=..., functional=..., variant=None)`` -- damping
@@ -22,7 +24,7 @@ from __future__ import annotations
 from . import _lib, tables, workloads  # noqa: F401
 from .cutoff import Cutoff
 from .damping import Damping, Param, RationalDamping, ZeroDamping
-from .disp import check_status, dftd4, dispersion_energy_gradient, get_properties
+from .disp import check_status, dftd4, dispersion_energy_gradient, get_properties, hessian
 from .model import D4Model, D4SModel
 from .parameters import DispersionMethod, get_params
 
@@ -39,6 +41,7 @@ __all__ = [
     "dftd4",
     "dispersion_energy_gradient",
     "get_properties",
+    "hessian",
     "check_status",
     "get_params",
     "DispersionMethod",

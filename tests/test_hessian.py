@@ -1,0 +1,87 @@
+"""
+Hessian of the total dispersion energy (``hessian``): central differences of
+the analytic gradient, the scheme of the Fortran dftd4 program behind the
+reference's golden Hessians (``test/test_grad/test_hessian.py:20-28``).  The
+golden values themselves need the element tables this build lacks (see the
+parity notes), so the bar is the oracle's exact second derivatives
+(autograd through the float64 restatement) at the reference test's
+tolerance, 1e-7 (``test_hessian.py:47``).
+"""
+
+from __future__ import annotations
+
+from importlib import import_module
+
+import pytest
+import torch
+
+import oracle
+from conftest import package
+
+TOL = 1e-7
+PARAM = {"s6": 1.0, "s8": 1.62438102, "s9": 1.0, "a1": 0.40329022, "a2": 4.80537871}
+
+
+def _batch():
+    wl = package().workloads
+    b = wl.batch_uniform(305, 2, 4, 7, wl.ELEMENTS_12, True, "t", 7)
+    return tuple(torch.from_numpy(x) for x in (b.numbers, b.positions, b.charge))
+
+
+def _oracle_hessian(nt, pt, ct):
+    out = []
+    for k in range(nt.shape[0]):
+        def energy(p, k=k):
+            return oracle.dftd4(nt[k:k + 1], p[None], ct[k:k + 1], PARAM).sum()
+        out.append(torch.autograd.functional.hessian(energy, pt[k].clone()))
+    return torch.stack(out)
+
+
+def test_fd_hessian_of_a_quadratic_is_exact():
+    """E = 1/2 x^T A x per structure: central differences of A x give A."""
+    disp = import_module("tad-dftd4_gb300.disp")
+    B, N = 3, 4
+    g = torch.Generator().manual_seed(11)
+    a = torch.randn(B, 3 * N, 3 * N, generator=g, dtype=torch.float64)
+    a = a + a.transpose(1, 2)
+    nums = (torch.arange(B) + 1)[:, None].expand(B, N)  # numbers tag the structure
+    pos = torch.randn(B, N, 3, generator=g, dtype=torch.float64)
+
+    def grad_fn(n, p, c):
+        k = n[:, 0] - 1  # structure of each geometry
+        return torch.einsum("mij,mj->mi", a[k], p.reshape(-1, 3 * N)).reshape(-1, N, 3)
+
+    h = disp._fd_hessian(grad_fn, nums, pos, torch.zeros(B), 1e-3, max_structs=40)
+    assert torch.allclose(h.reshape(B, 3 * N, 3 * N), a, atol=1e-9, rtol=0)
+
+
+def test_fd_hessian_of_the_oracle_gradient_matches_autograd():
+    """The scheme and its step (1e-4 Bohr) on the oracle's own gradient
+    against its exact second derivatives: the differencing error is far
+    below the bar."""
+    disp = import_module("tad-dftd4_gb300.disp")
+    nt, pt, ct = _batch()
+
+    def grad_fn(n, p, c):
+        return oracle.dftd4_energy_and_grad(n, p, c, PARAM)[1]
+
+    h = disp._fd_hessian(grad_fn, nt, pt, ct, 1e-4)
+    assert (h - _oracle_hessian(nt, pt, ct)).abs().max().item() < 1e-8
+
+
+@pytest.mark.gpu
+def test_hessian_matches_oracle_second_derivatives():
+    if not torch.cuda.is_available():
+        pytest.skip("no CUDA device")
+    d4 = package()
+    nt, pt, ct = _batch()
+    dev = torch.device("cuda")
+    ref = _oracle_hessian(nt, pt, ct)
+    h = d4.hessian(nt.to(dev), pt.to(dev), ct.to(dev), PARAM).cpu()
+    assert h.shape == (2, 7, 3, 7, 3)
+    assert torch.allclose(h, ref, atol=TOL, rtol=TOL)
+    h1 = d4.hessian(nt[0].to(dev), pt[0].to(dev), ct[0].to(dev), PARAM).cpu()
+    assert h1.shape == (7, 3, 7, 3)
+    assert torch.allclose(h1, ref[0], atol=TOL, rtol=TOL)
+    real = nt != 0
+    assert (h[~real] == 0).all()
