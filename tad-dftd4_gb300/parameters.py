@@ -3,14 +3,24 @@ Damping parameters per density functional: ``get_params``, the drop-in for
 ``tad_dftd4.damping.parameters.get_params``
 (``damping/parameters/loader.py:61-133``).
 
-The table is the reference's own (``data/damping_params.json``, built from
-its ``d3.toml`` / ``d4.toml`` by ``data/make_params.py``) and the lookup has
-the same rules: ``functional=None`` or ``"default"`` takes the method's
-default section, otherwise the functional's section (the name is tested as
-given and looked up case-folded); the variant defaults to the method's first
-default variant; the ``doi`` entry is dropped unless ``keep_doi``; unknown
-functionals, methods or variants raise ``KeyError``.  The block is returned
-as found, without defaults merged in (``dftd4`` applies those).
+The numbers are the reference's own (``data/damping_params.json``, built from
+its ``d3.toml`` / ``d4.toml`` by ``data/make_params.py``).  Each method's file
+is turned once into a ``_MethodTable``: the method's default variants, the
+default parameter blocks, and per functional the blocks of this method (or
+``None`` when the functional has no entry for it).  A lookup is then two
+dictionary probes.  Observable behaviour is the reference's:
+
+* ``functional=None`` or ``"default"`` selects the default blocks, and the
+  variant must be one of the method's default variants -- so a missing
+  ``variant`` is an error there, as in the reference;
+* a functional name must appear in the file exactly as given, and its
+  blocks are then taken under the case-folded name;
+* ``variant=None`` with a functional means the method's first default
+  variant;
+* the ``doi`` entry is dropped unless ``keep_doi``; the block is returned as
+  stored, without defaults merged in (``dftd4`` applies those);
+* failures raise ``KeyError`` with the reference's messages, an unknown
+  method ``ValueError``, a method without a file ``FileNotFoundError``.
 """
 
 from __future__ import annotations
@@ -35,12 +45,45 @@ class DispersionMethod(str, Enum):
     d5 = "d5"
 
 
+class _MethodTable:
+    """The parameter file of one dispersion method, indexed for lookups."""
+
+    def __init__(self, method: str, raw: dict):
+        self.method = method
+        defaults = raw.get("default", {})
+        self.default_variants: tuple = tuple(defaults.get(method, ()))
+        self.default_blocks: dict = defaults.get("parameter", {}).get(method, {})
+        self.functionals: dict = {name: entry.get(method)
+                                  for name, entry in raw.get("parameter", {}).items()}
+
+    def blocks(self, functional: str | None, variant: str | None) -> tuple[dict, str]:
+        """The variant blocks that apply and the variant to take from them."""
+        m = self.method
+        if functional is None or functional == "default":
+            if variant not in self.default_variants:
+                raise KeyError(f"Variant '{variant}' not found in default parameters for "
+                               f"method={m!r}.")
+            return self.default_blocks, variant
+        if functional not in self.functionals:
+            raise KeyError(f"Functional '{functional!r}' not found in damping parameters.")
+        folded = functional.casefold()
+        if folded not in self.functionals:
+            raise KeyError(folded)
+        blocks = self.functionals[folded]
+        if blocks is None:
+            raise KeyError(f"Method '{DispersionMethod(m)}' not found in damping parameters "
+                           f"for '{functional!r}'.")
+        if variant is None:
+            variant = self.default_variants[0]
+        return blocks, variant
+
+
 @lru_cache(maxsize=None)
-def _load(method: DispersionMethod) -> dict:
-    tables = json.loads(PARAMS_PATH.read_text())["tables"]
-    if method.value not in tables:
+def _load(method: DispersionMethod) -> _MethodTable:
+    files = json.loads(PARAMS_PATH.read_text())["tables"]
+    if method.value not in files:
         raise FileNotFoundError(f"parameter table for method {method.value!r} missing")
-    return tables[method.value]
+    return _MethodTable(method.value, files[method.value])
 
 
 def get_params(*, method: DispersionMethod | str, functional: str | None,
@@ -48,28 +91,9 @@ def get_params(*, method: DispersionMethod | str, functional: str | None,
     """Damping parameters of ``functional`` for ``method`` (and ``variant``)."""
     method = DispersionMethod(method)
     table = _load(method)
-    if functional in (None, "default"):
-        default_section = table["default"]
-        variant_section = default_section[method.value]
-        if variant not in variant_section:
-            raise KeyError(f"Variant '{variant}' not found in default parameters for "
-                           f"method={method.value!r}.")
-        disp_method_section = default_section["parameter"]
-    else:
-        func_section = table["parameter"]
-        if functional not in func_section:
-            raise KeyError(f"Functional '{functional!r}' not found in damping parameters.")
-        disp_method_section = func_section[functional.casefold()]
-        if method.value not in disp_method_section:
-            raise KeyError(f"Method '{method}' not found in damping parameters for "
-                           f"'{functional!r}'.")
-    if variant is None:
-        variant = table["default"][method.value][0]
-    variant_section = disp_method_section[method.value]
-    if variant not in variant_section:
+    blocks, variant = table.blocks(functional, variant)
+    block = blocks.get(variant)
+    if block is None:
         raise KeyError(f"Variant '{variant}' not found for functional={functional!r}, "
                        f"method={method.value!r}.")
-    out = dict(variant_section[variant])
-    if not keep_doi:
-        out.pop("doi", None)
-    return out  # a Param mapping
+    return {k: v for k, v in block.items() if keep_doi or k != "doi"}

@@ -63,6 +63,28 @@ def test_errors():
 def test_method_missing_in_functional():
     table = {"default": {"d4": ["bj-eeq-atm"]}, "parameter": {"pbe": {"reference": {}}}}
     mod = params_module()
-    with patch.object(mod, "_load", return_value=table):
+    with patch.object(mod, "_load", return_value=mod._MethodTable("d4", table)):
         with pytest.raises(KeyError, match="Method"):
             mod.get_params(method="d4", functional="pbe", variant="bj-eeq-atm")
+
+
+def test_every_lookup_matches_the_reference_loader():
+    """Every functional / variant of the reference's d3.toml and d4.toml, and
+    the failing lookups, give what the reference's own get_params returned
+    (tests/golden/params_golden.json, made by make_params_golden.py)."""
+    import json
+    from pathlib import Path
+
+    calls = json.loads((Path(__file__).parent / "golden" / "params_golden.json").read_text())
+    gp = package().get_params
+    assert len(calls) > 700
+    for call in calls:
+        kw = {k: call[k] for k in ("method", "functional", "variant", "keep_doi")}
+        want = call["result"]
+        if "ok" in want:
+            assert gp(**kw) == want["ok"], kw
+        else:
+            with pytest.raises(KeyError) as info:
+                gp(**kw)
+            assert want["error"] == "KeyError", kw
+            assert str(info.value) == want["message"], (kw, str(info.value))
