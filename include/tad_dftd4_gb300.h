@@ -42,7 +42,7 @@
 extern "C" {
 #endif
 
-#define D4_ABI_VERSION 1
+#define D4_ABI_VERSION 2
 #define D4_NREF 7   /* reference systems per element (reference/d4/params.py) */
 #define D4_NFREQ 23 /* imaginary frequencies of the Casimir-Polder grid (utils.py:52-80) */
 
@@ -65,7 +65,25 @@ typedef enum d4_model_kind { D4_MODEL_D4 = 0, D4_MODEL_D4S = 1 } d4_model_kind;
 #define D4_FLAG_GRADIENT 1u    /* also compute dE/dR (d_gradient must be set) */
 #define D4_FLAG_CHARGES_IN 2u  /* use batch->d_charges_in instead of the EEQ solve */
 #define D4_FLAG_MIXED 4u       /* precision form: FP32 pair/triple maths, FP64 sums */
-#define D4_FLAG_PARAM_GRAD 8u  /* also compute dE/d(s6, s8, s10, a1, a2, s9, alp) */
+#define D4_FLAG_PARAM_GRAD 8u  /* also compute the parameter gradient (d_param_grad) */
+#define D4_FLAG_EXACT_C9 16u   /* ATM with exact C9 = (3/pi) sum_w w a_i a_j a_k
+                                  (D4ATMExact, dispersion/threebody.py:276-302,
+                                  dispersion/d4.py:67-84) instead of
+                                  sqrt(C6 C6 C6); plain FP64 method only */
+
+/* Entries per structure of d_param_grad: dE_b / d(s6, s8, s10, a1, a2, s9,
+   alp, rs6, rs8, bet), then two unused entries. */
+#define D4_PARAM_GRAD_STRIDE 12
+
+/* Two-body damping functions (damping/functions.py).  RATIONAL is the
+   Becke-Johnson damping dftd4() uses; the others are the D3-family damping
+   functions a caller can pass as ``damping_function`` (plain FP64 method). */
+typedef enum d4_damping_kind {
+  D4_DAMP_RATIONAL = 0, /* 1 / (r^n + (a1 sqrt(3 r4r2_i r4r2_j) + a2)^n), 262-305 */
+  D4_DAMP_ZERO = 1,     /* f / r^n, f = 1 / (1 + 6 (rs_n r / rvdw)^alp_n), 308-378 */
+  D4_DAMP_MZERO = 2,    /* f / r^n, f = 1 / (1 + 6 (r / (rs_n rvdw) + bet rvdw)^-alp_n), 381-434 */
+  D4_DAMP_OP = 3        /* r^bet / (r^n (r^bet + R0^bet)), 437-484 */
+} d4_damping_kind;
 
 /*
  * Element tables, device pointers.  Row 0 is the dummy element.  The first
@@ -111,6 +129,11 @@ typedef struct d4_params {
   double cut_cn_eeq; /* EEQ CN cutoff (25) */
   double cn_eeq_max; /* smooth EEQ CN cap (8) */
   double kcn, k4, k5, k6; /* CN counting constants (defaults.py:41-50) */
+  /* two-body damping (added in ABI version 2; zero-initialised = rational) */
+  int32_t damping;   /* d4_damping_kind */
+  int32_t reserved;
+  double rs6, rs8;   /* zero / modified-zero damping radius scalings */
+  double bet;        /* modified-zero / optimised-power damping exponent */
 } d4_params_t;
 
 /* A zero-padded batch (device pointers). */
@@ -124,6 +147,8 @@ typedef struct d4_batch {
   const double *d_r4r2_in;    /* [B][N] per-atom r4r2 values, or NULL for the table */
   const double *d_energy_weights; /* [B][N] weights w of the differentiated quantity
                                      sum_i w_i E_i, or NULL for all ones */
+  const double *d_rvdw_in; /* [B][N][N] pairwise van der Waals radii, required by the
+                              zero and modified-zero damping (ABI version 2) */
 } d4_batch_t;
 
 /* Outputs (device pointers; optional ones may be NULL). */
@@ -132,7 +157,7 @@ typedef struct d4_outputs {
   double *d_gradient; /* [B][N][3] dE/dR, written with D4_FLAG_GRADIENT */
   double *d_charges;  /* [B][N] EEQ charges (optional) */
   double *d_cn;       /* [B][N] D4 coordination numbers (optional) */
-  double *d_param_grad; /* [B][8] dE_b/d(s6,s8,s10,a1,a2,s9,alp,-), D4_FLAG_PARAM_GRAD */
+  double *d_param_grad; /* [B][D4_PARAM_GRAD_STRIDE], D4_FLAG_PARAM_GRAD */
   double *d_cn_eeq;   /* [B][N] capped EEQ coordination numbers (optional) */
 } d4_outputs_t;
 

@@ -31,6 +31,8 @@ __all__ = [
     "c6_d4",
     "c6_d4s",
     "dispersion2",
+    "weighted_pols",
+    "c9_exact",
     "atm_dispersion",
     "dftd4",
     "dftd4_energy_and_grad",
@@ -396,6 +398,32 @@ def _param(param: Mapping, key: str, dtype) -> torch.Tensor:
     return torch.as_tensor(val, dtype=dtype)
 
 
+def _damp_d3(kind: str, order: int, r, rvdw, radius_r4r2, param, dtype):
+    """D3-family two-body damping t_n = f_n / r^n, ``damping/functions.py``:
+    zero 329-378 (argument rs * r / rvdw, exponent alp, alp + 2 for n = 8),
+    modified zero 381-434 (r / (rs rvdw) + bet rvdw, exponent -alp_n),
+    optimised power 437-484 (r^bet / (r^bet r^n + R0^bet r^n), as written
+    there)."""
+    alp = _param(param, "alp", dtype)
+    if kind == "zero":
+        rs = torch.as_tensor(param["rs6" if order == 6 else "rs8"], dtype=dtype)
+        alp_n = alp if order == 6 else alp + 2.0
+        t = rs * r / rvdw
+        return (1.0 / (1.0 + 6.0 * t**alp_n)) / r**order
+    if kind == "mzero":
+        rs = torch.as_tensor(param["rs6" if order == 6 else "rs8"], dtype=dtype)
+        bet = torch.as_tensor(param["bet"], dtype=dtype)
+        alp_n = alp if order == 6 else alp + 2.0
+        t = r / (rs * rvdw) + bet * rvdw
+        return (1.0 / (1.0 + 6.0 * t ** (-alp_n))) / r**order
+    if kind == "op":
+        bet = torch.as_tensor(param["bet"], dtype=dtype)
+        ab = radius_r4r2**bet
+        rb = r**bet
+        return rb / (rb * r**order + ab * r**order)
+    raise ValueError(kind)
+
+
 def dispersion2(
     numbers: torch.Tensor,
     positions: torch.Tensor,
@@ -403,38 +431,74 @@ def dispersion2(
     c6: torch.Tensor,
     r4r2: torch.Tensor,
     cutoff: float = DEFAULTS["disp2"],
+    damping: str = "rational",
+    rvdw: torch.Tensor | None = None,
 ) -> torch.Tensor:
-    """BJ-damped two-body energy, ``dispersion/twobody.py:89-201`` with
-    ``damping/functions.py:116-169, 262-305``."""
+    """Damped two-body energy, ``dispersion/twobody.py:89-201`` with
+    ``damping/functions.py:116-169`` (gating) and the damping function:
+    rational 262-305 (default) or the D3 family (``_damp_d3``).  The
+    dipole-quadrupole order is evaluated unless both s8 and rs8 are missing
+    and is scaled by s8 (default 1)."""
     dtype = positions.dtype
-    for key in ("a1", "a2"):
-        if param.get(key) is None:
-            raise TypeError(f"RationalDamping (order 6) requires keyword(s): {key}")
+    if damping in ("rational", "op"):
+        for key in ("a1", "a2"):
+            if param.get(key) is None:
+                raise TypeError(f"RationalDamping (order 6) requires keyword(s): {key}")
     mask = _real_pairs(numbers)
     r = _distances(positions, mask)
     qq = 3.0 * r4r2.unsqueeze(-1) * r4r2.unsqueeze(-2)
-    a1 = torch.as_tensor(param["a1"], dtype=dtype)
-    a2 = torch.as_tensor(param["a2"], dtype=dtype)
-    radius = a1 * torch.sqrt(qq) + a2
+    radius = None
+    if damping in ("rational", "op"):
+        a1 = torch.as_tensor(param["a1"], dtype=dtype)
+        a2 = torch.as_tensor(param["a2"], dtype=dtype)
+        radius = a1 * torch.sqrt(qq) + a2
+    rv = None
+    if damping in ("zero", "mzero"):
+        rv = torch.where(mask, rvdw.to(dtype), torch.ones_like(r))
     inside = mask & (r <= cutoff)
     zero = torch.zeros_like(r)
 
     def damp(order):
-        return torch.where(inside, 1.0 / (r**order + radius**order), zero)
+        if damping == "rational":
+            return torch.where(inside, 1.0 / (r**order + radius**order), zero)
+        return torch.where(inside, _damp_d3(damping, order, r, rv, radius, param, dtype), zero)
 
     s6 = _param(param, "s6", dtype)
     e6 = torch.sum(c6 * damp(6), dim=-1)
     edisp = s6 * e6
-    if param.get("s8") is not None:
-        s8 = torch.as_tensor(param["s8"], dtype=dtype)
+    if param.get("s8") is not None or param.get("rs8") is not None:
+        s8 = _param(param, "s8", dtype)
         edisp = edisp + s8 * torch.sum(c6 * qq * damp(8), dim=-1)
     if "s10" in param:
+        if damping != "rational":
+            raise ValueError(f"{damping} damping has no order 10")
         c10 = c6 * qq * qq * 49.0 / 40.0
         if param["s10"] is not None:
             edisp = edisp + torch.as_tensor(param["s10"], dtype=dtype) * torch.sum(
                 c10 * damp(10), dim=-1
             )
     return -0.5 * edisp
+
+
+def weighted_pols(numbers: torch.Tensor, gw: torch.Tensor, alpha: torch.Tensor,
+                  model: str) -> torch.Tensor:
+    """Weighted polarisabilities a_i(w): D4 ``model/d4.py:291-307``
+    (sum_r gw_ir alpha_irw); D4S ``model/d4s.py:292-316`` (the pair weights
+    gw[m, n, r] contracted with alpha[n, r, w] over n and r, divided by the
+    number of real atoms)."""
+    if model == "d4":
+        return torch.einsum("...nr,...nrw->...nw", gw, alpha)
+    # per structure: the reference divides by a (B, 1) count, which only
+    # broadcasts for a single structure; (B, 1, 1) gives every structure its own
+    nat = _real_atoms(numbers).sum(-1, keepdim=True).unsqueeze(-1).to(alpha.dtype)
+    return torch.einsum("...mnr,...nrw->...mw", gw, alpha) / nat
+
+
+def c9_exact(aiw: torch.Tensor, tables: OracleTables) -> torch.Tensor:
+    """C9_ijk = (3/pi) sum_w w_w a_i a_j a_k (``threebody.py:276-302`` with
+    ``utils.py:155-205``)."""
+    w = tables.freq_weights.to(aiw.dtype)
+    return THOPI * torch.einsum("...iw,...jw,...kw,w->...ijk", aiw, aiw, aiw, w)
 
 
 def atm_dispersion(
@@ -444,17 +508,25 @@ def atm_dispersion(
     c6_0: torch.Tensor,
     r4r2: torch.Tensor,
     cutoff: float = DEFAULTS["disp3"],
+    c9: torch.Tensor | None = None,
+    absolute: bool = False,
 ) -> torch.Tensor:
     """
-    ATM three-body energy with C9 = sqrt|C6 C6 C6| and BJ radii,
-    ``dispersion/threebody.py:54-163, 210-256, 311-321``; zero damping of
-    order 9 with the (r0, r1) argument order of ``threebody.py:133-145``.
+    ATM three-body energy with C9 = sqrt|C6 C6 C6| (or the given exact
+    ``c9``) and BJ radii, ``dispersion/threebody.py:54-163, 210-256,
+    311-321``; zero damping of order 9 with the (r0, r1) argument order of
+    ``threebody.py:133-145``.  ``absolute``: sum the magnitudes of the
+    triple terms instead (the scale of each atom's rounding error).
     """
     dtype = positions.dtype
     s9 = _param(param, "s9", dtype)
     # threebody.py:93-94 converts alp to the positions' dtype before /3.
     alp_third = _param(param, "alp", dtype) / 3.0
-    a1 = _param(param, "a1", dtype)
+    # RadiiBJMixin (threebody.py:250-253) falls back to torch.tensor(A1) in
+    # the term's own dtype, which is torch's default (float32): a missing a1
+    # is float32(0.4) = 0.4000000059604645 (a2 = 5 is exact either way)
+    a1 = torch.as_tensor(param["a1"] if param.get("a1") is not None
+                         else float(np.float32(DEFAULTS["a1"])), dtype=dtype)
     a2 = _param(param, "a2", dtype)
     mask_p = _real_pairs(numbers)
     mask_t = _real_triples(numbers)
@@ -480,10 +552,16 @@ def atm_dispersion(
     inside = mask_t & (r2ij <= cut2) & (r2jk <= cut2)
     ang = torch.where(inside, 0.375 * s / r5 + 1.0 / r3, torch.zeros_like(r2))
 
-    prod = c6_0.unsqueeze(-1) * c6_0.unsqueeze(-2) * c6_0.unsqueeze(-3)
-    prod = torch.abs(prod)
-    c9 = torch.where(mask_t & (prod > 0), torch.sqrt(torch.where(prod > 0, prod, one)), 0.0)
+    if c9 is None:
+        prod = c6_0.unsqueeze(-1) * c6_0.unsqueeze(-2) * c6_0.unsqueeze(-3)
+        prod = torch.abs(prod)
+        c9 = torch.where(mask_t & (prod > 0), torch.sqrt(torch.where(prod > 0, prod, one)),
+                         0.0)
+    else:
+        c9 = torch.where(mask_t, c9, torch.zeros_like(c9))
     energy = ang * fdamp * s9 * c9
+    if absolute:
+        energy = energy.abs()
     return torch.sum(energy, dim=(-2, -1)) / 6.0
 
 
@@ -499,10 +577,15 @@ def dftd4(
     cutoff: Mapping | None = None,
     ref_charges: str = "eeq",
     return_parts: bool = False,
+    damping: str = "rational",
+    rvdw: torch.Tensor | None = None,
+    exact_c9: bool = False,
 ):
     """
     Atom-resolved D4 energy, the whole ``disp.py:44-146`` path:
-    CN -> EEQ -> weights -> C6 -> BJ two-body + ATM(q = 0).
+    CN -> EEQ -> weights -> C6 -> two-body (``damping``: rational, zero,
+    mzero or op; ``rvdw`` the pair radii of the zero family) + ATM(q = 0),
+    with the exact C9 of ``DispD4Exact`` when ``exact_c9``.
     """
     tables = tables or load_tables()
     dtype = positions.dtype
@@ -527,11 +610,17 @@ def dftd4(
         c6_0 = c6_d4s(gw0, alpha, tables)
     else:
         raise ValueError(f"Unknown model '{model}'")
-    e2 = dispersion2(numbers, positions, param, c6, r4r2, cutoff=cut["disp2"])
-    e3 = atm_dispersion(numbers, positions, param, c6_0, r4r2, cutoff=cut["disp3"])
+    e2 = dispersion2(numbers, positions, param, c6, r4r2, cutoff=cut["disp2"],
+                     damping=damping, rvdw=rvdw)
+    c9 = c9_exact(weighted_pols(numbers, gw0, alpha, model), tables) if exact_c9 else None
+    e3 = atm_dispersion(numbers, positions, param, c6_0, r4r2, cutoff=cut["disp3"], c9=c9)
     energy = e2 + e3
     if return_parts:
-        return energy, {"cn": cn, "q": q, "c6": c6, "c6_0": c6_0, "e2": e2, "e3": e3}
+        with torch.no_grad():
+            e3_abs = atm_dispersion(numbers, positions, param, c6_0, r4r2, cutoff=cut["disp3"],
+                                    c9=c9, absolute=True)
+        return energy, {"cn": cn, "q": q, "c6": c6, "c6_0": c6_0, "e2": e2, "e3": e3,
+                        "scale": e2.abs() + e3_abs}
     return energy
 
 

@@ -14,7 +14,7 @@ from pathlib import Path
 
 from . import _build
 
-ABI_VERSION = 1
+ABI_VERSION = 2
 NREF = 7
 NFREQ = 23
 
@@ -38,6 +38,13 @@ FLAG_GRADIENT = 1
 FLAG_CHARGES_IN = 2
 FLAG_MIXED = 4
 FLAG_PARAM_GRAD = 8
+FLAG_EXACT_C9 = 16
+PARAM_GRAD_STRIDE = 12  # D4_PARAM_GRAD_STRIDE: s6 s8 s10 a1 a2 s9 alp rs6 rs8 bet - -
+
+DAMP_RATIONAL = 0
+DAMP_ZERO = 1
+DAMP_MZERO = 2
+DAMP_OP = 3
 STATUS_OFFSET = 0  # D4_STATUS_OFFSET: byte offset of the device status word in a workspace
 
 
@@ -87,6 +94,11 @@ class Params(ctypes.Structure):
         ("k4", c_double),
         ("k5", c_double),
         ("k6", c_double),
+        ("damping", c_int32),
+        ("reserved", c_int32),
+        ("rs6", c_double),
+        ("rs8", c_double),
+        ("bet", c_double),
     ]
 
 
@@ -100,6 +112,7 @@ class Batch(ctypes.Structure):
         ("d_charges_in", c_void_p),
         ("d_r4r2_in", c_void_p),
         ("d_energy_weights", c_void_p),
+        ("d_rvdw_in", c_void_p),
     ]
 
 

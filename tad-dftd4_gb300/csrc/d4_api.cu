@@ -81,6 +81,16 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   if (cfg->kind != D4_MODEL_D4 && cfg->kind != D4_MODEL_D4S) return D4_ERR_ARGUMENT;
   if (cfg->kind == D4_MODEL_D4S && !tables->wfpair) return D4_ERR_ARGUMENT;
   if (cfg->kind == D4_MODEL_D4 && n_slots != 1) return D4_ERR_ARGUMENT;
+  // D3-family two-body damping and exact C9 run on the plain FP64 kernels;
+  // the zero and modified-zero damping need the pairwise radii; no
+  // quadrupole-quadrupole (s10) term beside them (damping/functions.py:352-356)
+  const int damp = params->damping;
+  if (damp < D4_DAMP_RATIONAL || damp > D4_DAMP_OP) return D4_ERR_ARGUMENT;
+  if ((flags & D4_FLAG_MIXED) && (damp != D4_DAMP_RATIONAL || (flags & D4_FLAG_EXACT_C9)))
+    return D4_ERR_ARGUMENT;
+  if ((damp == D4_DAMP_ZERO || damp == D4_DAMP_MZERO) && !batch->d_rvdw_in)
+    return D4_ERR_ARGUMENT;
+  if (damp != D4_DAMP_RATIONAL && params->has_s10) return D4_ERR_ARGUMENT;
   d4::Workspace w = d4::carve_workspace(d_workspace, batch->n_struct, batch->n_pad, n_slots,
                                         flags);
   if (workspace_bytes < w.bytes) return D4_ERR_WORKSPACE;
@@ -94,6 +104,7 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   c.charges_in = batch->d_charges_in;
   c.r4r2_in = batch->d_r4r2_in;
   c.weights = batch->d_energy_weights;
+  c.rvdw_in = batch->d_rvdw_in;
   c.B = batch->n_struct;
   c.N = batch->n_pad;
   c.S = n_slots;

@@ -450,11 +450,11 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) v[k] = warp_sumf(pg[k]);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * (double)v[0]);
-      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * (double)v[1]);
-      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * (double)v[2]);
-      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)v[3]);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)v[4]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 0], 0.5 * (double)v[0]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 1], 0.5 * (double)v[1]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 2], 0.5 * (double)v[2]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], (double)v[3]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], (double)v[4]);
     }
   }
   if (i >= N) return;

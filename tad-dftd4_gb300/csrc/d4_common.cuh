@@ -84,7 +84,7 @@ struct Workspace {
   double *dEdq;     // [B*N]
   double *dEdcnq;   // [B*N] dE/d(raw EEQ CN)
   double *e3;       // [B*N] ATM energy (accumulated atomically)
-  double *pgrad;    // [B*8] parameter gradients (atomics)
+  double *pgrad;    // [B*D4_PARAM_GRAD_STRIDE] parameter gradients (atomics)
   double *A;        // [B*N*S*23] weighted polarisabilities at q
   double *A0;       // [B*N*S*23] at q = 0
   double *dA_dcn;   // [B*N*S*23]
@@ -100,6 +100,11 @@ struct Workspace {
   double *pr_P;     // [B*N*N] sum of weighted triple energies (atomics)
   double *pr_da1;   // [B*N*N] d log R0 / d a1 (parameter gradients only)
   double *pr_da2;   // [B*N*N] d log R0 / d a2 (parameter gradients only)
+  // exact C9 (D4_FLAG_EXACT_C9, FP64 method only)
+  double *ax;       // [B*N*23] polarisabilities a_i(iw) of the exact C9
+  double *gax;      // [B*N*23] dE/da_i(iw)
+  double *gbar;     // [B*S*23] D4S: slot sums of dE/da over the structure's atoms / nat
+  double *f3x;      // [B*N*3] ATM part of dE/dR
   double *eeq_L;    // [B*N*(N+1)/2] packed Cholesky factor (FP64 method) or
                     // packed FP64 EEQ matrix (precision form)
   float4 *pos32;    // [B*N] positions relative to the structure's first slot, FP32,
@@ -190,7 +195,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   w.dEdq = (double *)take(8 * BN);
   w.dEdcnq = (double *)take(8 * BN);
   w.e3 = (double *)take(8 * BN);
-  w.pgrad = (double *)take(8 * 8 * B);
+  w.pgrad = (double *)take(8 * (size_t)D4_PARAM_GRAD_STRIDE * B);
   w.A = mixed ? nullptr : (double *)take(8 * BNS23);
   w.A0 = mixed ? nullptr : (double *)take(8 * BNS23);
   w.dA_dcn = (grad && !mixed) ? (double *)take(8 * BNS23) : nullptr;
@@ -207,6 +212,11 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   const bool pgrad = (flags & D4_FLAG_PARAM_GRAD) != 0;
   w.pr_da1 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
   w.pr_da2 = (pgrad && !mixed) ? (double *)take(8 * BNN) : nullptr;
+  const bool exact = (flags & D4_FLAG_EXACT_C9) != 0 && !mixed;
+  w.ax = exact ? (double *)take(8 * BN * NFREQ) : nullptr;
+  w.gax = (exact && grad) ? (double *)take(8 * BN * NFREQ) : nullptr;
+  w.gbar = (exact && grad) ? (double *)take(8 * (size_t)B * S * NFREQ) : nullptr;
+  w.f3x = (exact && grad) ? (double *)take(8 * BN * 3) : nullptr;
   w.eeq_L = mixed ? nullptr : (double *)take(8 * (size_t)B * ((size_t)N * (N + 1) / 2));
   w.pos32 = (float4 *)take(16 * BN);
   w.aux32 = (float4 *)take(16 * BN);
@@ -284,6 +294,7 @@ struct Ctx {
   const double *charges_in;
   const double *r4r2_in;
   const double *weights;
+  const double *rvdw_in;  // [B*N*N] pairwise radii of the zero / modified-zero damping
   int B, N, S;
   uint32_t flags;
   Workspace w;

@@ -116,7 +116,7 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
     }
     if (threadIdx.x == 0 && c.w.n_real) c.w.n_real[b] = base;
   }
-  if (threadIdx.x < 8) c.w.pgrad[b * 8 + threadIdx.x] = 0.0;
+  if (threadIdx.x < D4_PARAM_GRAD_STRIDE) c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + threadIdx.x] = 0.0;
   if (b == 0 && threadIdx.x < NFREQ)
     c.w.fw32[threadIdx.x] = (float)(THOPI * c.tab.freq_weights[threadIdx.x]);
   if (c.w.pr_S && c.N <= PREP_ZERO_MAX_N) {
@@ -567,6 +567,55 @@ __global__ void __launch_bounds__(256) weights_kernel(Ctx c) {
 
 // ---------------------------------------------------------------- pairs
 
+// One order n of a D3-family two-body damping (damping/functions.py:308-484):
+// t = f_n / r^n and its derivatives with respect to r and to the damping
+// parameters.  ``rv`` is the pair's van der Waals radius (zero and
+// modified-zero damping), ``R0`` = a1 sqrt(3 r4r2_i r4r2_j) + a2 (optimised
+// power), ``rs`` the order's radius scaling, ``pw`` its exponent (alp for
+// n = 6, alp + 2 for n = 8; bet for the optimised power).
+struct DampD3 {
+  double t, dr, dR0, drs, dalp, dbet;
+};
+
+__device__ __forceinline__ DampD3 damp_d3(int kind, int n, double r, double R0, double rv,
+                                          double rs, double pw, double bet) {
+  DampD3 d{0.0, 0.0, 0.0, 0.0, 0.0, 0.0};
+  double rn = r * r;
+  rn = rn * rn * rn;
+  if (n == 8) rn *= r * r;
+  if (kind == D4_DAMP_ZERO) {
+    // f = 1 / (1 + 6 u^p), u = rs r / rv (the reference's argument order)
+    const double u = rs * r / rv;
+    const double up = pow(u, pw);
+    const double f = 1.0 / (1.0 + 6.0 * up);
+    d.t = f / rn;
+    const double dfdu = -6.0 * f * f * (u > 0.0 ? pw * up / u : 0.0);
+    d.dr = dfdu * (rs / rv) / rn - n * d.t / r;
+    d.drs = dfdu * (r / rv) / rn;
+    d.dalp = u > 0.0 ? -6.0 * f * f * up * log(u) / rn : 0.0;
+  } else if (kind == D4_DAMP_MZERO) {
+    // f = 1 / (1 + 6 u^-p), u = r / (rs rv) + bet rv
+    const double u = r / (rs * rv) + bet * rv;
+    const double um = pow(u, -pw);
+    const double f = 1.0 / (1.0 + 6.0 * um);
+    d.t = f / rn;
+    const double dfdu = 6.0 * pw * um / u * f * f;
+    d.dr = dfdu / (rs * rv) / rn - n * d.t / r;
+    d.drs = -dfdu * r / (rs * rs * rv) / rn;
+    d.dbet = dfdu * rv / rn;
+    d.dalp = 6.0 * um * log(u) * f * f / rn;
+  } else {  // D4_DAMP_OP: r^bet / (r^bet r^n + R0^bet r^n) = 1 / (r^n (1 + (R0/r)^bet))
+    const double x = R0 / r;
+    const double v = pow(x, bet);
+    const double h = 1.0 / (1.0 + v);
+    d.t = h / rn;
+    d.dr = d.t / r * (bet * v * h - n);
+    d.dR0 = -d.t * bet * v * h / R0;
+    d.dbet = -d.t * v * h * log(x);
+  }
+  return d;
+}
+
 // Fused C6 + rational (BJ) two-body energy, its direct gradient and its C6
 // adjoint, and the per-pair tables the ATM kernel consumes.  One warp per
 // atom i; lanes over partners j.  C6 is never stored.
@@ -604,7 +653,9 @@ __global__ void __launch_bounds__(256) pair_fwd_kernel(Ctx c) {
   const int slot_i = c.w.slot[ai];
   const double *fw = c.tab.freq_weights;
   double e_acc = 0.0, gx = 0.0, gy = 0.0, gz = 0.0;
-  double pg[5] = {0, 0, 0, 0, 0};  // s6, s8, s10, a1, a2
+  // s6, s8, s10, a1, a2, -, alp, rs6, rs8, bet (slots of d_param_grad)
+  double pg[10] = {0, 0, 0, 0, 0, 0, 0, 0, 0, 0};
+  const double *rvdw_row = c.rvdw_in ? c.rvdw_in + ai * N : nullptr;
   for (int s = 0; s < nslot; ++s) {
     if (lane < NFREQ) {
       const size_t o = (ai * c.S + s) * NFREQ + lane;
@@ -642,7 +693,51 @@ __global__ void __launch_bounds__(256) pair_fwd_kernel(Ctx c) {
         c.w.pr_da1[pij] = sqq / R0;
         c.w.pr_da2[pij] = 1.0 / R0;
       }
-      if (r <= p.cut_disp2) {
+      if (r <= p.cut_disp2 && p.damping != D4_DAMP_RATIONAL) {
+        // D3-family damping: e = s6 c6 t6 + s8 c8 t8 (dispersion2,
+        // dispersion/twobody.py:147-182), derivatives of -e as below
+        const double rv = rvdw_row ? rvdw_row[j] : 0.0;
+        const bool zero_kind = p.damping != D4_DAMP_OP;
+        const DampD3 d6 = damp_d3(p.damping, 6, r, R0, rv, p.rs6,
+                                  zero_kind ? p.alp : p.bet, p.bet);
+        double e = p.s6 * c6 * d6.t;
+        double dEdr = -p.s6 * c6 * d6.dr;
+        double K = -p.s6 * d6.t;
+        double gR0 = -p.s6 * c6 * d6.dR0, grs6 = -p.s6 * c6 * d6.drs, grs8 = 0.0;
+        double galp = -p.s6 * c6 * d6.dalp, gbet = -p.s6 * c6 * d6.dbet;
+        pg[0] += -wi * c6 * d6.t;
+        if (p.has_s8) {
+          const double c8 = c6 * qq;
+          const DampD3 d8 = damp_d3(p.damping, 8, r, R0, rv, p.rs8,
+                                    zero_kind ? p.alp + 2.0 : p.bet, p.bet);
+          e += p.s8 * c8 * d8.t;
+          dEdr += -p.s8 * c8 * d8.dr;
+          K += -p.s8 * qq * d8.t;
+          gR0 += -p.s8 * c8 * d8.dR0;
+          grs8 += -p.s8 * c8 * d8.drs;
+          galp += -p.s8 * c8 * d8.dalp;
+          gbet += -p.s8 * c8 * d8.dbet;
+          pg[1] += -wi * c8 * d8.t;
+        }
+        e_acc += -0.5 * e;
+        const double phi = 0.5 * (wi + atom_weight(c, aj));
+        dEdr *= phi;
+        K *= phi;
+        pg[3] += wi * 0.5 * gR0 * sqq;
+        pg[4] += wi * 0.5 * gR0;
+        pg[6] += wi * 0.5 * galp;
+        pg[7] += wi * 0.5 * grs6;
+        pg[8] += wi * 0.5 * grs8;
+        pg[9] += wi * 0.5 * gbet;
+        const double f = dEdr / r;
+        gx += f * dx;
+        gy += f * dy;
+        gz += f * dz;
+        if (grad) {
+#pragma unroll
+          for (int w = 0; w < NFREQ; ++w) gacc[w] += K * Aj[w];
+        }
+      } else if (r <= p.cut_disp2) {
         const double r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R02 * R02 * R02;
         const double t6 = 1.0 / (r6 + R06);
         double e = p.s6 * c6 * t6;
@@ -707,14 +802,20 @@ __global__ void __launch_bounds__(256) pair_fwd_kernel(Ctx c) {
   gy = warp_sum(gy);
   gz = warp_sum(gz);
   if (c.flags & D4_FLAG_PARAM_GRAD) {
+    const int npg = p.damping != D4_DAMP_RATIONAL ? 10 : 5;
 #pragma unroll
-    for (int k = 0; k < 5; ++k) pg[k] = warp_sum(pg[k]);
+    for (int k = 0; k < 10; ++k)
+      if (k < npg) pg[k] = warp_sum(pg[k]);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * pg[0]);
-      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * pg[1]);
-      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * pg[2]);
-      atomicAdd(&c.w.pgrad[b * 8 + 3], pg[3]);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], pg[4]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 0], 0.5 * pg[0]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 1], 0.5 * pg[1]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 2], 0.5 * pg[2]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], pg[3]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], pg[4]);
+      if (npg > 5) {
+#pragma unroll
+        for (int k = 6; k < 10; ++k) atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + k], pg[k]);
+      }
     }
   }
   if (lane == 0) {
@@ -885,10 +986,10 @@ __global__ void __launch_bounds__(256) atm_kernel(Ctx c) {
     g_a1 = warp_sum(g_a1);
     g_a2 = warp_sum(g_a2);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 3], g_a1);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], g_a2);
-      atomicAdd(&c.w.pgrad[b * 8 + 5], g_s9);
-      atomicAdd(&c.w.pgrad[b * 8 + 6], g_alp);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], g_a1);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], g_a2);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 5], g_s9);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 6], g_alp);
     }
   }
   __syncthreads();
@@ -954,7 +1055,13 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_kernel(Ctx c) {
 #pragma unroll
     for (int w = 0; w < NFREQ; ++w) {
       const double g = warp_sum(gacc[w]);
-      if (lane == w) c.w.G0[(ax * c.S + s) * NFREQ + w] = THOPI * fw[w] * g;
+      if (lane == w) {
+        double g0 = THOPI * fw[w] * g;
+        if (c.w.gax)  // exact C9: the adjoint of a_x (D4) or of the slot averages (D4S)
+          g0 += c.cfg.kind == D4_MODEL_D4S ? c.w.gbar[((size_t)b * c.S + s) * NFREQ + w]
+                                           : c.w.gax[ax * NFREQ + w];
+        c.w.G0[(ax * c.S + s) * NFREQ + w] = g0;
+      }
     }
   }
   if (lane < NFREQ)
@@ -962,6 +1069,11 @@ __global__ void __launch_bounds__(256) pair_atm_bwd_kernel(Ctx c) {
   gx = warp_sum(gx);
   gy = warp_sum(gy);
   gz = warp_sum(gz);
+  if (c.w.f3x) {  // exact C9: the ATM force of atom x from its own warp
+    gx += c.w.f3x[3 * ax];
+    gy += c.w.f3x[3 * ax + 1];
+    gz += c.w.f3x[3 * ax + 2];
+  }
   __syncwarp();
   // chain rule to CN and q
   double dcn = 0.0, dq = 0.0;
@@ -1059,7 +1171,7 @@ __global__ void charges_in_kernel(Ctx c) {
 // s9 / alp / ATM radii from atm_kernel.
 __global__ void param_grad_finish_kernel(Ctx c) {
   const int t = blockIdx.x * blockDim.x + threadIdx.x;
-  if (t < 8 * c.B) c.out.d_param_grad[t] = c.w.pgrad[t];
+  if (t < D4_PARAM_GRAD_STRIDE * c.B) c.out.d_param_grad[t] = c.w.pgrad[t];
 }
 
 // ---------------------------------------------------------------- alpha
@@ -1130,7 +1242,9 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   stage_end(ST_PAIR_FWD, st);
   const dim3 tiles(((N + 7) / 8) * ((N + 31) / 32), B);
   stage_begin(ST_ATM, st);
-  if (grad) {
+  if (c.flags & D4_FLAG_EXACT_C9) {
+    launch_atm_exact(c, st);
+  } else if (grad) {
     if (c.flags & D4_FLAG_PARAM_GRAD)
       atm_kernel<true, true><<<tiles, 256, 0, st>>>(c);
     else
@@ -1158,7 +1272,7 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   const size_t total = (size_t)B * N;
   finish_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
   if (c.flags & D4_FLAG_PARAM_GRAD)
-    param_grad_finish_kernel<<<(8 * B + 255) / 256, 256, 0, st>>>(c);
+    param_grad_finish_kernel<<<(D4_PARAM_GRAD_STRIDE * B + 255) / 256, 256, 0, st>>>(c);
   stage_end(ST_FINISH, st);
   return 0;
 }
@@ -1255,7 +1369,7 @@ void launch_finish(const Ctx &c, cudaStream_t st) {
   const size_t total = (size_t)c.B * c.N;
   finish_kernel<<<(unsigned)((total + 255) / 256), 256, 0, st>>>(c);
   if (c.flags & D4_FLAG_PARAM_GRAD)
-    param_grad_finish_kernel<<<(8 * c.B + 255) / 256, 256, 0, st>>>(c);
+    param_grad_finish_kernel<<<(D4_PARAM_GRAD_STRIDE * c.B + 255) / 256, 256, 0, st>>>(c);
 }
 
 int launch_prepare_alpha(const d4_tables_t &tab, const d4_model_cfg_t &cfg,

@@ -30,6 +30,7 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint);
 void launch_pair_fwd_tc(const Ctx &c, cudaStream_t st);  // D4, precision form (d4_c6tc.cu)
 bool pair_atm_bwd_tc_ok(const Ctx &c);
 void launch_pair_atm_bwd_tc(const Ctx &c, cudaStream_t st);
+void launch_atm_exact(const Ctx &c, cudaStream_t st);  // exact C9, FP64 (d4_exact.cu)
 int launch_properties(const Ctx &c, double *c6out, double *alpha_out, double *q_out,
                       cudaStream_t st);
 

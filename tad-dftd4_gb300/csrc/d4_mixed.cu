@@ -478,11 +478,11 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
 #pragma unroll
     for (int k = 0; k < 5; ++k) v[k] = warp_sumf(pg[k]);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 0], 0.5 * (double)v[0]);
-      atomicAdd(&c.w.pgrad[b * 8 + 1], 0.5 * (double)v[1]);
-      atomicAdd(&c.w.pgrad[b * 8 + 2], 0.5 * (double)v[2]);
-      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)v[3]);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)v[4]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 0], 0.5 * (double)v[0]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 1], 0.5 * (double)v[1]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 2], 0.5 * (double)v[2]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], (double)v[3]);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], (double)v[4]);
     }
   }
   if (GRAD) {
@@ -902,10 +902,10 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
     pg.a1 = warp_sumf(pg.a1);
     pg.a2 = warp_sumf(pg.a2);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)pg.a1);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)pg.a2);
-      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)pg.s9);
-      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)pg.alp);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], (double)pg.a1);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], (double)pg.a2);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 5], (double)pg.s9);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 6], (double)pg.alp);
     }
   }
   if (SMEM) {
@@ -1546,10 +1546,10 @@ __global__ void __launch_bounds__(ATM_SPARSE_THREADS, 2) atm_sparse_kernel(Ctx c
     pg.a1 = warp_sumf(pg.a1);
     pg.a2 = warp_sumf(pg.a2);
     if (lane == 0) {
-      atomicAdd(&c.w.pgrad[b * 8 + 3], (double)pg.a1);
-      atomicAdd(&c.w.pgrad[b * 8 + 4], (double)pg.a2);
-      atomicAdd(&c.w.pgrad[b * 8 + 5], (double)pg.s9);
-      atomicAdd(&c.w.pgrad[b * 8 + 6], (double)pg.alp);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 3], (double)pg.a1);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 4], (double)pg.a2);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 5], (double)pg.s9);
+      atomicAdd(&c.w.pgrad[b * D4_PARAM_GRAD_STRIDE + 6], (double)pg.alp);
     }
   }
   Ej = warp_sumf(Ej);

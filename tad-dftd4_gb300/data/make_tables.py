@@ -33,7 +33,10 @@ them in: they are uploaded once per device from this file.  Two groups exist.
    ``eeq_rad``.  Those packages are not part of the reference source tree.
    Pass ``--external FILE.npz`` holding these eight arrays (length >= 104,
    row 0 = dummy) dumped from an installation of those packages to get the
-   physical values.  Without it, deterministic PLACEHOLDER values are written
+   physical values (the file may also hold ``vdw_pairwise`` (>= 104 x 104),
+   tad-mctc's pairwise van der Waals radii, which the zero-damping family of
+   two-body damping functions takes; without it those callers pass ``rvdw``).
+   Without it, deterministic PLACEHOLDER values are written
    and ``provenance`` says so for each of them.  Placeholders make every
    kernel and every parity test meaningful (GPU and oracle see the same
    inputs), but energies then differ from a real tad-dftd4 installation.
@@ -144,6 +147,13 @@ def build(src: Path, external: Path | None = None) -> dict[str, np.ndarray]:
     prov = {k: "tad-dftd4 source" for k in tables}
     if external is not None:
         ext = np.load(external)
+        if "vdw_pairwise" in ext.files:  # optional: the zero-damping family's radii
+            vdw = np.asarray(ext["vdw_pairwise"], dtype=np.float64)
+            full = np.zeros((N_ELEM, N_ELEM))
+            m = min(vdw.shape[0], N_ELEM)
+            full[:m, :m] = vdw[:m, :m]
+            tables["vdw_pairwise"] = full
+            prov["vdw_pairwise"] = f"external: {external.name}"
         for key in EXTERNAL_KEYS:
             arr = np.asarray(ext[key])
             full = np.zeros(N_ELEM, dtype=np.int64 if key == "zeff" else np.float64)

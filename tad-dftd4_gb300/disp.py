@@ -22,7 +22,8 @@ import torch
 
 from . import _lib, tables as _tables
 from .cutoff import (D4_CN_CUTOFF, D4_CN_EEQ_MAX, D4_K4, D4_K5, D4_K6, D4_KCN, Cutoff)
-from .damping import PARAM_ORDER, Damping, Param, RationalDamping, ZeroDamping, resolve
+from .damping import (PARAM_ORDER, Damping, MZeroDamping, OptimisedPowerDamping, Param,
+                      RationalDamping, ZeroDamping, resolve)
 from .model import BaseModel, D4Model, D4SModel
 
 __all__ = ["dftd4", "dispersion_energy_gradient", "get_properties", "hessian", "check_status",
@@ -40,18 +41,21 @@ _PENDING: list = []
 _PENDING_MAX = 64
 
 
-def _raise_status(status: int, what: str) -> None:
+def _raise_status(status: int, what: str, origin: str = "") -> None:
     if status == 4:
-        raise ValueError("atomic number outside the element tables")
+        raise ValueError("atomic number outside the element tables" + origin)
     if status == 6:
-        raise ValueError("non-finite positions or charges")
-    _lib.check(status, what)
+        raise ValueError("non-finite positions or charges" + origin)
+    _lib.check(status, what + origin)
 
 
 def _read_token(token) -> None:
     word, ev, what = token
     ev.synchronize()
-    _raise_status(int(word[0]), what)
+    _raise_status(int(word[0]), "d4_dispersion (device status)", f" [raised for {what}]")
+
+
+_CALLS = [0]  # public calls with deferred status so far (labels their errors)
 
 
 def check_status() -> None:
@@ -109,6 +113,8 @@ class Runner:
     r4r2: torch.Tensor | None = None
     n_slots: int = 1
     mixed: bool = False
+    rvdw: torch.Tensor | None = None  # (B, N, N) pair radii of rvdw-type damping
+    exact_c9: bool = False            # ATM with the exact C9 (DispD4Exact)
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
@@ -126,10 +132,12 @@ class Runner:
             flags |= _lib.FLAG_CHARGES_IN
         if self.mixed:
             flags |= _lib.FLAG_MIXED
+        if self.exact_c9:
+            flags |= _lib.FLAG_EXACT_C9
         energy = torch.empty((B, N), dtype=torch.float64, device=device)
         grad = (torch.empty((B, N, 3), dtype=torch.float64, device=device)
                 if flags & _lib.FLAG_GRADIENT else None)
-        pgrad = (torch.empty((B, 8), dtype=torch.float64, device=device)
+        pgrad = (torch.empty((B, _lib.PARAM_GRAD_STRIDE), dtype=torch.float64, device=device)
                  if param_grad else None)
         qout = torch.empty((B, N), dtype=torch.float64, device=device) if charges_out else None
         cnout = torch.empty((B, N), dtype=torch.float64, device=device) if cn_out else None
@@ -145,6 +153,7 @@ class Runner:
             cut_disp2=self.cut["disp2"], cut_disp3=self.cut["disp3"],
             cut_cn=self.cut["cn"], cut_cn_eeq=self.cut["cn_eeq"],
             cn_eeq_max=D4_CN_EEQ_MAX, kcn=D4_KCN, k4=D4_K4, k5=D4_K5, k6=D4_K6,
+            damping=p["damping"], rs6=p["rs6"], rs8=p["rs8"], bet=p["bet"],
         )
         batch = _lib.Batch(
             n_struct=B, n_pad=N, d_numbers=self.numbers.data_ptr(), d_positions=pos.data_ptr(),
@@ -152,6 +161,7 @@ class Runner:
             d_charges_in=self.q.data_ptr() if self.q is not None else None,
             d_r4r2_in=self.r4r2.data_ptr() if self.r4r2 is not None else None,
             d_energy_weights=w.data_ptr() if w is not None else None,
+            d_rvdw_in=self.rvdw.data_ptr() if self.rvdw is not None else None,
         )
         outs = _lib.Outputs(
             d_energy=energy.data_ptr(),
@@ -176,7 +186,9 @@ class Runner:
                 word.copy_(work[:4].view(torch.int32), non_blocking=True)
                 ev = torch.cuda.Event()
                 ev.record(cur)
-                self.token = (word, ev, "d4_dispersion (device status)")
+                _CALLS[0] += 1
+                self.token = (word, ev, f"forward call #{_CALLS[0]} with gradients "
+                                        f"({B} structures x {N} atoms)")
                 _PENDING.append(self.token)
             elif CHECK_STATUS:
                 _raise_status(lib.d4_read_status(work.data_ptr(), stream),
@@ -236,12 +248,39 @@ class _D4Function(torch.autograd.Function):
         return gpos, gpar, None
 
 
+def _named(fn, name: str) -> bool:
+    """True for ``None`` (the default) or a function called ``name``: the
+    reference's defaults ``tad_mctc.ncoord.cn_d4`` / ``erf_count`` passed
+    explicitly select the built-in D4 coordination number."""
+    return fn is None or getattr(fn, "__name__", None) == name
+
+
 PRECISIONS = ("fp64", "mixed")
 _PVEC: dict = {}
 
 
+_DAMPING_BY_NAME = {cls.__name__: cls for cls in
+                    (RationalDamping, ZeroDamping, MZeroDamping, OptimisedPowerDamping)}
+
+
+def _damping(fn) -> Damping:
+    """The two-body damping selected by ``damping_function``: this package's
+    classes, or tad-dftd4's own instances matched by class name."""
+    if fn is None:
+        return RationalDamping()
+    if isinstance(fn, Damping) and fn.kind >= 0:
+        return fn
+    cls = _DAMPING_BY_NAME.get(type(fn).__name__)
+    if cls is None:
+        raise NotImplementedError(
+            f"damping function {type(fn).__name__} is not built in (rational, zero, "
+            "modified-zero and optimised-power damping are)")
+    return cls()
+
+
 def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
-             cn_function, counting_function, damping_function, precision=None):
+             cn_function, counting_function, damping_function, precision=None,
+             exact_c9: bool = False):
     _drain_pending()
     device = positions.device
     dtype = positions.dtype
@@ -267,18 +306,19 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
     if q is not None and numbers.shape != q.shape:
         raise ValueError(f"Shape of atomic charges ({q.shape}) is not consistent with "
                          f"atomic numbers ({numbers.shape}).")
-    if cn_function is not None or counting_function is not None:
+    if not (_named(cn_function, "cn_d4") and _named(counting_function, "erf_count")):
         raise NotImplementedError(
             "only the default D4 coordination number (cn_d4 with erf_count) is built in")
-    if damping_function is not None and not isinstance(damping_function, RationalDamping):
-        if isinstance(damping_function, Damping) and damping_function.radius_type != "r4r2":
-            raise ValueError("`rvdw` radius type is not used by the two-body term of dftd4")
-        raise NotImplementedError("only rational (BJ) damping is built in for dftd4")
-    resolved = resolve(param)
+    damp = _damping(damping_function)
+    resolved = resolve(param, damp)
+    plain_only = damp.kind != RationalDamping.kind or exact_c9
     if precision is None:
-        precision = "mixed" if dtype == torch.float32 else "fp64"
+        precision = "mixed" if dtype == torch.float32 and not plain_only else "fp64"
     if precision not in PRECISIONS:
         raise ValueError(f"precision must be one of {PRECISIONS}, got {precision!r}")
+    if precision == "mixed" and plain_only:
+        raise ValueError("the precision form runs the rational damping with the approximate "
+                         "C9; other damping functions and the exact C9 use precision='fp64'")
     if device.type != "cuda":
         raise RuntimeError("tad-dftd4_gb300 runs on CUDA devices; move the inputs to a GPU")
 
@@ -303,11 +343,20 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
         "disp2": cut_host["disp2"], "disp3": cut_host["disp3"],
         "cn": D4_CN_CUTOFF, "cn_eeq": cut_host["cn_eeq"],
     }
+    rv = None
+    if damp.radius_type == "rvdw":
+        if rvdw is None:
+            rvdw = _tables.vdw_pairwise(device, nums)
+        if rvdw is None:
+            raise ValueError(
+                "`rvdw` must be provided for `rvdw` radius type: the pairwise van der Waals "
+                "radii (tad-mctc's VDW_PAIRWISE) are not in the element table file")
+        rv = rvdw.reshape(B, N, N).to(device=device, dtype=torch.float64).contiguous()
     runner = Runner(
         numbers=nums, charge=chg, tables=tab, model=mdl, params=resolved, cut=cut,
         q=None if q is None else q.reshape(-1, N).to(torch.float64).contiguous(),
         r4r2=None if r4r2 is None else r4r2.reshape(-1, N).to(torch.float64).contiguous(),
-        n_slots=n_slots, mixed=precision == "mixed",
+        n_slots=n_slots, mixed=precision == "mixed", rvdw=rv, exact_c9=exact_c9,
     )
     if any(isinstance(param.get(k), torch.Tensor) for k in PARAM_ORDER):
         pvec = []
@@ -341,8 +390,15 @@ def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, 
     with 0 for padding, ``positions`` (..., N, 3) in Bohr on a CUDA device,
     total ``charge`` (scalar or per structure), damping parameters ``param``.
     Returns (..., N) energies in Hartree with the dtype of ``positions``.
-    ``cn_function`` / ``counting_function`` / ``damping_function`` accept
-    only the defaults (D4 CN with erf counting, rational damping).
+    ``cn_function`` / ``counting_function`` accept the defaults (the D4 CN
+    with erf counting, given as ``None`` or as tad-mctc's ``cn_d4`` /
+    ``erf_count``).  ``damping_function`` selects the two-body damping:
+    ``RationalDamping`` (default), ``ZeroDamping``, ``MZeroDamping`` or
+    ``OptimisedPowerDamping`` (this package's classes or tad-dftd4's own
+    instances); the zero-damping family takes the pairwise radii ``rvdw``
+    (..., N, N), which must be passed unless the table file carries them.
+    The damping functions other than the rational one run on the plain FP64
+    kernels whatever the dtype.
 
     ``precision`` (an addition to the reference signature): ``"fp64"`` runs
     the plain method in double precision (default for float64 positions);
@@ -350,9 +406,20 @@ def dftd4(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param, 
     compensated sums, FP32 EEQ factorisation refined in FP64, FP64 CN,
     weights and final reductions (default for float32 positions).
     """
+    return _evaluate(numbers, positions, charge, param, model=model, rcov=rcov, r4r2=r4r2,
+                     rvdw=rvdw, q=q, cutoff=cutoff, cn_function=cn_function,
+                     counting_function=counting_function, damping_function=damping_function,
+                     precision=precision)
+
+
+def _evaluate(numbers, positions, charge, param, *, model, rcov, r4r2, rvdw, q, cutoff,
+              cn_function, counting_function, damping_function, precision,
+              exact_c9: bool = False) -> torch.Tensor:
+    """The library call behind ``dftd4`` and the ``Disp`` classes: energies
+    with gradients through the hand-written adjoint."""
     runner, pvec, shape = _prepare(numbers, positions, charge, param, model, rcov, r4r2,
                                    rvdw, q, cutoff, cn_function, counting_function,
-                                   damping_function, precision)
+                                   damping_function, precision, exact_c9)
     pos = positions.reshape(-1, shape[-1], 3)
     energy = _D4Function.apply(pos, pvec, runner)
     return energy.reshape(shape)
@@ -366,8 +433,10 @@ def dispersion_energy_gradient(numbers, positions, charge, param, **kw):
     runner, _, shape = _prepare(numbers, positions, charge, param, kw.pop("model", "d4"),
                                 kw.pop("rcov", None), kw.pop("r4r2", None),
                                 kw.pop("rvdw", None), kw.pop("q", None),
-                                kw.pop("cutoff", None), None, None, None,
-                                kw.pop("precision", None))
+                                kw.pop("cutoff", None), kw.pop("cn_function", None),
+                                kw.pop("counting_function", None),
+                                kw.pop("damping_function", None),
+                                kw.pop("precision", None), kw.pop("exact_c9", False))
     if kw:
         raise TypeError(f"unexpected arguments {sorted(kw)}")
     pos = positions.reshape(-1, shape[-1], 3)
@@ -379,27 +448,41 @@ def dispersion_energy_gradient(numbers, positions, charge, param, **kw):
 def _fd_hessian(grad_fn, numbers: torch.Tensor, positions: torch.Tensor,
                 charge: torch.Tensor, step: float, max_structs: int = 4096) -> torch.Tensor:
     """Central differences of a batched gradient: ``grad_fn(numbers (M, N),
-    positions (M, N, 3), charge (M,))`` -> (M, N, 3).  Every structure's 6N
-    displaced geometries (+-step along each coordinate) go into one call (at
-    most ``max_structs`` geometries per call).  Returns the symmetrised
-    (B, N, 3, N, 3) second derivatives in float64."""
+    positions (M, N, 3), charge (M,), source (M,))`` -> (M, N, 3), where
+    ``source`` holds the index of the structure each geometry displaces.
+    Each structure has 2 x 3N displaced geometries (+-step along each
+    coordinate); a call takes at most ``max_structs`` of them -- several
+    structures' sets at once when they fit, else consecutive slices of one
+    structure's coordinates.  Returns the symmetrised (B, N, 3, N, 3) second
+    derivatives in float64."""
     B, N = numbers.shape
     dt = torch.float64
     dev = positions.device
     pos = positions.detach().to(dt)
     m = 3 * N
-    shift = (torch.eye(m, dtype=dt, device=dev) * step).reshape(m, N, 3)
     out = torch.empty((B, m, N, 3), dtype=dt, device=dev)
-    per = max(1, max_structs // (2 * m))
-    for b0 in range(0, B, per):
-        b1 = min(B, b0 + per)
-        nb = b1 - b0
+    cap = max(2, int(max_structs))
+    # (structure range, coordinate range) per call
+    plan = []
+    if 2 * m <= cap:
+        per = cap // (2 * m)
+        plan = [((b0, min(B, b0 + per)), (0, m)) for b0 in range(0, B, per)]
+    else:
+        rows = cap // 2
+        plan = [((b, b + 1), (k0, min(m, k0 + rows))) for b in range(B)
+                for k0 in range(0, m, rows)]
+    for (b0, b1), (k0, k1) in plan:
+        nb, nk = b1 - b0, k1 - k0
+        shift = torch.zeros((nk, m), dtype=dt, device=dev)
+        shift[torch.arange(nk, device=dev), torch.arange(k0, k1, device=dev)] = step
+        shift = shift.reshape(nk, N, 3)
         p = pos[b0:b1, None]
-        geo = torch.cat([p + shift, p - shift], dim=1).reshape(nb * 2 * m, N, 3)
-        nums = numbers[b0:b1, None].expand(nb, 2 * m, N).reshape(-1, N)
-        chg = charge[b0:b1, None].to(dt).expand(nb, 2 * m).reshape(-1)
-        g = grad_fn(nums, geo, chg).to(dt).reshape(nb, 2, m, N, 3)
-        out[b0:b1] = (g[:, 0] - g[:, 1]) / (2.0 * step)
+        geo = torch.cat([p + shift, p - shift], dim=1).reshape(nb * 2 * nk, N, 3)
+        nums = numbers[b0:b1, None].expand(nb, 2 * nk, N).reshape(-1, N)
+        chg = charge[b0:b1, None].to(dt).expand(nb, 2 * nk).reshape(-1)
+        src = torch.arange(b0, b1, device=dev)[:, None].expand(nb, 2 * nk).reshape(-1)
+        g = grad_fn(nums, geo, chg, src).to(dt).reshape(nb, 2, nk, N, 3)
+        out[b0:b1, k0:k1] = (g[:, 0] - g[:, 1]) / (2.0 * step)
     h = out.reshape(B, N, 3, N, 3)
     return 0.5 * (h + h.permute(0, 3, 4, 1, 2))
 
@@ -429,11 +512,23 @@ def hessian(numbers: torch.Tensor, positions: torch.Tensor, charge, param: Param
     if chg.numel() != B:
         raise ValueError(f"charge of shape {tuple(chg.shape)} for {B} structures")
     kw.setdefault("precision", "fp64")
+    max_structs = kw.pop("max_structs", 4096)
+    # per-atom (and per-pair) inputs follow their structure's displaced copies
+    per_atom = {}
+    for key in ("q", "rcov", "r4r2", "rvdw"):
+        v = kw.pop(key, None)
+        if v is None:
+            continue
+        if tuple(v.shape[:len(shape)]) != tuple(shape):
+            raise ValueError(f"Shape of {key} ({tuple(v.shape)}) is not consistent with "
+                             f"atomic numbers ({tuple(shape)}).")
+        per_atom[key] = v.reshape(B, *v.shape[len(shape):])
 
-    def grad_fn(n, p, c):
-        return dispersion_energy_gradient(n, p, c, param, **kw)[1]
+    def grad_fn(n, p, c, src):
+        extra = {k: v.index_select(0, src.to(v.device)) for k, v in per_atom.items()}
+        return dispersion_energy_gradient(n, p, c, param, **kw, **extra)[1]
 
-    h = _fd_hessian(grad_fn, nums, pos, chg, step)
+    h = _fd_hessian(grad_fn, nums, pos, chg, step, max_structs)
     return h.reshape(*shape, 3, N, 3).to(positions.dtype)
 
 

@@ -170,3 +170,29 @@ def device_tables(device: torch.device, ref_charges: str = "eeq", ga: float = 3.
     tab = DeviceTables(device, ref_charges, float(ga), float(gc), t, st, max_z)
     _DEVICE[key] = tab
     return tab
+
+
+_VDW: dict = {}
+
+
+def vdw_pairwise(device: torch.device, numbers: torch.Tensor,
+                 path: str | Path | None = None) -> torch.Tensor | None:
+    """
+    Pairwise van der Waals radii rvdw[b, i, j] = VDW_PAIRWISE[Z_i, Z_j] of a
+    padded batch (the radii the zero-damping family takes, tad-dftd4
+    ``dispersion/base.py:275-281``), or ``None`` when the table file holds no
+    ``vdw_pairwise`` table (that table belongs to tad-mctc; a file built by
+    ``data/make_tables.py --external`` from an installation carries it).
+    """
+    host = host_tables(path)
+    if "vdw_pairwise" not in host:
+        return None
+    device = torch.device(device)
+    key = (str(device), str(path or tables_path()))
+    tab = _VDW.get(key)
+    if tab is None:
+        tab = torch.from_numpy(np.ascontiguousarray(host["vdw_pairwise"])).to(
+            device=device, dtype=torch.float64)
+        _VDW[key] = tab
+    z = numbers.to(device=device, dtype=torch.int64).clamp(0, tab.shape[0] - 1)
+    return tab[z.unsqueeze(-1), z.unsqueeze(-2)]

@@ -15,6 +15,7 @@ if str(REPO) not in sys.path:
     sys.path.insert(0, str(REPO))
 
 GOLDEN = REPO / "tests" / "golden" / "golden.npz"
+GOLDEN_VARIANTS = REPO / "tests" / "golden" / "golden_variants.npz"
 
 
 def pytest_configure(config):
@@ -26,9 +27,9 @@ def package():
     return importlib.import_module("tad-dftd4_gb300")
 
 
-def golden_cases():
-    """List of (tag, dict of arrays, meta) from the golden fixture file."""
-    with np.load(GOLDEN) as npz:
+def golden_cases(path=GOLDEN):
+    """List of (tag, dict of arrays, meta) from a golden fixture file."""
+    with np.load(path) as npz:
         index = json.loads(str(npz["index"]))
         out = []
         for tag in index:
@@ -50,3 +51,8 @@ def assert_close(actual, expected, rtol, atol, what=""):
         f"{what}: {bad.sum()} of {bad.size} off; max abs err {err.max():.3e}, "
         f"max rel err {(err / np.maximum(np.abs(expected), 1e-300)).max():.3e}"
     )
+
+
+def golden_variant_cases():
+    """Cases of the damping-variant / exact-C9 fixture file."""
+    return golden_cases(GOLDEN_VARIANTS)

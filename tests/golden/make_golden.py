@@ -11,7 +11,7 @@ from the stand-ins (an independent restatement of the published method).
 
 Run from the repository root (needs the reference source tree)::
 
-    python tests/golden/make_golden.py --src /root/reference/src
+    python tests/golden/make_golden.py --src <reference>/src
 
 Cases: the geometries of the reference's examples (``examples/single.py``,
 ``examples/batch.py``) and NaN test (``test/test_grad/test_nan.py``), read from
@@ -34,6 +34,7 @@ import torch
 HERE = Path(__file__).resolve().parent
 REPO = HERE.parents[1]
 OUT = HERE / "golden.npz"
+OUT_VARIANTS = HERE / "golden_variants.npz"
 
 
 def _setup(src: Path):
@@ -125,6 +126,86 @@ def seeded_cases(workloads) -> list[dict]:
 DEFAULT_PARAM = {"s6": 1.0, "s8": 1.2, "s9": 1.0, "a1": 0.40, "a2": 5.0}
 
 
+def pair_radii(numbers: np.ndarray) -> np.ndarray:
+    """Deterministic pairwise radii for the zero-damping family (the
+    reference's VDW_PAIRWISE table lives in tad-mctc, absent here, so the
+    fixtures pass ``rvdw`` explicitly): 2.8 + 0.35 (sqrt Z_i + sqrt Z_j)
+    Bohr, symmetric, positive also for padding."""
+    z = np.sqrt(numbers.astype(np.float64))
+    return 2.8 + 0.35 * (z[..., :, None] + z[..., None, :])
+
+
+def variant_cases(workloads) -> list[dict]:
+    """D3-family two-body damping (damping/functions.py:308-484) and the
+    exact-C9 method DispD4Exact (dispersion/d4.py:71-84)."""
+    cases = []
+    b = workloads.single32(8)
+    cases.append({"name": "zero_damping", "numbers": b.numbers, "positions": b.positions,
+                  "charge": b.charge, "damping": "zero", "rvdw": pair_radii(b.numbers),
+                  "param": {"s6": 1.0, "s8": 0.9, "rs6": 1.2, "rs8": 1.0, "alp": 14.0,
+                            "s9": 1.0}})
+    b = workloads.batch_uniform(13, 3, 8, 24, workloads.ELEMENTS_12, True, "v3", 24)
+    cases.append({"name": "mzero_damping_batch", "numbers": b.numbers,
+                  "positions": b.positions, "charge": b.charge, "damping": "mzero",
+                  "rvdw": pair_radii(b.numbers),
+                  "param": {"s6": 1.0, "s8": 0.8, "rs6": 1.1, "rs8": 1.0, "alp": 14.0,
+                            "bet": 0.3, "a1": 0.45, "a2": 4.5, "s9": 1.0}})
+    b = workloads.single32(9)
+    cases.append({"name": "op_damping", "numbers": b.numbers, "positions": b.positions,
+                  "charge": np.array([-1.0]), "damping": "op",
+                  "param": {"s6": 1.0, "s8": 0.7, "a1": 0.5, "a2": 3.0, "bet": 2.0,
+                            "s9": 1.0}})
+    b = workloads.single32(10)
+    cases.append({"name": "zero_damping_short_cutoffs", "numbers": b.numbers,
+                  "positions": b.positions, "charge": b.charge, "damping": "zero",
+                  "rvdw": pair_radii(b.numbers), "cutoff": {"disp2": 9.0, "disp3": 6.0},
+                  "param": {"s6": 0.9, "rs6": 1.3, "rs8": 1.1, "alp": 16.0, "s9": 1.0}})
+    b = workloads.single32(11)
+    cases.append({"name": "exact_c9", "numbers": b.numbers, "positions": b.positions,
+                  "charge": b.charge, "exact_c9": True})
+    b = workloads.batch_uniform(14, 3, 6, 20, workloads.ELEMENTS_12, True, "x3", 20)
+    # D4S is left out here: the reference's D4S get_weighted_pols divides a
+    # (B, N, 23) tensor by a (B, 1) atom count (model/d4s.py:313-316), which
+    # does not broadcast for batches, so it has no batched D4S result
+    cases.append({"name": "exact_c9_batch_short_cutoff", "numbers": b.numbers,
+                  "positions": b.positions, "charge": b.charge, "exact_c9": True,
+                  "cutoff": {"disp3": 7.0}, "models": ("d4",),
+                  "param": {"s6": 1.0, "s8": 1.1, "a1": 0.42, "a2": 4.8, "s9": 1.2,
+                            "alp": 15.0}})
+    return cases
+
+
+def run_variant(d4, case: dict, model_key: str) -> dict[str, np.ndarray]:
+    from tad_dftd4.damping import (MZeroDamping, OptimisedPowerDamping, RationalDamping,
+                                   ZeroDamping)
+    from tad_dftd4.dispersion.d4 import DispD4Exact
+
+    dd = {"device": torch.device("cpu"), "dtype": torch.float64}
+    numbers = torch.tensor(case["numbers"])
+    positions = torch.tensor(case["positions"], **dd)
+    charge = torch.tensor(case["charge"], **dd)
+    pdict = case.get("param", DEFAULT_PARAM)
+    param = {k: torch.tensor(v, **dd, requires_grad=True) for k, v in pdict.items()}
+    cutoff = d4.Cutoff(**case.get("cutoff", {}), **dd)
+    cls = d4.D4Model if model_key == "d4" else d4.D4SModel
+    model = cls(numbers, **dd)
+    pos = positions.clone().requires_grad_(True)
+    if case.get("exact_c9"):
+        disp = DispD4Exact(model=model, **dd)
+        energy = disp.calculate(numbers, pos, charge, param, cutoff=cutoff)
+    else:
+        damping = {"zero": ZeroDamping, "mzero": MZeroDamping, "op": OptimisedPowerDamping,
+                   "rational": RationalDamping}[case["damping"]]()
+        rvdw = torch.tensor(case["rvdw"], **dd) if "rvdw" in case else None
+        energy = d4.dftd4(numbers, pos, charge, param, model=model, cutoff=cutoff,
+                          rvdw=rvdw, damping_function=damping)
+    keys = sorted(param)
+    grads = torch.autograd.grad(energy.sum(), [pos] + [param[k] for k in keys])
+    return {"energy": energy.detach().numpy(), "grad": grads[0].numpy(),
+            "param_grad": np.array([g.item() for g in grads[1:]]),
+            "param_grad_keys": np.array(json.dumps(keys))}
+
+
 def run_case(d4, case: dict, model_key: str) -> dict[str, np.ndarray]:
     from tad_dftd4.damping import RationalDamping, ZeroDamping
     from tad_dftd4.dispersion.d4 import D4ATMApprox
@@ -176,13 +257,46 @@ def run_case(d4, case: dict, model_key: str) -> dict[str, np.ndarray]:
     return out
 
 
+def write_variants(d4, workloads, out: Path) -> None:
+    arrays: dict[str, np.ndarray] = {}
+    index = []
+    for case in variant_cases(workloads):
+        for model_key in case.get("models", ("d4", "d4s")):
+            tag = f"{case['name']}/{model_key}"
+            res = run_variant(d4, case, model_key)
+            meta = {"name": case["name"], "model": model_key,
+                    "param": case.get("param", DEFAULT_PARAM),
+                    "cutoff": case.get("cutoff", {}), "ref_charges": "eeq",
+                    "energy_only": False, "damping": case.get("damping", "rational"),
+                    "exact_c9": bool(case.get("exact_c9", False))}
+            arrays[f"{tag}/numbers"] = np.asarray(case["numbers"], dtype=np.int64)
+            arrays[f"{tag}/positions"] = np.asarray(case["positions"], dtype=np.float64)
+            arrays[f"{tag}/charge"] = np.asarray(case["charge"], dtype=np.float64)
+            if "rvdw" in case:
+                arrays[f"{tag}/rvdw"] = np.asarray(case["rvdw"], dtype=np.float64)
+            arrays[f"{tag}/meta"] = np.array(json.dumps(meta))
+            for k, v in res.items():
+                arrays[f"{tag}/{k}"] = v
+            index.append(tag)
+            print(tag, "E =", float(res["energy"].sum()))
+    arrays["index"] = np.array(json.dumps(index))
+    np.savez_compressed(out, **arrays)
+    print("wrote", out)
+
+
 def main():
     parser = argparse.ArgumentParser()
     parser.add_argument("--src", type=Path, required=True, help="reference src/ directory")
     parser.add_argument("--out", type=Path, default=OUT)
+    parser.add_argument("--variants-out", type=Path, default=OUT_VARIANTS)
+    parser.add_argument("--only-variants", action="store_true",
+                        help="write only the damping-variant / exact-C9 fixtures")
     args = parser.parse_args()
     sys.path.insert(0, str(REPO))
     d4, workloads = _setup(args.src)
+    write_variants(d4, workloads, args.variants_out)
+    if args.only_variants:
+        return
     cases = reference_cases(args.src.parent) + seeded_cases(workloads)
     arrays: dict[str, np.ndarray] = {}
     index = []

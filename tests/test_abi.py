@@ -34,7 +34,7 @@ def test_library_exports_every_declared_function():
 
 def test_abi_version_and_status_strings():
     lib = package()._lib.load()
-    assert lib.d4_abi_version() == 1
+    assert lib.d4_abi_version() == 2
     assert lib.d4_status_string(0) == b"ok"
     assert b"EEQ" in lib.d4_status_string(5)
 
@@ -64,9 +64,11 @@ STRUCTS = {
     "d4_model_cfg_t": ("ModelCfg", ["kind", "ga", "gc", "wf"]),
     "d4_params_t": ("Params", ["s6", "s8", "s10", "a1", "a2", "s9", "alp", "has_s8",
                                "has_s10", "cut_disp2", "cut_disp3", "cut_cn", "cut_cn_eeq",
-                               "cn_eeq_max", "kcn", "k4", "k5", "k6"]),
+                               "cn_eeq_max", "kcn", "k4", "k5", "k6", "damping", "reserved",
+                               "rs6", "rs8", "bet"]),
     "d4_batch_t": ("Batch", ["n_struct", "n_pad", "d_numbers", "d_positions", "d_charge",
-                             "d_charges_in", "d_r4r2_in", "d_energy_weights"]),
+                             "d_charges_in", "d_r4r2_in", "d_energy_weights",
+                             "d_rvdw_in"]),
     "d4_outputs_t": ("Outputs", ["d_energy", "d_gradient", "d_charges", "d_cn",
                                  "d_param_grad", "d_cn_eeq"]),
     "d4_properties_t": ("Properties", ["d_cn", "d_charges", "d_c6", "d_alpha"]),

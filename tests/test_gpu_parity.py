@@ -247,3 +247,156 @@ def test_get_properties_matches_reference(d4, tag, arrays, meta):
     assert_close(c6.cpu(), arrays["c6"], 1e-12, 1e-12, "c6")
     alpha_ref = np.einsum("...r,...r->...", arrays["gw"], arrays["alpha"][..., 0])
     assert_close(alpha.cpu(), alpha_ref, 1e-12, 1e-13, "alpha")
+
+
+# ---------------------------------------------------------------- damping
+# variants and exact C9 (reference fixtures golden_variants.npz)
+
+from conftest import golden_variant_cases  # noqa: E402
+
+VARIANTS = golden_variant_cases()
+
+
+def _run_variant(d4, arrays, meta):
+    dev = torch.device("cuda")
+    numbers = torch.from_numpy(arrays["numbers"]).to(dev)
+    pos = torch.from_numpy(arrays["positions"]).to(dev).requires_grad_(True)
+    charge = torch.from_numpy(arrays["charge"]).to(dev)
+    cutoff = d4.Cutoff(**meta["cutoff"]) if meta["cutoff"] else None
+    keys = sorted(meta["param"])
+    param = {k: torch.tensor(v, dtype=torch.float64, device=dev, requires_grad=True)
+             for k, v in meta["param"].items()}
+    model = _model(d4, meta, numbers)
+    if meta["exact_c9"]:
+        energy = d4.DispD4Exact(model=model).calculate(numbers, pos, charge, param,
+                                                       cutoff=cutoff)
+    else:
+        damping = {"zero": d4.ZeroDamping, "mzero": d4.MZeroDamping,
+                   "op": d4.OptimisedPowerDamping}[meta["damping"]]()
+        rvdw = torch.from_numpy(arrays["rvdw"]).to(dev) if "rvdw" in arrays else None
+        energy = d4.dftd4(numbers, pos, charge, param, model=model, cutoff=cutoff,
+                          rvdw=rvdw, damping_function=damping)
+    gs = torch.autograd.grad(energy.sum(), [pos] + [param[k] for k in keys])
+    return (energy.detach().cpu().numpy(), gs[0].cpu().numpy(),
+            np.array([g.item() for g in gs[1:]]))
+
+
+@pytest.mark.parametrize("tag,arrays,meta", VARIANTS, ids=[c[0] for c in VARIANTS])
+def test_damping_variants_and_exact_c9_match_reference(d4, tag, arrays, meta):
+    """Zero / modified-zero / optimised-power two-body damping and the exact
+    C9 of DispD4Exact, plain FP64 kernels, against the reference's own
+    classes: energies 1e-12, position and parameter gradients 1e-10."""
+    e, g, pg = _run_variant(d4, arrays, meta)
+    assert_close(e, arrays["energy"], E_RTOL, E_ATOL, "energy")
+    assert_close(g, arrays["grad"], G_RTOL, G_ATOL, "grad")
+    assert_close(pg, arrays["param_grad"], G_RTOL, G_ATOL, "param_grad")
+
+
+@pytest.mark.parametrize("model", ["d4", "d4s"])
+def test_exact_c9_batch_vs_oracle(d4, model):
+    """Exact C9 on a padded, charged batch (the reference's D4S variant has
+    no batched result; the oracle divides per structure)."""
+    b = _batch(102, 5, 4, 40)
+    param = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0, "s9": 1.0}
+    numbers = torch.from_numpy(b.numbers)
+    positions = torch.from_numpy(b.positions)
+    charge = torch.from_numpy(b.charge)
+    e_ref, g_ref = oracle.dftd4_energy_and_grad(numbers, positions, charge, param,
+                                                model=model, exact_c9=True,
+                                                cutoff={"disp3": 12.0})
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(numbers.to(dev), positions.to(dev), charge.to(dev),
+                                         param, model=model, exact_c9=True,
+                                         cutoff=d4.Cutoff(disp3=12.0))
+    assert_close(e.cpu().numpy(), e_ref.numpy(), E_RTOL, E_ATOL, "energy")
+    assert_close(g.cpu().numpy(), g_ref.numpy(), G_RTOL, G_ATOL, "grad")
+
+
+def test_variant_argument_errors(d4):
+    """The reference's errors for the damping family: missing parameters
+    (TypeError), order 10 without it (ValueError), no pair radii, and the
+    precision form refusing what it does not run."""
+    dev = torch.device("cuda")
+    b = _batch(103, 1, 6, 10)
+    numbers = torch.from_numpy(b.numbers).to(dev)
+    positions = torch.from_numpy(b.positions).to(dev)
+    rv = torch.full((1, numbers.shape[1], numbers.shape[1]), 4.0, dtype=torch.float64,
+                    device=dev)
+    with pytest.raises(TypeError, match=r"ZeroDamping \(order 8\) requires keyword\(s\): rs8"):
+        d4.dftd4(numbers, positions, 0.0, {"rs6": 1.0, "s8": 1.0}, rvdw=rv,
+                 damping_function=d4.ZeroDamping())
+    with pytest.raises(ValueError, match="OP-damping is only implemented"):
+        d4.dftd4(numbers, positions, 0.0, {"a1": 0.4, "a2": 5.0, "bet": 1.0, "s10": 1.0},
+                 damping_function=d4.OptimisedPowerDamping())
+    with pytest.raises(ValueError, match="rvdw"):
+        d4.dftd4(numbers, positions, 0.0, {"rs6": 1.0}, damping_function=d4.ZeroDamping())
+    with pytest.raises(ValueError, match="precision form"):
+        d4.dftd4(numbers, positions, 0.0, {"rs6": 1.0}, rvdw=rv,
+                 damping_function=d4.ZeroDamping(), precision="mixed")
+
+
+# ---------------------------------------------------------------- the plain
+# FP64 method at the benchmarked sizes (the batch512 workload draws N from
+# [8, 200]): the oracle per structure, unpadded, against the padded batch
+
+def _oracle_with_scale(numbers, positions, charge, param, model="d4"):
+    """Oracle energies, gradients and the per-atom error scale: each atom
+    energy is a float64 sum of ~N two-body and ~N^2/2 three-body terms of
+    both signs, so two summation orders differ by up to ~1e-16 sqrt(terms)
+    times the sum of the terms' magnitudes, not times the net value.  The
+    scale is |E2_i| + sum |ATM shares of i|."""
+    pos = positions.clone().requires_grad_(True)
+    e, parts = oracle.dftd4(numbers, pos, charge, param, model=model, return_parts=True)
+    (g,) = torch.autograd.grad(e.sum(), pos)
+    return e.detach().numpy(), g.numpy(), parts["scale"].numpy()
+
+
+@pytest.mark.parametrize("model", ["d4", "d4s"])
+def test_plain_fp64_at_batch512_sizes_vs_oracle(d4, model):
+    """8 charged structures with N in [150, 200], padded to 200, 12
+    elements at density 0.01 / Bohr^3 (the batch512 generator).  Energies:
+    1e-12 relative to the magnitude of each atom's summed contributions
+    (|E2_i| + sum of |ATM shares|; a few atoms' net energies cancel to 1e-3
+    of that, where the plain relative error of two float64 summation orders
+    reaches ~4e-11); gradients 1e-10 relative with a 1e-13 Eh/Bohr floor."""
+    wl = package().workloads
+    b = wl.batch_uniform(7, 8, 150, 200, wl.ELEMENTS_12, True, "plain8", 200)
+    param = dict(wl.BJ_PARAMS)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(torch.from_numpy(b.numbers).to(dev),
+                                         torch.from_numpy(b.positions).to(dev),
+                                         torch.from_numpy(b.charge).to(dev), param,
+                                         model=model, precision="fp64")
+    e, g = e.cpu().numpy(), g.cpu().numpy()
+    for k in range(len(b.numbers)):
+        n = int((b.numbers[k] != 0).sum())
+        assert 150 <= n <= 200
+        e_ref, g_ref, scale = _oracle_with_scale(
+            torch.from_numpy(b.numbers[k:k + 1, :n]), torch.from_numpy(b.positions[k:k + 1, :n]),
+            torch.from_numpy(b.charge[k:k + 1]), param, model=model)
+        err = np.abs(e[k, :n] - e_ref[0])
+        assert (err <= E_RTOL * scale[0] + E_ATOL).all(), (k, (err / scale[0]).max())
+        assert_close(g[k, :n], g_ref[0], G_RTOL, G_ATOL, f"grad {k}")
+        assert (e[k, n:] == 0).all() and (g[k, n:] == 0).all()
+
+
+def test_plain_fp64_global_memory_eeq_vs_oracle(d4):
+    """One 280-atom structure: its packed Cholesky factor exceeds shared
+    memory, so the FP64 EEQ solve and its adjoint run from global memory
+    (the path every 400-1100-atom precision-form test compares against)."""
+    wl = package().workloads
+    z, r = wl.structure(4280, 280)
+    numbers, positions = z[None], r[None]
+    charge = np.array([1.0])
+    param = dict(wl.BJ_PARAMS)
+    dev = torch.device("cuda")
+    e, g = d4.dispersion_energy_gradient(torch.from_numpy(numbers).to(dev),
+                                         torch.from_numpy(positions).to(dev),
+                                         torch.from_numpy(charge).to(dev), param,
+                                         precision="fp64")
+    e_ref, g_ref, scale = _oracle_with_scale(torch.from_numpy(numbers),
+                                             torch.from_numpy(positions),
+                                             torch.from_numpy(charge), param)
+    err = np.abs(e.cpu().numpy() - e_ref)
+    assert (err <= E_RTOL * scale + E_ATOL).all(), (err / scale).max()
+    assert_close(g.cpu().numpy(), g_ref, G_RTOL, G_ATOL, "grad")

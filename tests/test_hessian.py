@@ -47,12 +47,38 @@ def test_fd_hessian_of_a_quadratic_is_exact():
     nums = (torch.arange(B) + 1)[:, None].expand(B, N)  # numbers tag the structure
     pos = torch.randn(B, N, 3, generator=g, dtype=torch.float64)
 
-    def grad_fn(n, p, c):
+    calls = []
+
+    def grad_fn(n, p, c, src):
         k = n[:, 0] - 1  # structure of each geometry
+        assert torch.equal(k, src)
+        calls.append(len(n))
         return torch.einsum("mij,mj->mi", a[k], p.reshape(-1, 3 * N)).reshape(-1, N, 3)
 
     h = disp._fd_hessian(grad_fn, nums, pos, torch.zeros(B), 1e-3, max_structs=40)
     assert torch.allclose(h.reshape(B, 3 * N, 3 * N), a, atol=1e-9, rtol=0)
+    assert max(calls) <= 40 and sum(calls) == B * 2 * 3 * N
+
+
+def test_fd_hessian_splits_a_structure_beyond_the_call_limit():
+    """6N displaced geometries above max_structs: the coordinates of one
+    structure are split over several calls, none larger than the limit."""
+    disp = import_module("tad-dftd4_gb300.disp")
+    B, N = 2, 5  # 30 geometries per structure
+    g = torch.Generator().manual_seed(12)
+    a = torch.randn(B, 3 * N, 3 * N, generator=g, dtype=torch.float64)
+    a = a + a.transpose(1, 2)
+    nums = (torch.arange(B) + 1)[:, None].expand(B, N)
+    pos = torch.randn(B, N, 3, generator=g, dtype=torch.float64)
+    calls = []
+
+    def grad_fn(n, p, c, src):
+        calls.append(len(n))
+        return torch.einsum("mij,mj->mi", a[src], p.reshape(-1, 3 * N)).reshape(-1, N, 3)
+
+    h = disp._fd_hessian(grad_fn, nums, pos, torch.zeros(B), 1e-3, max_structs=8)
+    assert torch.allclose(h.reshape(B, 3 * N, 3 * N), a, atol=1e-9, rtol=0)
+    assert max(calls) <= 8 and sum(calls) == B * 2 * 3 * N
 
 
 def test_fd_hessian_of_the_oracle_gradient_matches_autograd():
@@ -62,7 +88,7 @@ def test_fd_hessian_of_the_oracle_gradient_matches_autograd():
     disp = import_module("tad-dftd4_gb300.disp")
     nt, pt, ct = _batch()
 
-    def grad_fn(n, p, c):
+    def grad_fn(n, p, c, src):
         return oracle.dftd4_energy_and_grad(n, p, c, PARAM)[1]
 
     h = disp._fd_hessian(grad_fn, nt, pt, ct, 1e-4)

@@ -15,7 +15,7 @@ import pytest
 import torch
 
 import oracle
-from conftest import assert_close, golden_cases
+from conftest import assert_close, golden_cases, golden_variant_cases
 
 CASES = golden_cases()
 RTOL, ATOL = 1e-12, 1e-15
@@ -83,3 +83,32 @@ def test_exceptional_case_is_exceptional():
     refcn = tables.refcovcn[numbers]
     dcn = (cn.unsqueeze(-1) - refcn).abs().min(-1)[0]
     assert (dcn > 11.0).any(), dcn
+
+
+VARIANTS = golden_variant_cases()
+
+
+def _variant_kwargs(arrays, meta):
+    kw = {"model": meta["model"], "damping": meta["damping"], "exact_c9": meta["exact_c9"]}
+    if "rvdw" in arrays:
+        kw["rvdw"] = torch.from_numpy(arrays["rvdw"])
+    return kw
+
+
+@pytest.mark.parametrize("tag,arrays,meta", VARIANTS, ids=[c[0] for c in VARIANTS])
+def test_damping_variants_and_exact_c9(tag, arrays, meta):
+    """The oracle's D3-family damping and exact C9 against the reference's
+    ZeroDamping / MZeroDamping / OptimisedPowerDamping and DispD4Exact:
+    energies 1e-12, position and parameter gradients 1e-10."""
+    numbers, positions, charge, param, cutoff = _inputs(arrays, meta)
+    pos = positions.clone().requires_grad_(True)
+    keys = sorted(param)
+    ptens = {k: torch.tensor(v, dtype=torch.float64, requires_grad=True)
+             for k, v in param.items()}
+    energy = oracle.dftd4(numbers, pos, charge, ptens, cutoff=cutoff,
+                          **_variant_kwargs(arrays, meta))
+    assert_close(energy.detach(), arrays["energy"], RTOL, ATOL, "energy")
+    grads = torch.autograd.grad(energy.sum(), [pos] + [ptens[k] for k in keys])
+    assert_close(grads[0], arrays["grad"], 1e-10, 1e-14, "grad")
+    assert_close(np.array([g.item() for g in grads[1:]]), arrays["param_grad"],
+                 1e-10, 1e-14, "param_grad")
