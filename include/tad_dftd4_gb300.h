@@ -71,6 +71,13 @@ typedef enum d4_model_kind { D4_MODEL_D4 = 0, D4_MODEL_D4S = 1 } d4_model_kind;
                                   dispersion/d4.py:67-84) instead of
                                   sqrt(C6 C6 C6); plain FP64 method only */
 
+/* Test hook of the timeout handling: the tensor-core pair kernel of the
+   precision form treats the first wait for its MMAs as timed out and takes
+   its error path (status D4_ERR_DEVICE_TIMEOUT, a bounded wait for the MMAs
+   in flight, tensor memory released, early return).  Results of such a call
+   are incomplete; the next call is unaffected. */
+#define D4_FLAG_TEST_TIMEOUT 0x80000000u
+
 /* Entries per structure of d_param_grad: dE_b / d(s6, s8, s10, a1, a2, s9,
    alp, rs6, rs8, bet), then two unused entries. */
 #define D4_PARAM_GRAD_STRIDE 12
@@ -263,6 +270,16 @@ const char *d4_stage_name(int32_t stage);
  */
 int d4_probe_fma(int32_t fp64, int32_t n_blocks, int32_t iters, double *d_sink,
                  float *ms_out, void *stream);
+
+/*
+ * Self-test of the bounded waits every tensor-core kernel uses: one CTA
+ * initialises an mbarrier that nothing arrives on and waits for it with the
+ * library's wait loop, limited to ``limit_ns`` nanoseconds of the GPU's
+ * global timer; the outcome (D4_ERR_DEVICE_TIMEOUT when the limit ran out,
+ * as it must) goes to ``*d_result`` (device int).  No counterpart in the
+ * reference.
+ */
+int d4_selftest_wait(int32_t *d_result, uint64_t limit_ns, void *stream);
 
 /*
  * Allocation-free variant of d4_dispersion.  This entry point has no

@@ -39,6 +39,7 @@ FLAG_CHARGES_IN = 2
 FLAG_MIXED = 4
 FLAG_PARAM_GRAD = 8
 FLAG_EXACT_C9 = 16
+FLAG_TEST_TIMEOUT = 0x80000000  # test hook: the pair kernel's first MMA wait counts as timed out
 PARAM_GRAD_STRIDE = 12  # D4_PARAM_GRAD_STRIDE: s6 s8 s10 a1 a2 s9 alp rs6 rs8 bet - -
 
 DAMP_RATIONAL = 0
@@ -166,6 +167,7 @@ SIGNATURES = {
         [ctypes.POINTER(Tables), ctypes.POINTER(ModelCfg), ctypes.POINTER(Batch),
          ctypes.POINTER(Params), c_void_p, c_size_t, ctypes.POINTER(Properties), c_void_p],
     ),
+    "d4_selftest_wait": (c_int, [c_void_p, ctypes.c_uint64, c_void_p]),
     "d4_dispersion_noalloc": (
         c_int,
         [ctypes.POINTER(Tables), ctypes.POINTER(ModelCfg), ctypes.POINTER(Batch),

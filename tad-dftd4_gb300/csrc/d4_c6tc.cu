@@ -196,6 +196,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   const uint32_t t_lane = (uint32_t)(quad * 32) << 16;
   uint32_t parity = 0;
   bool timed_out = false;
+  const bool test_timeout = (c.flags & D4_FLAG_TEST_TIMEOUT) != 0;
   for (int j0 = ch0 * TC_NJ; j0 < ch1 * TC_NJ; j0 += TC_NJ) {
     // B operands (digits under per-row scales) and partner data of the chunk
     __shared__ int s_eb[2][TC_NJ];
@@ -257,7 +258,9 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
       }
       tc::commit(mbar);
     }
-    const bool done = tc::mbar_wait(mbar, parity);
+    // (test hook: the first wait of a D4_FLAG_TEST_TIMEOUT call counts as
+    // timed out; the drain below then waits for these MMAs for real)
+    const bool done = (test_timeout && j0 == ch0 * TC_NJ) ? false : tc::mbar_wait(mbar, parity);
     parity ^= 1u;
     if (__syncthreads_or(!done)) {
       timed_out = true;

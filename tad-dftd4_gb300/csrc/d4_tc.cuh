@@ -104,12 +104,13 @@ __device__ __forceinline__ bool mbar_try_wait(uint32_t mbar, uint32_t parity) {
 }
 
 // Wait for the phase with the given parity to complete, at most
-// WAIT_LIMIT_NS; false when the limit ran out.
-__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity) {
+// ``limit_ns``; false when the limit ran out.
+__device__ __forceinline__ bool mbar_wait(uint32_t mbar, uint32_t parity,
+                                          unsigned long long limit_ns = WAIT_LIMIT_NS) {
   if (mbar_try_wait(mbar, parity)) return true;
   const unsigned long long t0 = global_ns();
   while (!mbar_try_wait(mbar, parity))
-    if (global_ns() - t0 > WAIT_LIMIT_NS) return false;
+    if (global_ns() - t0 > limit_ns) return false;
   return true;
 }
 

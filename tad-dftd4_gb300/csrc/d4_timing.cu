@@ -3,6 +3,7 @@
 
 #include "d4_common.cuh"
 #include "d4_kernels.cuh"
+#include "d4_tc.cuh"
 
 namespace d4 {
 namespace {
@@ -62,9 +63,25 @@ __global__ void __launch_bounds__(256) fma_probe_kernel(int iters, double *sink)
   sink[(size_t)blockIdx.x * blockDim.x + threadIdx.x] = (double)s;
 }
 
+// One thread waits, with the library's bounded wait loop, for an mbarrier
+// phase that nothing completes (initialised for one arrival, none made).
+__global__ void selftest_wait_kernel(int32_t *result, unsigned long long limit_ns) {
+  __shared__ __align__(8) unsigned long long bar;
+  const uint32_t mbar = tc::smem_u32(&bar);
+  tc::mbar_init(mbar, 1);
+  *result = tc::mbar_wait(mbar, 0u, limit_ns) ? D4_OK : D4_ERR_DEVICE_TIMEOUT;
+}
+
 }  // namespace d4
 
 extern "C" {
+
+int d4_selftest_wait(int32_t *d_result, uint64_t limit_ns, void *stream) {
+  if (!d_result || limit_ns > 1000000000ull) return D4_ERR_ARGUMENT;
+  d4::selftest_wait_kernel<<<1, 1, 0, static_cast<cudaStream_t>(stream)>>>(
+      d_result, (unsigned long long)limit_ns);
+  return cudaGetLastError() == cudaSuccess ? D4_OK : D4_ERR_CUDA;
+}
 
 int d4_timing_begin(int32_t max_calls) {
   using namespace d4;

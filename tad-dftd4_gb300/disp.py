@@ -118,7 +118,8 @@ class Runner:
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
-            cn_out: bool = False, cn_eeq_out: bool = False, defer_status: bool = False):
+            cn_out: bool = False, cn_eeq_out: bool = False, defer_status: bool = False,
+            extra_flags: int = 0):
         lib = _lib.load()
         device = positions.device
         B, N = self.numbers.shape
@@ -134,6 +135,7 @@ class Runner:
             flags |= _lib.FLAG_MIXED
         if self.exact_c9:
             flags |= _lib.FLAG_EXACT_C9
+        flags |= extra_flags
         energy = torch.empty((B, N), dtype=torch.float64, device=device)
         grad = (torch.empty((B, N, 3), dtype=torch.float64, device=device)
                 if flags & _lib.FLAG_GRADIENT else None)
