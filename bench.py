@@ -70,6 +70,9 @@ def parse_args():
     ap.add_argument("--no-cpu-baseline", action="store_true")
     ap.add_argument("--no-large", action="store_true",
                     help="skip the one-structure 16000-atom measurement")
+    ap.add_argument("--large-n", type=int, default=0,
+                    help="only run the large-structure measurement, with this many "
+                         "atoms (no FP64 check), and print its JSON")
     ap.add_argument("--serve-requests", type=int, default=20000,
                     help="requests of the serving stream (0 skips it)")
     ap.add_argument("--serve-plain-requests", type=int, default=3000,
@@ -315,14 +318,18 @@ def probe_peak(lib, pkg, dev, fp64: bool) -> float:
 KERNELS_PER_CALL = 13
 
 
-def run_large(pkg, disp, lib, dev, steps: int = 3):
-    """One 16000-atom structure (H/C/N/O/S, density 0.01, neutral, pair and
-    ATM cutoffs 50 / 25 Bohr), precision form, energy + forces: seconds per
-    structure and per-stage times.  The inputs (10 GB of workspace) are far
-    larger than L2."""
+def run_large(pkg, disp, lib, dev, steps: int = 3, natoms: int = 16000,
+              fp64_check: bool = True):
+    """One large structure (16000 atoms by default; H/C/N/O/S, density 0.01,
+    neutral, pair and ATM cutoffs 50 / 25 Bohr), precision form, energy +
+    forces: milliseconds per structure and per-stage times (the inputs, 10 GB
+    of workspace at 16000 atoms, are far larger than L2).  Then the errors
+    against a float64 reference of the same structure (the neighbour-list
+    restatement of the oracle, run on the GPU as the checker; not timed) and
+    the EEQ residual of the returned charges in float64."""
     import torch
 
-    batch = pkg.workloads.large16k(2)
+    batch = pkg.workloads.large16k(2, natoms)
     n = batch.numbers.shape[1]
     nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (batch.numbers, batch.positions,
                                                         batch.charge))
@@ -345,9 +352,12 @@ def run_large(pkg, disp, lib, dev, steps: int = 3):
     pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
     ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
     fsum = g[0].sum(0).abs().max().item()
+    _, _, _, q, _ = runner.run(pt, gradient=False, charges_out=True)
+    torch.cuda.synchronize()
     out = {
-        "workload": "large16k: 1 structure, N=16000 H/C/N/O/S (0.45/0.3/0.1/0.1/0.05), "
-                    "density 0.01/Bohr^3, neutral, seed 2, cutoffs disp2=50 disp3=25",
+        "workload": f"large{natoms // 1000}k: 1 structure, N={natoms} H/C/N/O/S "
+                    "(0.45/0.3/0.1/0.1/0.05), density 0.01/Bohr^3, neutral, seed 2, "
+                    "cutoffs disp2=50 disp3=25",
         "method": "precision form, energy + forces",
         "ms_per_structure": float(np.median(ms)), "structures_per_s": 1e3 / float(np.median(ms)),
         "atom_pairs_per_s": n * (n - 1) / 2 / (float(np.median(ms)) * 1e-3),
@@ -356,11 +366,46 @@ def run_large(pkg, disp, lib, dev, steps: int = 3):
         "energy_eh": float(e.sum()),
         "max_abs_sum_of_forces_eh_bohr": fsum,
         "peak_device_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
-        "fp64_check": "no FP64 result at this size (the CPU oracle and the plain FP64 "
-                      "kernels are dense O(N^3)); the same kernels are checked against the "
-                      "plain FP64 path on 1100-atom structures in the GPU tests",
     }
-    del runner, e, g
+    e_prod = e[0].detach().clone()
+    g_prod = g[0].detach().clone()
+    q_prod = q[0].detach().clone()
+    del runner, e, g, q
+    torch.cuda.empty_cache()
+    if fp64_check:
+        out["error_vs_fp64_reference"] = large_fp64_errors(nt[0], pt[0], e_prod, g_prod,
+                                                           q_prod, param)
+    return out
+
+
+def large_fp64_errors(numbers, positions, e_prod, g_prod, q_prod, param):
+    """|dE|, max |dF| and the charges' EEQ residual of a large structure
+    against the float64 neighbour-list restatement (oracle/d4_nbr.py),
+    evaluated on the GPU; checker only, outside every timed region."""
+    import torch
+
+    from oracle import d4_nbr
+
+    t0 = time.perf_counter()
+    cutoff = {"disp2": 50.0, "disp3": 25.0}
+    e_ref, g_ref, extra = d4_nbr.dftd4_large(numbers, positions, 0.0, param, cutoff=cutoff)
+    res_prod = d4_nbr.eeq_residual(numbers, positions, 0.0, q_prod)
+    res_ref = d4_nbr.eeq_residual(numbers, positions, 0.0, extra["q"])
+    out = {
+        "reference": "float64 neighbour-list restatement of the oracle (dense pair terms, "
+                     "factorised C6, ATM over neighbour triples, dense float64 EEQ solve), "
+                     "cross-checked against the dense oracle in tests/test_oracle_nbr.py",
+        "abs_dE_total_eh": abs(float(e_prod.sum() - e_ref.sum())),
+        "max_abs_dE_atom_eh": float((e_prod - e_ref).abs().max()),
+        "max_abs_dF_eh_bohr": float((g_prod - g_ref).abs().max()),
+        "max_abs_dq": float((q_prod - extra["q"]).abs().max()),
+        "eeq_residual_precision_form": res_prod,
+        "eeq_residual_fp64_solve": res_ref,
+        "energy_fp64_eh": float(e_ref.sum()),
+        "atm_triples": extra["triples"],
+        "checker_seconds": time.perf_counter() - t0,
+    }
+    del e_ref, g_ref, extra
     torch.cuda.empty_cache()
     return out
 
@@ -601,15 +646,6 @@ def run_ours(args, world, rank, local):
             "atom_pairs_per_s": world * pairs * args.steps / total_s,
             "latency_ms": {"p50": float(np.percentile(step_ms, 50)),
                            "p99": float(np.percentile(step_ms, 99))},
-            "plain_fp64": {"value": plain_value, "unit": UNIT,
-                           "ms_per_step": plain_total * 1e3 / plain_steps,
-                           "speedup_of_precision_form": value / plain_value,
-                           "stage_ms": plain_stages,
-                           "atm_achieved_tflops": plain_achieved, "fp64_peak_tflops": fp64_peak},
-            "error_vs_fp64_oracle": err_m,
-            "error_plain_fp64_vs_oracle": err_p,
-            "error_precision_vs_plain_all_structures": {"max_abs_dE_eh": e_all,
-                                                        "max_abs_dF_eh_bohr": f_all},
             "e2e": {"value": e2e_value, "unit": UNIT, "h2d_bytes_per_step": h2d,
                     "d2h_bytes_per_step": d2h,
                     "latency_ms": {"p50": 1e3 * float(np.percentile(lat, 50)),
@@ -633,6 +669,17 @@ def run_ours(args, world, rank, local):
             "large16k": large,
             "diff256": diff,
             "serving": serve,
+            # last, so that a record that keeps only the end of the line keeps them
+            "plain_fp64": {"value": plain_value, "unit": UNIT,
+                           "ms_per_step": plain_total * 1e3 / plain_steps,
+                           "speedup_of_precision_form": value / plain_value,
+                           "stage_ms": plain_stages,
+                           "atm_achieved_tflops": plain_achieved, "fp64_peak_tflops": fp64_peak},
+            "error_vs_fp64_oracle": err_m,
+            "error_plain_fp64_vs_oracle": err_p,
+            "error_precision_vs_plain_all_structures": {"max_abs_dE_eh": e_all,
+                                                        "max_abs_dF_eh_bohr": f_all},
+            "large16k_error_vs_fp64": (large or {}).get("error_vs_fp64_reference"),
         }
         print(json.dumps(line), flush=True)
 
@@ -640,6 +687,15 @@ def run_ours(args, world, rank, local):
 def main():
     args = parse_args()
     world, rank, local = dist_setup(args.gpus)
+    if args.large_n > 0:
+        import torch
+
+        pkg = importlib.import_module("tad-dftd4_gb300")
+        disp = importlib.import_module("tad-dftd4_gb300.disp")
+        out = run_large(pkg, disp, pkg._lib.load(), torch.device("cuda", local),
+                        steps=max(1, args.steps), natoms=args.large_n, fp64_check=False)
+        print(json.dumps(out), flush=True)
+        return
     if args.impl == "reference":
         run_reference(args, world, rank)
     else:
