@@ -124,8 +124,11 @@ def _distances(positions: torch.Tensor, mask: torch.Tensor) -> torch.Tensor:
 
 
 def erf_count(r: torch.Tensor, r0: torch.Tensor, kcn: float) -> torch.Tensor:
-    """Error-function counting function 1/2 (1 + erf(-k (r/r0 - 1)))."""
-    return 0.5 * (1.0 + torch.erf(-kcn * (r / r0 - 1.0)))
+    """Error-function counting function 1/2 (1 + erf(-k (r/r0 - 1))),
+    evaluated as 1/2 erfc(k (r/r0 - 1)): the same function without the
+    cancellation of 1 + erf(-x) for the far pairs (x >> 1) that make up the
+    coordination number of a nearly isolated atom."""
+    return 0.5 * torch.erfc(kcn * (r / r0 - 1.0))
 
 
 def cn_d4(
@@ -171,7 +174,10 @@ def cn_eeq(
     """
     EEQ coordination number: plain erf counting within ``cutoff``
     (``Cutoff.cn_eeq``, ``dispersion/base.py:401-407``), then the smooth cap
-    log(1 + e^max) - log(1 + e^(max - cn)) at ``defaults.py:32``.
+    log(1 + e^max) - log(1 + e^(max - cn)) at ``defaults.py:32``, evaluated
+    as log1p(expm1(cn) / (1 + e^(cn - max))): the same function without the
+    cancellation of the two logarithms for cn << 1 (nearly isolated atoms,
+    whose sqrt(cn) enters the EEQ right-hand side).
     """
     dtype = positions.dtype
     mask = _real_pairs(numbers)
@@ -180,7 +186,7 @@ def cn_eeq(
     r0 = rcov.unsqueeze(-1) + rcov.unsqueeze(-2)
     cf = erf_count(r, r0, kcn)
     cn = torch.where(mask & (r <= cutoff), cf, torch.zeros_like(r)).sum(-1)
-    return math.log(1.0 + math.exp(cn_max)) - torch.log(1.0 + torch.exp(cn_max - cn))
+    return torch.log1p(torch.expm1(cn) / (1.0 + torch.exp(cn - cn_max)))
 
 
 def eeq_charges(
@@ -620,7 +626,7 @@ def dftd4(
             e3_abs = atm_dispersion(numbers, positions, param, c6_0, r4r2, cutoff=cut["disp3"],
                                     c9=c9, absolute=True)
         return energy, {"cn": cn, "q": q, "c6": c6, "c6_0": c6_0, "e2": e2, "e3": e3,
-                        "scale": e2.abs() + e3_abs}
+                        "scale": e2.detach().abs() + e3_abs}
     return energy
 
 

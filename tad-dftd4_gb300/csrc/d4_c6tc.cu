@@ -304,7 +304,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         const float3 dv = pos_diff(pi, li, pj, S.lj[r]);
         const float dx = dv.x, dy = dv.y, dz = dv.z;
         const float r2 = dx * dx + dy * dy + dz * dz;
-        const float ir = rsqrtf(r2);
+        const float ir = __frcp_rn(sqrtf(r2));  // correctly rounded: no bias in the ATM records
         const float rr = r2 * ir;
         const float c6 = c6v[q];
         const float c60 = c60v[q];
@@ -328,17 +328,17 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
         }
         const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
         const float iR0 = __frcp_rn(R0);
-        // log2(R0 / r) and (R0 / r)^(alp/3) of the ATM damping through the
-        // accurate log2f / exp2f (SFU estimates bias the three-body energy by
-        // ~1e-6 relative)
-        const float l2R0r = log2f(R0 * ir) + R0d.lo * iR0 * 1.4426950408889634f;
+        // log(R0 / r) and (R0 / r)^(alp/3) of the ATM damping through logf /
+        // expf (SFU estimates bias the three-body energy by ~1e-6 relative;
+        // exp2f keeps a mean relative error of ~-3e-8, expf ~+5e-9, and every
+        // triple multiplies three of these factors)
+        const float lnR0r = logf(R0 * ir) + R0d.lo * iR0;
         const float ir2 = __frcp_rn(r2);
-        Tt[(size_t)j * N + i] = make_float4(r2, ir2, exp2f(alp3 * l2R0r),
+        Tt[(size_t)j * N + i] = make_float4(r2, ir2, expf(alp3 * lnR0r),
                                             sqrtf(fmaxf(c60, 0.f)) * (ir * ir2));
         r2mx = fmaxf(r2mx, r2);
         if (PGRAD)
-          Tdat[(size_t)j * N + i] =
-              make_float4(sqq * iR0, iR0, l2R0r * 0.6931471805599453f, 0.f);
+          Tdat[(size_t)j * N + i] = make_float4(sqq * iR0, iR0, lnR0r, 0.f);
         if (rr <= cut2) {
           const float r6 = r2 * r2 * r2, R02 = R0 * R0, R06 = R06d.hi;
           const float t6 = __frcp_rn((r6 + R06) + R06d.lo);

@@ -134,6 +134,8 @@ struct Workspace {
   float2 *sfw;      // [32] sqrt((3/pi) w) of the Casimir-Polder weights, double-float
   float4 *pairA;    // [MAX_ELEM_ID^2] (R0, qq) per element pair, double-floats (hi, lo, hi, lo)
   float4 *pairB;    // [MAX_ELEM_ID^2] (R0^6, R0^8) per element pair, double-floats
+  float4 *cnpair;   // [MAX_ELEM_ID^2] (1 / (rcov_a + rcov_b), k4 exp(-(|en_a - en_b| + k5)^2
+                    //  / k6)) per element pair, double-floats (hi, lo, hi, lo)
   float4 *ref32;    // [MAX_ELEM_ID*7] (refcovcn, refq + zeff, Gaussians, zeta at q = 0)
   float2 *el32;     // [MAX_ELEM_ID] (zeff, gam * gc)
   float *G32;       // [B*N*S*23] dE/dA
@@ -246,6 +248,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     w.sfw = (float2 *)take(8 * 32);
     w.pairA = (float4 *)take(16 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
     w.pairB = (float4 *)take(16 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
+    w.cnpair = (float4 *)take(16 * (size_t)MAX_ELEM_ID * MAX_ELEM_ID);
     w.ref32 = (float4 *)take(16 * (size_t)MAX_ELEM_ID * NREF);
     w.el32 = (float2 *)take(8 * (size_t)MAX_ELEM_ID);
     w.G32 = grad ? (float *)take(4 * BNS23) : nullptr;
@@ -322,9 +325,12 @@ __device__ __forceinline__ void set_status(int *status, int code) {
   atomicCAS(status, 0, code);
 }
 
-// Error-function counting function of the CN: 1/2 (1 + erf(-k (r/r0 - 1))).
+// Error-function counting function of the CN, 1/2 (1 + erf(-x)) with
+// x = k (r/r0 - 1), evaluated as 1/2 erfc(x): the same function without the
+// cancellation of 1 + erf(-x) for x >> 1, where the far pairs of a nearly
+// isolated atom make up its whole (tiny) coordination number.
 __device__ __forceinline__ double erf_count(double r, double r0, double k) {
-  return 0.5 * (1.0 + erf(-k * (r / r0 - 1.0)));
+  return 0.5 * erfc(k * (r / r0 - 1.0));
 }
 
 // Its derivative with respect to r.

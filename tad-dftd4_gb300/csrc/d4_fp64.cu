@@ -141,9 +141,8 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
 
 // D4 coordination number (EN weighted, cut_cn) and the EEQ coordination
 // number (plain count, cut_cn_eeq, smooth cap) in one pass over the pairs.
-// 1/2 (1 + erf(-x)) is exactly 0.0 in FP64 for x > 6, so a pair whose FP32
-// estimate of x exceeds 7 adds nothing and is dropped before any FP64 work
-// (the sums stay bitwise the same).  The surviving partners of the warp's
+// A pair whose FP32 estimate of x exceeds 9 (1/2 erfc(x) < 1e-36) is dropped
+// before any FP64 work.  The surviving partners of the warp's
 // atom are queued in shared memory and evaluated 32 at a time, so the FP64
 // instructions run with full warps.
 __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
@@ -190,7 +189,7 @@ __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
       const float4 pj32 = P32[j];
       const float ex = pi32.x - pj32.x, ey = pi32.y - pj32.y, ez = pi32.z - pj32.z;
       const float r32 = sqrtf(ex * ex + ey * ey + ez * ez);
-      keep = kcn32 * (r32 / (rci32 + X32[j].x) - 1.0f) <= 7.0f;
+      keep = kcn32 * (r32 / (rci32 + X32[j].x) - 1.0f) <= 9.0f;  // erfc(9) / 2 < 1e-36
     }
     const unsigned m = __ballot_sync(0xffffffffu, keep);
     if (keep) s_q[warp][queued + __popc(m & ((1u << lane) - 1u))] = j;
@@ -210,7 +209,11 @@ __global__ void __launch_bounds__(256) cn_kernel(Ctx c) {
   if (lane == 0) {
     c.w.cn[ai] = s_d4;
     const double m = c.par.cn_eeq_max;
-    c.w.cnq[ai] = log1p(exp(m)) - log1p(exp(m - s_q4));
+    // log(1 + e^m) - log(1 + e^(m - cn)) as log1p(expm1(cn) / (1 + e^(cn - m))):
+    // the same function without the cancellation of the two logarithms, so
+    // that nearly isolated atoms (cn << 1) keep a relative accuracy (the EEQ
+    // right-hand side takes sqrt(cn), which magnifies absolute noise there)
+    c.w.cnq[ai] = log1p(expm1(s_q4) / (1.0 + exp(s_q4 - m)));
     c.w.dcnq[ai] = 1.0 / (1.0 + exp(s_q4 - m));
     if (c.out.d_cn) c.out.d_cn[ai] = s_d4;
   }

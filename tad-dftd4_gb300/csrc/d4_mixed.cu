@@ -90,6 +90,18 @@ __global__ void tables32_kernel(Ctx c) {
     c.w.pairA[t] = A;
     c.w.pairB[t] = Bq;
   }
+  if (t < MAX_ELEM_ID * MAX_ELEM_ID) {  // CN pair constants in FP64, kept as double-floats
+    // (an FP32 rounding of them would shift every pair of an element pair the
+    // same way: a bias that adds up over the structure instead of averaging out)
+    const int za = t / MAX_ELEM_ID, zb = t % MAX_ELEM_ID;
+    float4 v = make_float4(0.f, 0.f, 0.f, 0.f);
+    if (za < c.tab.n_elem && zb < c.tab.n_elem && za > 0 && zb > 0) {
+      const dfl a = df_from(1.0 / (c.tab.cov_d3[za] + c.tab.cov_d3[zb]));
+      const dfl e = df_from(en_factor(c.tab.en[za], c.tab.en[zb], c.par.k4, c.par.k5, c.par.k6));
+      v = make_float4(a.hi, a.lo, e.hi, e.lo);
+    }
+    c.w.cnpair[t] = v;
+  }
   if (t < MAX_ELEM_ID * MAX_ELEM_ID) {  // 1 / sqrt(rad_a^2 + rad_b^2)
     const int za = t / MAX_ELEM_ID, zb = t % MAX_ELEM_ID;
     dfl g = {0.f, 0.f};
@@ -144,9 +156,13 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
     const float4 *R = c.w.ref32 + zi * NREF;
     const float *Z0L = c.w.z0lo + zi * NREF;
     float4 rv[NREF];
-    float dcn[NREF], cf[NREF], dq[NREF];
+    float dcn[NREF], cf[NREF], dq[NREF], ua[NREF], zq[NREF];
     double y64[NREF];
     double best = INFINITY;
+    // charge scaling argument gam gc (q - q_ref) / (q + zeff) in FP64, rounded
+    // once (an FP32-rounded gam would bias every atom of the element alike)
+    const double qmod64 = q + (double)c.tab.zeff[zi];
+    const double gam64 = c.tab.gam[zi] * c.cfg.gc;
 #pragma unroll
     for (int r = 0; r < NREF; ++r) {
       rv[r] = R[r];
@@ -158,6 +174,13 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       dcn[r] = (float)d;
       cf[r] = (float)cfr;
       dq[r] = (float)(q - c.tab.refq[zi * NREF + r]);
+      // zeta(q) = exp(-ga expm1(u)) with the outer exponential in FP64,
+      // rounded once: FP32 expf carries a mean relative error of ~+5e-9,
+      // which C6 ~ zeta_i zeta_j would double into a bias shared by every pair
+      // of the structure (expm1f's error is scaled down by u ~ 0.1 there)
+      const double u64 = qmod64 > 0.0 ? gam64 * (q - c.tab.refq[zi * NREF + r]) / qmod64 : 0.0;
+      ua[r] = (float)u64;
+      zq[r] = (float)exp(-c.cfg.ga * (double)expm1f((float)u64));
       if (refc > 0) best = fmin(best, y64[r]);
     }
     if (best < INFINITY) {
@@ -194,8 +217,8 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
         float z, dz;
         if (qmod > 0.f) {
           // model/base.py:308-335 as exp(-ga expm1(gam (q - q_ref) / (q + zeff)))
-          const float em1 = expm1f(gam * dq[r] / qmod);
-          z = expf(-ga * em1);
+          const float em1 = expm1f(ua[r]);
+          z = zq[r];
           dz = -ga * z * (1.f + em1) * gam * rv[r].y / (qmod * qmod);
         } else {
           z = expf(ga);
@@ -247,8 +270,11 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
 // ---------------------------------------------------------------- CN
 
 // D4 and EEQ coordination numbers in FP32 (precision form): the counting
-// function as 1/2 erfc(x) (no cancellation for small counts), compensated
-// per-lane sums, FP64 per-atom totals and the smooth EEQ cap in FP64.
+// function as 1/2 erfc(x) (no cancellation for small counts) with
+// x = kcn (r / r0 - 1) from 1/r0 as a double-float per element pair, the EN
+// factor as a double-float per element pair (no FP32-rounded constant), and
+// compensated per-lane sums; FP64 per-atom totals and the smooth EEQ cap in
+// FP64.
 __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
   const int b = blockIdx.y;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
@@ -270,23 +296,23 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *PL = c.w.pos32lo + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
-  const float4 pi = P[i], li = PL[i], xi = X[i];
-  const float kcn = c.pf.kcn, k4 = c.pf.k4, k5 = c.pf.k5, k6 = c.pf.k6;
+  const float4 pi = P[i], li = PL[i];
+  const float kcn = c.pf.kcn;
   const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
+  const float4 *CP = c.w.cnpair + (size_t)zi * MAX_ELEM_ID;
   Acc32 s_d4, s_q;
   for (int j = lane; j < n; j += 32) {
-    if (j == i || c.w.z[(size_t)b * N + j] == 0) continue;
-    const float4 pj = P[j], xj = X[j];
+    const int zj = c.w.z[(size_t)b * N + j];
+    if (j == i || zj == 0) continue;
+    const float4 pj = P[j];
+    const float4 cp = CP[zj];
     const float3 d = pos_diff(pi, li, pj, PL[j]);
     const float dx = d.x, dy = d.y, dz = d.z;
     const float r = sqrtf(dx * dx + dy * dy + dz * dz);
-    const float x = kcn * (r / (xi.x + xj.x) - 1.0f);
+    const float x = kcn * fmaf(r, cp.y, fmaf(r, cp.x, -1.0f));  // kcn (r / r0 - 1)
     if (x > 9.0f) continue;  // erfc(9) / 2 < 1e-36
     const float cf = 0.5f * erfcf(x);
-    if (r <= cut_cn) {
-      const float t = fabsf(xi.y - xj.y) + k5;
-      s_d4.add(k4 * __expf(-(t * t) / k6) * cf);
-    }
+    if (r <= cut_cn) s_d4.add(fmaf(cf, cp.z, cf * cp.w));
     if (r <= cut_q) s_q.add(cf);
   }
   // FP32 warp reductions of the compensated per-lane sums (hi and lo apart)
@@ -298,7 +324,9 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
     c.w.cn[ai] = d4;
     // log(1 + e^m) - log(1 + e^(m - q)) = log1p(expm1(q) / (1 + e^(q - m))):
     // no cancellation, FP32 relative accuracy also for small q (the EEQ
-    // right-hand side takes its square root, which is steep near 0)
+    // right-hand side takes its square root, which is steep near 0).  Its
+    // FP32 rounding differs from atom to atom and averages out in the
+    // energies; the FP64 form would cost an FP64 pass per atom.
     const float t = 1.0f + expf(q - m);
     c.w.cnq[ai] = (double)log1pf(expm1f(q) / t);
     c.w.dcnq[ai] = (double)(1.0f / t);
@@ -347,7 +375,6 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   const int slot_i = c.w.slot[ai];
   float4 *T = c.w.ptf + (size_t)ai * N;
   float4 *Tda = PGRAD ? c.w.ptf_da + (size_t)ai * N : nullptr;
-  const float alp3_log2e = c.pf.alp3 * 1.4426950408889634f;
   // R0 = a1 sqrt(qq) + a2, qq = 3 r4r2_i r4r2_j, R0^6 and R0^8 as
   // double-floats, so that no FP32 rounding of a per-element-pair constant
   // biases every pair of that element pair the same way: from the per-call
@@ -381,7 +408,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
       const float3 d = pos_diff(pi, li, pj, PL[j]);
       const float dx = d.x, dy = d.y, dz = d.z;
       const float r2 = dx * dx + dy * dy + dz * dz;
-      const float ir = rsqrtf(r2);
+      const float ir = __frcp_rn(sqrtf(r2));  // correctly rounded: no bias in the ATM records
       const float r = r2 * ir;
       const float *Aj = c.w.A32 + a32_index(b, j, slot_i, 0, N, c.S);
       const float *A0j = c.w.A032 + a32_index(b, j, slot_i, 0, N, c.S);
@@ -411,7 +438,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
       const float R0 = R0d.hi, sqq = sqrtf(qqd.hi);
       const float lnR0r = logf(R0 * ir) + R0d.lo / R0;
       const float ir2 = __frcp_rn(r2);
-      T[j] = make_float4(r2, ir2, exp2f(alp3_log2e * lnR0r), sqrtf(c60) * (ir * ir2));
+      T[j] = make_float4(r2, ir2, expf(c.pf.alp3 * lnR0r), sqrtf(c60) * (ir * ir2));
       r2mx = fmaxf(r2mx, r2);
       if (PGRAD) Tda[j] = make_float4(sqq / R0, 1.0f / R0, lnR0r, 0.f);
       if (r <= cut2) {
@@ -1663,32 +1690,31 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
   const int n = c.w.n_eff[b];
   if (i >= n || zi == 0) return;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
-  const float kcn = c.pf.kcn, k4 = c.pf.k4, k5 = c.pf.k5, k6 = c.pf.k6;
+  const float kcn = c.pf.kcn;
   const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *X = c.w.aux32 + (size_t)b * N;
   const float4 *D = c.w.adj32 + (size_t)b * N;
   const float4 *PL = c.w.pos32lo + (size_t)b * N;
   const float4 pi = P[i], li = PL[i], xi = X[i], di = D[i];
+  const float4 *CP = c.w.cnpair + (size_t)zi * MAX_ELEM_ID;
   Acc32 gx, gy, gz;
   for (int j = lane; j < n; j += 32) {
     const size_t aj = (size_t)b * N + j;
-    if (j == i || c.w.z[aj] == 0) continue;
+    const int zj = c.w.z[aj];
+    if (j == i || zj == 0) continue;
     const float4 pj = P[j], xj = X[j], dj = D[j];
+    const float4 cp = CP[zj];
     const float3 d = pos_diff(pi, li, pj, PL[j]);
     const float dx = d.x, dy = d.y, dz = d.z;
     const float r2 = dx * dx + dy * dy + dz * dz;
     const float ir = rsqrtf(r2);
     const float r = r2 * ir;
     float dEdr = 0.f;
-    const float r0 = xi.x + xj.x;
-    const float xx = kcn * (r / r0 - 1.0f);
+    const float xx = kcn * fmaf(r, cp.y, fmaf(r, cp.x, -1.0f));  // kcn (r / r0 - 1)
     if (xx < 9.0f) {
-      const float dcf = -kcn / r0 * INV_SQRT_PI_F * __expf(-xx * xx);
-      if (r <= cut_cn) {
-        const float t = fabsf(xi.y - xj.y) + k5;
-        dEdr += (di.x + dj.x) * k4 * __expf(-(t * t) / k6) * dcf;
-      }
+      const float dcf = -kcn * cp.x * INV_SQRT_PI_F * __expf(-xx * xx);
+      if (r <= cut_cn) dEdr += (di.x + dj.x) * (cp.z + cp.w) * dcf;
       if (eeq && r <= cut_q) dEdr += (di.y + dj.y) * dcf;
     }
     if (eeq) {

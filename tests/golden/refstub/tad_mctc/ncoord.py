@@ -13,7 +13,8 @@ from .data import COV_D3, PAULING_EN
 
 
 def erf_count(rij, r0, kcn=7.5):
-    return 0.5 * (1.0 + torch.erf(-kcn * (rij / r0 - 1.0)))
+    # 1/2 (1 + erf(-x)) written as 1/2 erfc(x): no cancellation for x >> 1
+    return 0.5 * torch.erfc(kcn * (rij / r0 - 1.0))
 
 
 def _pairs(numbers, positions):
@@ -43,8 +44,10 @@ def cn_eeq(numbers, positions, *, cutoff=25.0, cn_max=8.0, kcn=7.5):
     r0 = rc[..., :, None] + rc[..., None, :]
     keep = mask & (r <= cutoff)
     cn = torch.sum(torch.where(keep, erf_count(r, r0, kcn), 0.0), dim=-1)
+    # smooth cap log(1 + e^max) - log(1 + e^(max - cn)), written without the
+    # cancellation of the two logarithms for cn << 1
     cmax = torch.tensor(cn_max, **dd)
-    return torch.log1p(torch.exp(cmax)) - torch.log1p(torch.exp(cmax - cn))
+    return torch.log1p(torch.expm1(cn) / (1.0 + torch.exp(cn - cmax)))
 
 
 def cn_d3(numbers, positions, **kwargs):  # pragma: no cover - not on this path

@@ -348,7 +348,7 @@ def _oracle_with_scale(numbers, positions, charge, param, model="d4"):
     pos = positions.clone().requires_grad_(True)
     e, parts = oracle.dftd4(numbers, pos, charge, param, model=model, return_parts=True)
     (g,) = torch.autograd.grad(e.sum(), pos)
-    return e.detach().numpy(), g.numpy(), parts["scale"].numpy()
+    return e.detach().numpy(), g.numpy(), parts["scale"].detach().numpy()
 
 
 @pytest.mark.parametrize("model", ["d4", "d4s"])
