@@ -188,7 +188,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
   float gacc[NFREQ];
 #pragma unroll
   for (int w = 0; w < NFREQ; ++w) gacc[w] = 0.f;
-  float r2mx = 0.f;  // largest r^2 of this thread's pairs (the ATM's all-inside test)
+  float r2mx = 0.f;  // largest r^2 of this thread's pairs (the ATM's far-atom test)
 
   constexpr uint32_t IDESC = tc::idesc_tf32(TC_M, TC_NJ);
   const uint32_t a_base = tc::smem_u32(&S.a[0][0]);
@@ -397,8 +397,7 @@ __global__ void __launch_bounds__(TC_THREADS, 2) pair_fwd_tc_kernel(Ctx c) {
     tc::fence_before_sync();
     __syncthreads();  // chunk buffers and tensor memory are free again
   }
-  r2mx = warp_maxf(r2mx);
-  if ((tid & 31) == 0 && r2mx > 0.f) atomicMax(&c.w.atm_r2max[b], __float_as_uint(r2mx));
+  if (real && r2mx > 0.f) atomicMax(&c.w.atm_rowmax[ai], __float_as_uint(r2mx));
   if (timed_out) {
     // an MMA batch did not complete in time: report it, give the tensor
     // cores one more bounded wait, release the tensor memory and leave

@@ -157,8 +157,9 @@ struct Workspace {
                     // neighbour-triple ATM)
   int *sorder;      // [B] structures by decreasing n_eff (launch order of the
                     // per-structure kernels of the precision form)
-  unsigned *atm_r2max;  // [B] largest r^2 over the real pairs of each structure
-                        // (FP32 bits; written by the pair kernels of the precision form)
+  unsigned *atm_rowmax;  // [B*N] largest r^2 over the real pairs of each atom (FP32
+                         // bits; zeroed by the CN kernel, raised by the pair kernels of
+                         // the precision form)
   size_t bytes;
 };
 
@@ -228,7 +229,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   if (mixed) {
     w.adj32 = (float4 *)take(16 * BN);
     w.sorder = (int *)take(sizeof(int) * (size_t)B);
-    w.atm_r2max = (unsigned *)take(sizeof(unsigned) * (size_t)B);
+    w.atm_rowmax = (unsigned *)take(sizeof(unsigned) * BN);
     w.prS32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.prP32 = grad ? (float *)take(4 * BNN) : nullptr;
     w.eeq_hi = (float *)take(4 * BNN);

@@ -284,6 +284,7 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
   if (i >= N) return;
   const size_t ai = (size_t)b * N + i;
   const int zi = c.w.z[ai];
+  if (lane == 0) c.w.atm_rowmax[ai] = 0u;  // the pair kernels raise it
   if (i >= n || zi == 0) {
     if (lane == 0) {
       c.w.cn[ai] = 0.0;
@@ -389,7 +390,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   const float rho6 = p.s6 != 0.0 ? 1.f : 0.f;
   Acc32 e_acc, e8_acc, gx, gy, gz;
   float pg[5] = {0.f, 0.f, 0.f, 0.f, 0.f};
-  float r2mx = 0.f;  // largest r^2 of this atom's pairs (the ATM's all-inside test)
+  float r2mx = 0.f;  // largest r^2 of this atom's pairs (the ATM's far-atom test)
   for (int s = 0; s < nslot; ++s) {
     if (lane < NFREQ) {  // A' already carries sqrt((3/pi) w): C6 = sum_w A'_i A'_j
       const size_t o = a32_index(b, i, s, lane, N, c.S);
@@ -499,7 +500,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
     for (int s = nslot; s < c.S; ++s) c.w.G32[(ai * c.S + s) * NFREQ + lane] = 0.f;
   const Acc32 ea = warp_sum_acc(e_acc), ea8 = warp_sum_acc(e8_acc);
   r2mx = warp_maxf(r2mx);
-  if (lane == 0) atomicMax(&c.w.atm_r2max[b], __float_as_uint(r2mx));
+  if (lane == 0 && r2mx > 0.f) atomicMax(&c.w.atm_rowmax[ai], __float_as_uint(r2mx));
   if (PGRAD) {
     float v[5];
 #pragma unroll
@@ -536,7 +537,6 @@ __global__ void __launch_bounds__(1024) size_order_kernel(Ctx c) {
   extern __shared__ unsigned long long s_ord[];
   const int B = c.B;
   const int tid = threadIdx.x;
-  for (int t = tid; t < B; t += blockDim.x) c.w.atm_r2max[t] = 0u;  // the pair kernels raise it
   if (B > SORDER_MAX) {
     for (int t = tid; t < B; t += blockDim.x) c.w.sorder[t] = t;
     return;
@@ -962,13 +962,21 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
 
 // ---------------------------------------------------------------- ATM, register-tiled
 
-// Shared-memory ATM (n <= 234) for structures whose real pairs all lie
-// inside the three-body cutoff (the pair kernels record each structure's
-// largest r^2), with no padding below the last real atom and unit atom
-// weights: every triple then carries the full mask, so the attribution
-// weights are 1 and the atom energies follow from the pair sums,
-// E_x = sum_y P(x, y) (each triple reaches x through two pairs; the same
-// total as the per-triple attribution eu / 3 per atom).
+// Shared-memory ATM (n <= 234) for structures with no padding below the
+// last real atom and unit atom weights.  A triple whose three pairs lie
+// inside the three-body cutoff has attribution weight 1, and the atom
+// energies follow from the pair sums, E_x = sum_y P(x, y) (each triple
+// reaches x through two pairs; the same total as the per-triple attribution
+// eu / 3 per atom).  Triples with a pair beyond the cutoff are only possible
+// where one of the three atoms is "far" (its largest pair r^2, recorded by
+// the pair kernels, exceeds the cutoff): steps and tasks that touch a far
+// atom run the masked variant, which weights each triple by
+// (f_ij f_ik + f_ij f_jk + f_ik f_jk) / 3 (f: pair inside the cutoff; 1, 1/3
+// or 0) and corrects the atom energies of the 1/3 triples, whose pair sums
+// alone do not give the reference attribution (in these units the atom of
+// both inside pairs gets 0, the other two eu each, while the pair sums give
+// each 2 eu / 3): -2 eu / 3 to the common atom and +eu / 3 to the other two,
+// accumulated beside the row sums.
 //
 // A warp task is a tile of AT_C = 8 consecutive middle atoms j (j0 .. j0+7)
 // and a chunk of 8 outer atoms k > j.  Lane (q, l) = (lane / 8, lane % 8)
@@ -980,12 +988,14 @@ __global__ void __launch_bounds__(PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS)
 // (i, k) sums to shared memory once, and the group reduce-scatters its
 // sixteen (i, j) sums over its eight lanes.  8 x 8 tiles keep the triples
 // evaluated outside i < j < k at ~22 % for sizes 8..200 (8 x 32: ~50 %).
-// The triple arithmetic is that of atm_task with the weights at 1.
+// The triple arithmetic is that of atm_task with unit atom weights.
 // Structures outside these conditions run atm_task in the same kernel.
 constexpr int AT_C = 8;             // middle atoms per task (and outer atoms per chunk)
-constexpr int AT_THREADS = 768;     // 24 warps at 80 registers (measured: 512 threads
-                                    // at 128 registers, no spills, 4 % slower)
+constexpr int AT_THREADS = 512;     // 16 warps at 128 registers, no spills (measured on
+                                    // batch512: 768 threads at 80 registers spill and run
+                                    // 13 % slower, 640 at 96 registers 10 % slower)
 constexpr int AT_TASKS_MAX = 900;   // tiles x chunks for n <= 237 (30 x 30)
+constexpr int AT_FAR_WORDS = 8;     // far-atom bits for n <= 256
 // Triples per CTA: 600000 for batches of 512 structures and more (measured
 // best for batch512: 300000 -> 4 % slower, 1200000 -> 2x slower from the
 // largest CTAs), fewer for smaller batches so that they still fill the GPU.
@@ -1022,13 +1032,26 @@ __device__ __forceinline__ void lane_halving(float (&v)[NV]) {
   }
 }
 
+// Per-structure state of the tiled ATM: shared accumulators, the far-atom
+// bit set, the cutoff and the damping exponent.
+struct AtTile {
+  const float4 *__restrict__ T;
+  float *sS, *sP, *sE;
+  const unsigned *far;  // bit x: atom x has a pair beyond the three-body cutoff
+  float cut2, alp3h;
+  int n, N;
+  __device__ __forceinline__ bool is_far(int x) const {
+    return x < n && ((far[x >> 5] >> (x & 31)) & 1u) != 0u;
+  }
+};
+
 // One step of a tile task: inner atom i of this lane's group.  GUARD: some
 // (i, j) of the step are not pairs (i >= j, j beyond the structure, i
-// beyond the task's range).
-template <bool GRAD, bool GUARD>
-__device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, float *sS, float *sP,
-                                              int n, int N, int j0, int jend, int k, bool kok,
-                                              int i, float alp3h, const float (&zjk)[AT_C],
+// beyond the task's range).  MASK: a far atom takes part, so each triple
+// carries its cutoff weight and the 1/3 triples their energy corrections.
+template <bool GRAD, bool GUARD, bool MASK>
+__device__ __forceinline__ void atm_tile_step(const AtTile &a, int j0, int jend, int k, bool kok,
+                                              int i, const float (&zjk)[AT_C],
                                               const float (&izjk)[AT_C],
                                               const float (&ejk)[AT_C],
                                               const float (&qjk)[AT_C], float (&Sjk)[AT_C],
@@ -1036,9 +1059,10 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
   const int l = threadIdx.x & 7;
   const float4 zero4 = make_float4(0.f, 0.f, 0.f, 0.f);
   const bool iok = !GUARD || i < jend - 1;
-  const float4 *Ti = T + (size_t)(iok ? i : 0) * N;
+  const float4 *Ti = a.T + (size_t)(iok ? i : 0) * a.N;
   const bool lk = iok && kok && k > i;
   const float4 pik = lk ? Ti[k] : zero4;
+  const bool fik = !MASK || pik.x <= a.cut2;
   float Sik = 0.f, Pik = 0.f;
   constexpr int NV = GRAD ? 2 * AT_C : AT_C;
   float v[NV];  // (i, j) sums: dE/dr^2 (GRAD) then energies
@@ -1052,8 +1076,22 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
     } else {
       pij = Ti[j0 + t];
     }
-    const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y, pik.z, pik.w,
-                                       zjk[t], izjk[t], ejk[t], qjk[t], alp3h);
+    bool fij = true, fjk = true;
+    float qij = pij.w;
+    if (MASK) {  // cutoff weight 1, 1/3 or 0, folded into C9 / R^3
+      fij = pij.x <= a.cut2;
+      fjk = zjk[t] <= a.cut2;
+      const int m = (int)fij + (int)fik + (int)fjk;
+      qij *= m == 3 ? 1.f : (m == 2 ? (1.0f / 3.0f) : 0.f);
+    }
+    const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, qij, pik.x, pik.y, pik.z, pik.w,
+                                       zjk[t], izjk[t], ejk[t], qjk[t], a.alp3h);
+    if (MASK && !(fij & fik & fjk) && tr.eu != 0.f) {
+      // a 1/3 triple: -2 eu_w to the atom of both inside pairs, +eu_w to the others
+      atomicAdd(&a.sE[i], fjk ? tr.eu : -2.f * tr.eu);
+      atomicAdd(&a.sE[j0 + t], fik ? tr.eu : -2.f * tr.eu);
+      atomicAdd(&a.sE[k], fij ? tr.eu : -2.f * tr.eu);
+    }
     Pik += tr.eu;
     Pjk[t] += tr.eu;
     if (GRAD) {
@@ -1065,10 +1103,10 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
       v[t] = tr.eu;
     }
   }
-  const int rb = tri_row(i, n);
+  const int rb = tri_row(i, a.n);
   if (lk) {
-    if (GRAD) atomicAdd(&sS[rb + k], Sik);
-    atomicAdd(&sP[rb + k], Pik);
+    if (GRAD) atomicAdd(&a.sS[rb + k], Sik);
+    atomicAdd(&a.sP[rb + k], Pik);
   }
   // group sums over the eight lanes: lane l keeps values NV/8 l .. NV/8 l + NV/8 - 1
   lane_halving<NV, 4, 3>(v);
@@ -1077,16 +1115,39 @@ __device__ __forceinline__ void atm_tile_step(const float4 *__restrict__ T, floa
     const int idx = (NV / 8) * l + p;
     const int jt = j0 + idx % AT_C;
     if (!GUARD || (iok && jt > i && jt < jend && v[p] != 0.f))
-      atomicAdd(&((GRAD && idx < AT_C) ? sS : sP)[rb + jt], v[p]);
+      atomicAdd(&((GRAD && idx < AT_C) ? a.sS : a.sP)[rb + jt], v[p]);
   }
 }
 
+// The steps of a task over inner atoms i, i running from ib in steps of st4
+// while i < ilim: the masked step where a far atom takes part
+// (warp-uniform: any of the four groups' i), the plain one elsewhere.
+template <bool GRAD, bool GUARD>
+__device__ __forceinline__ int atm_tile_steps(const AtTile &a, bool any_far, bool task_far,
+                                              int ib, int ilim, int st4, int istep, int j0,
+                                              int jend, int k, bool kok,
+                                              const float (&zjk)[AT_C],
+                                              const float (&izjk)[AT_C],
+                                              const float (&ejk)[AT_C],
+                                              const float (&qjk)[AT_C], float (&Sjk)[AT_C],
+                                              float (&Pjk)[AT_C]) {
+  const int i_off = ((threadIdx.x & 31) >> 3) * istep;
+  for (; ib < ilim; ib += st4) {
+    const int i = ib + i_off;
+    if (any_far && (task_far || __any_sync(0xffffffffu, a.is_far(i))))
+      atm_tile_step<GRAD, GUARD, true>(a, j0, jend, k, kok, i, zjk, izjk, ejk, qjk, Sjk, Pjk);
+    else
+      atm_tile_step<GRAD, GUARD, false>(a, j0, jend, k, kok, i, zjk, izjk, ejk, qjk, Sjk, Pjk);
+  }
+  return ib;
+}
+
 template <bool GRAD>
-__device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, float *sS, float *sP,
-                                              int n, int N, int j0, int kc, int i0, int istep,
-                                              float alp3h) {
+__device__ __forceinline__ void atm_tile_task(const AtTile &a, bool any_far, int j0, int kc,
+                                              int i0, int istep) {
   const int lane = threadIdx.x & 31;
   const int q = lane >> 3;
+  const int n = a.n;
   const int k = kc + (lane & 7);
   const bool kok = k < n;
   float zjk[AT_C], izjk[AT_C], ejk[AT_C], qjk[AT_C], Sjk[AT_C], Pjk[AT_C];
@@ -1094,7 +1155,7 @@ __device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, floa
   for (int t = 0; t < AT_C; ++t) {
     const int jt = j0 + t;
     const bool ok = kok && jt < k;  // then also jt <= n - 2
-    const float4 r = ok ? T[(size_t)jt * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
+    const float4 r = ok ? a.T[(size_t)jt * a.N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
     zjk[t] = r.x;
     izjk[t] = r.y;
     ejk[t] = r.z;
@@ -1103,16 +1164,25 @@ __device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, floa
     Pjk[t] = 0.f;
   }
   const int jend = min(j0 + AT_C, n - 1);  // middle atoms j0 .. jend - 1
+  // a far middle or outer atom makes every step of the task a masked one
+  bool task_far = false;
+  if (any_far) {
+    bool mine = a.is_far(k);
+#pragma unroll
+    for (int t = 0; t < AT_C; ++t) mine |= a.is_far(j0 + t);
+    task_far = __any_sync(0xffffffffu, mine);
+  }
   // group q takes i = i0 + (4 s + q) istep, s = 0, 1, ...
   const int st4 = 4 * istep;
   int ib = i0;  // i of group 0 in this step
-  if (j0 + AT_C <= n - 1)
-    for (; ib + 3 * istep < j0; ib += st4)
-      atm_tile_step<GRAD, false>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
-                                 izjk, ejk, qjk, Sjk, Pjk);
-  for (; ib < jend - 1; ib += st4)
-    atm_tile_step<GRAD, true>(T, sS, sP, n, N, j0, jend, k, kok, ib + q * istep, alp3h, zjk,
-                              izjk, ejk, qjk, Sjk, Pjk);
+  if (j0 + AT_C <= n - 1) {
+    // plain steps while all four groups' i are below j0: ib + 3 istep < j0
+    const int ilim = j0 - 3 * istep;
+    ib = atm_tile_steps<GRAD, false>(a, any_far, task_far, ib, ilim, st4, istep, j0, jend, k,
+                                     kok, zjk, izjk, ejk, qjk, Sjk, Pjk);
+  }
+  atm_tile_steps<GRAD, true>(a, any_far, task_far, ib, jend - 1, st4, istep, j0, jend, k, kok,
+                             zjk, izjk, ejk, qjk, Sjk, Pjk);
   // (j, k) sums of the four groups: group q keeps values NV/4 q .. NV/4 q + NV/4 - 1
   constexpr int NV = GRAD ? 2 * AT_C : AT_C;
   float v[NV];
@@ -1131,14 +1201,15 @@ __device__ __forceinline__ void atm_tile_task(const float4 *__restrict__ T, floa
     const int idx = (NV / 4) * q + p;
     const int jt = j0 + idx % AT_C;
     if (kok && jt < k && v[p] != 0.f)
-      atomicAdd(&((GRAD && idx < AT_C) ? sS : sP)[tri_u(jt, k, n)], v[p]);
+      atomicAdd(&((GRAD && idx < AT_C) ? a.sS : a.sP)[tri_u(jt, k, n)], v[p]);
   }
 }
 
 template <bool GRAD>
 __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
   extern __shared__ float s_acc[];
-  __shared__ int s_next, s_ntask;
+  __shared__ int s_next, s_ntask, s_any_far;
+  __shared__ unsigned s_far[AT_FAR_WORDS];
   const int b = c.w.sorder[blockIdx.y];
   const int cta = blockIdx.x;
   const int N = c.N;
@@ -1152,10 +1223,17 @@ __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
   float *sS = s_acc, *sP = s_acc + P, *sE = s_acc + 2 * P;
   int *s_task = reinterpret_cast<int *>(s_acc + 2 * P + n);
   const float cut2 = c.pf.cut3 * c.pf.cut3;
-  const bool fast = c.w.n_real[b] == n && __uint_as_float(c.w.atm_r2max[b]) <= cut2;
+  const bool tiled = c.w.n_real[b] == n;
   for (int t = threadIdx.x; t < 2 * P + n; t += blockDim.x) s_acc[t] = 0.f;
+  if (threadIdx.x == 0) s_any_far = 0;
+  if (warp < AT_FAR_WORDS) {  // far atoms: largest pair r^2 beyond the cutoff
+    const int x = 32 * warp + lane;
+    const bool far = x < n && __uint_as_float(c.w.atm_rowmax[(size_t)b * N + x]) > cut2;
+    const unsigned m = __ballot_sync(0xffffffffu, far);
+    if (lane == 0) s_far[warp] = m;
+  }
   const int NT = (n - 2 + AT_C - 1) / AT_C;  // tiles of middle atoms 1 .. n - 2
-  if (fast && threadIdx.x < NT) {
+  if (tiled && threadIdx.x < NT) {
     // task table: tiles from the last (longest i range) to the first, the
     // chunks of eight outer atoms of each in order
     auto nch = [&](int ti) { return (n - 1 - (1 + AT_C * ti) + AT_C - 1) / AT_C; };
@@ -1169,14 +1247,26 @@ __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
     }
   }
   __syncthreads();
+  if (threadIdx.x < AT_FAR_WORDS && s_far[threadIdx.x] != 0u) s_any_far = 1;
+  __syncthreads();
   const float4 *T = c.w.ptf + (size_t)b * N * N;
-  if (fast) {
-    const float alp3h = 0.5f * c.pf.alp3;
+  if (tiled) {
+    AtTile a;
+    a.T = T;
+    a.sS = sS;
+    a.sP = sP;
+    a.sE = sE;
+    a.far = s_far;
+    a.cut2 = cut2;
+    a.alp3h = 0.5f * c.pf.alp3;
+    a.n = n;
+    a.N = N;
+    const bool any_far = s_any_far != 0;
     const int ntask = s_ntask;
     for (int task = warp; task < ntask;) {
       const int e = s_task[task];
       const int j0 = 1 + AT_C * (e >> 8);
-      atm_tile_task<GRAD>(T, sS, sP, n, N, j0, j0 + 1 + AT_C * (e & 255), cta, K, alp3h);
+      atm_tile_task<GRAD>(a, any_far, j0, j0 + 1 + AT_C * (e & 255), cta, K);
       int nx = 0;
       if (lane == 0) nx = atomicAdd(&s_next, 1);
       task = __shfl_sync(0xffffffffu, nx, 0);
@@ -1245,9 +1335,9 @@ __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
         }
       }
     }
-    if (fast) {
+    if (tiled) {
       er = warp_sumf(er);
-      if (lane == 0) sE[j] = er;
+      if (lane == 0) sE[j] += er;  // beside the 1/3-triple corrections
     }
   }
   __syncthreads();
@@ -1269,13 +1359,13 @@ __global__ void __launch_bounds__(AT_THREADS, 1) atm_tiled_kernel(Ctx c) {
         }
       }
     }
-    if (fast) {
+    if (tiled) {
       ec = warp_sumf(ec);
       const float ev = ec + sE[k];  // E_k = sum_y P(k, y)
       if (lane == 0 && ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + k], (double)ev * escale);
     }
   }
-  if (!fast)
+  if (!tiled)
     for (int x = threadIdx.x; x < n; x += blockDim.x) {
       const float ev = sE[x];
       if (ev != 0.f) atomicAdd(&c.w.e3[(size_t)b * N + x], (double)ev * escale);

@@ -252,16 +252,19 @@ def test_neighbour_triple_atm_matches_dense_fp64_path(d4):
     assert (gm - gp).abs().max().item() <= F_TOL
 
 
-@pytest.mark.parametrize("cut3", [40.0, 12.0])
+@pytest.mark.parametrize("cut3", [40.0, 20.0, 12.0])
 @pytest.mark.parametrize("gradient", [True, False])
 def test_atm_tiles_and_per_triple_fallback_match_fp64(d4, cut3, gradient):
-    """The shared-memory ATM evaluates structures whose real pairs all lie
-    inside disp3 with register tiles of eight middle atoms (unit attribution
-    weights, atom energies from the pair sums); structures with a pair beyond
-    disp3 or padding below their last atom take the per-triple masks in the
-    same kernel.  disp3 = 40 Bohr: most structures tiled; 12 Bohr: most per
-    triple.  Energies (per structure and per atom) and forces match the
-    plain FP64 path within the precision bar, with and without gradients."""
+    """The shared-memory ATM evaluates gapless structures with register tiles
+    of eight middle atoms: plain steps (unit attribution weights, atom
+    energies from the pair sums) where no atom of the step has a pair beyond
+    disp3, masked steps (weights 1, 1/3, 0 and the energy corrections of the
+    1/3 triples) where one has; structures with padding below their last
+    atom take the per-triple masks in the same kernel.  disp3 = 40 Bohr: a
+    few far atoms in the largest structures; 20 Bohr: plain and masked steps
+    mixed; 12 Bohr: nearly every step masked.  Energies (per structure and
+    per atom) and forces match the plain FP64 path within the precision bar,
+    with and without gradients."""
     from importlib import import_module
     disp = import_module("tad-dftd4_gb300.disp")
     wl = package().workloads
