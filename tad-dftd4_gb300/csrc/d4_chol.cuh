@@ -15,8 +15,13 @@ constexpr unsigned FULL = 0xffffffffu;
 // r; rows beyond the matrix are padded with the identity), then the inverse
 // of the factor (lane c computes column c), which replaces the block in
 // place: the panel and the triangular solves only need the inverse.  A
-// non-positive pivot sets *bad and goes on with pivot 1.
+// non-positive pivot sets *bad and goes on with pivot 1.  The inverse runs
+// column-oriented (x_k /= L_kk, then x_r -= L_rk x_k for all r > k: 32 short
+// steps whose updates are independent) with the pivots' reciprocals kept
+// from the factorisation, instead of 32 row sums that each wait for the
+// previous row and a division.
 static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
+  __shared__ float s_dinv[PB];
   const int r = threadIdx.x & 31;
   const bool live = r < kb;
   float *row = L + tri_index(k0 + (live ? r : 0), k0);
@@ -31,8 +36,12 @@ static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
       d = 1.f;
     }
     const float inv = rsqrtf(d);
-    if (r == c) a[c] = d * inv;
-    else if (r > c) a[c] *= inv;
+    if (r == c) {
+      a[c] = d * inv;
+      s_dinv[c] = inv;  // 1 / L_cc
+    } else if (r > c) {
+      a[c] *= inv;
+    }
 #pragma unroll
     for (int j = 0; j < PB; ++j) {
       if (j > c) {
@@ -45,22 +54,20 @@ static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
   for (int j = 0; j < PB; ++j)
     if (live && j <= r) row[j] = a[j];
   __syncwarp();
-  // inverse: X[rr][c] = -(sum_{k=c}^{rr-1} L[rr][k] X[k][c]) / L[rr][rr]; x = column c
+  // inverse, column c = lane: solve L x = e_c by columns of L
   const int c = r;
   float x[PB];
 #pragma unroll
-  for (int rr = 0; rr < PB; ++rr) {
-    x[rr] = 0.f;
-    if (rr < kb) {
-      const float *lr = L + tri_index(k0 + rr, k0);
-      float acc0 = 0.f, acc1 = 0.f;
+  for (int rr = 0; rr < PB; ++rr) x[rr] = rr == c ? 1.f : 0.f;
 #pragma unroll
-      for (int k = 0; k < rr; ++k) {
-        if (k & 1) acc1 = fmaf(lr[k], x[k], acc1);
-        else acc0 = fmaf(lr[k], x[k], acc0);
+  for (int k = 0; k < PB; ++k) {
+    x[k] *= s_dinv[k];
+#pragma unroll
+    for (int rr = 0; rr < PB; ++rr) {  // static bounds: x stays in registers
+      if (rr > k) {
+        const float lrk = rr < kb ? L[tri_index(k0 + rr, k0) + k] : 0.f;
+        x[rr] = fmaf(-lrk, x[k], x[rr]);
       }
-      const float dii = 1.0f / lr[rr];
-      x[rr] = rr == c ? dii : (rr > c ? -(acc0 + acc1) * dii : 0.f);
     }
   }
   __syncwarp();
@@ -95,18 +102,32 @@ static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *ba
     if (warp == 0) chol_diag_block(L, k0, kb, bad);
     __syncthreads();
     const int t0 = k0 + kb;
-    // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T
-    for (int i = t0 + warp; i < m; i += nw) {
-      float *row = L + tri_index(i, k0);
-      float v = 0.f;
-      if (lane < kb) {
-        const float *xc = L + tri_index(k0 + lane, k0);
-        for (int cc = 0; cc <= lane; ++cc) v = fmaf(row[cc], xc[cc], v);
-      }
-      __syncwarp();
-      if (lane < kb) {
-        row[lane] = v;
-        if (PT) PT[lane * ldp + (i - t0)] = v;
+    // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T; the
+    // lane's row of X stays in registers, the row of A21 is read broadcast,
+    // four independent partial sums
+    if (t0 < m) {
+      float xr[PB];
+      const float *xc = L + tri_index(k0 + (lane < kb ? lane : 0), k0);
+#pragma unroll
+      for (int cc = 0; cc < PB; ++cc) xr[cc] = (lane < kb && cc <= lane) ? xc[cc] : 0.f;
+      for (int i = t0 + warp; i < m; i += nw) {
+        float *row = L + tri_index(i, k0);
+        float v0 = 0.f, v1 = 0.f, v2 = 0.f, v3 = 0.f;
+#pragma unroll
+        for (int cc = 0; cc < PB; cc += 4) {
+          const float r0 = cc < kb ? row[cc] : 0.f, r1 = cc + 1 < kb ? row[cc + 1] : 0.f;
+          const float r2 = cc + 2 < kb ? row[cc + 2] : 0.f, r3 = cc + 3 < kb ? row[cc + 3] : 0.f;
+          v0 = fmaf(r0, xr[cc], v0);
+          v1 = fmaf(r1, xr[cc + 1], v1);
+          v2 = fmaf(r2, xr[cc + 2], v2);
+          v3 = fmaf(r3, xr[cc + 3], v3);
+        }
+        const float v = (v0 + v1) + (v2 + v3);
+        __syncwarp();
+        if (lane < kb) {
+          row[lane] = v;
+          if (PT) PT[lane * ldp + (i - t0)] = v;
+        }
       }
     }
     __syncthreads();
@@ -201,11 +222,17 @@ static __device__ void fwd_solve_blocked(const float *L, float *v, int ldv, int 
     const int kb = min(PB, m - k0);
     if (warp < nr) {
       float *vr = v + warp * ldv + k0;
-      float z = 0.f;
-      if (lane < kb) {
-        const float *xr = L + tri_index(k0 + lane, k0);
-        for (int cc = 0; cc <= lane; ++cc) z = fmaf(xr[cc], vr[cc], z);
+      const float *xr = L + tri_index(k0 + (lane < kb ? lane : 0), k0);
+      float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < PB; cc += 4) {
+        const bool ok = lane < kb;
+        z0 = fmaf(ok && cc <= lane ? xr[cc] : 0.f, cc < kb ? vr[cc] : 0.f, z0);
+        z1 = fmaf(ok && cc + 1 <= lane ? xr[cc + 1] : 0.f, cc + 1 < kb ? vr[cc + 1] : 0.f, z1);
+        z2 = fmaf(ok && cc + 2 <= lane ? xr[cc + 2] : 0.f, cc + 2 < kb ? vr[cc + 2] : 0.f, z2);
+        z3 = fmaf(ok && cc + 3 <= lane ? xr[cc + 3] : 0.f, cc + 3 < kb ? vr[cc + 3] : 0.f, z3);
       }
+      const float z = (z0 + z1) + (z2 + z3);
       __syncwarp();
       if (lane < kb) vr[lane] = z;
     }
@@ -215,9 +242,15 @@ static __device__ void fwd_solve_blocked(const float *L, float *v, int ldv, int 
       const int r = t / rows, i = k0 + kb + t % rows;
       const float *row = L + tri_index(i, 0) + k0;
       const float *xv = v + r * ldv + k0;
-      float acc = 0.f;
-      for (int cc = 0; cc < kb; ++cc) acc = fmaf(row[cc], xv[cc], acc);
-      v[r * ldv + i] -= acc;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < PB; cc += 4) {
+        if (cc < kb) a0 = fmaf(row[cc], xv[cc], a0);
+        if (cc + 1 < kb) a1 = fmaf(row[cc + 1], xv[cc + 1], a1);
+        if (cc + 2 < kb) a2 = fmaf(row[cc + 2], xv[cc + 2], a2);
+        if (cc + 3 < kb) a3 = fmaf(row[cc + 3], xv[cc + 3], a3);
+      }
+      v[r * ldv + i] -= (a0 + a1) + (a2 + a3);
     }
     __syncthreads();
   }
@@ -230,9 +263,21 @@ static __device__ void bwd_solve_blocked(const float *L, float *v, int ldv, int 
     const int kb = min(PB, m - k0);
     if (warp < nr) {
       float *vr = v + warp * ldv + k0;
-      float z = 0.f;
-      if (lane < kb)
-        for (int cc = lane; cc < kb; ++cc) z = fmaf(L[tri_index(k0 + cc, k0 + lane)], vr[cc], z);
+      float z0 = 0.f, z1 = 0.f, z2 = 0.f, z3 = 0.f;
+      const int cl = lane < kb ? lane : 0;
+#pragma unroll
+      for (int cc = 0; cc < PB; cc += 4) {
+        // column `lane` of the block inverse: rows cc >= lane
+        const bool o0 = lane < kb && cc >= lane && cc < kb;
+        const bool o1 = lane < kb && cc + 1 >= lane && cc + 1 < kb;
+        const bool o2 = lane < kb && cc + 2 >= lane && cc + 2 < kb;
+        const bool o3 = lane < kb && cc + 3 >= lane && cc + 3 < kb;
+        z0 = fmaf(o0 ? L[tri_index(k0 + cc, k0 + cl)] : 0.f, o0 ? vr[cc] : 0.f, z0);
+        z1 = fmaf(o1 ? L[tri_index(k0 + cc + 1, k0 + cl)] : 0.f, o1 ? vr[cc + 1] : 0.f, z1);
+        z2 = fmaf(o2 ? L[tri_index(k0 + cc + 2, k0 + cl)] : 0.f, o2 ? vr[cc + 2] : 0.f, z2);
+        z3 = fmaf(o3 ? L[tri_index(k0 + cc + 3, k0 + cl)] : 0.f, o3 ? vr[cc + 3] : 0.f, z3);
+      }
+      const float z = (z0 + z1) + (z2 + z3);
       __syncwarp();
       if (lane < kb) vr[lane] = z;
     }
@@ -240,9 +285,15 @@ static __device__ void bwd_solve_blocked(const float *L, float *v, int ldv, int 
     for (int t = tid; t < k0 * nr; t += nt) {
       const int r = t / k0, i = t % k0;
       const float *xv = v + r * ldv + k0;
-      float acc = 0.f;
-      for (int cc = 0; cc < kb; ++cc) acc = fmaf(L[tri_index(k0 + cc, i)], xv[cc], acc);
-      v[r * ldv + i] -= acc;
+      float a0 = 0.f, a1 = 0.f, a2 = 0.f, a3 = 0.f;
+#pragma unroll
+      for (int cc = 0; cc < PB; cc += 4) {
+        if (cc < kb) a0 = fmaf(L[tri_index(k0 + cc, i)], xv[cc], a0);
+        if (cc + 1 < kb) a1 = fmaf(L[tri_index(k0 + cc + 1, i)], xv[cc + 1], a1);
+        if (cc + 2 < kb) a2 = fmaf(L[tri_index(k0 + cc + 2, i)], xv[cc + 2], a2);
+        if (cc + 3 < kb) a3 = fmaf(L[tri_index(k0 + cc + 3, i)], xv[cc + 3], a3);
+      }
+      v[r * ldv + i] -= (a0 + a1) + (a2 + a3);
     }
     __syncthreads();
   }

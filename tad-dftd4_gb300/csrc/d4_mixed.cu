@@ -14,7 +14,6 @@
 namespace d4 {
 
 constexpr float INV_SQRT_PI_F = 0.564189583547756f;
-constexpr float SQRT3_F = 1.7320508075688772f;
 constexpr int ATM_CTA_TRIPLES = 300000;  // target triples per ATM CTA
 constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
 constexpr int ATM_THREADS = 1024;       // 32 warps: one CTA per SM (shared memory)
@@ -131,6 +130,15 @@ __device__ __forceinline__ size_t a32_index(int b, int i, int s, int w, int N, i
 // reference's FP64 norm underflows (every |dcn| > 11) it falls back to the
 // reference of largest refcovcn (model/d4.py:209-217), which is then also
 // the nearest one, so both give the same weights.
+//
+// The nearest reference's weight is never rounded: near 1 it would be
+// 1 - t with t spread over many decades, and FP32 rounds most such values
+// the same way (up to 1), so the weights of every atom would sum to slightly
+// more than 1 -- a bias that C6 ~ w_i w_j turns into a relative energy
+// shift of ~1e-8 shared by the whole structure.  A is assembled as
+// zeta_n alpha_n + sum_{r != n} gw_r (zeta_r alpha_r - zeta_n alpha_n), the
+// first term as a double-float, the corrections in FP32 (exact in the limit
+// of one reference, no value near 1 rounded).
 __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
   const int b = blockIdx.y;
   const int S = c.S, N = c.N;
@@ -141,7 +149,12 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
   const int zi = c.w.z[ai];
   const bool grad = c.w.dA32 != nullptr;
   const bool live = i < c.w.n_eff[b] && zi != 0 && s < c.w.n_slots[b];
+  // gq / g0: coefficients of the corrections (gw_r zeta_r for r != n,
+  // -G zeta_n with G = sum_{r != n} gw_r for the nearest reference n);
+  // zn / z0n: zeta of n at q and at q = 0 (double-floats) times weight 1
   float gq[NREF], g0[NREF], dgc[NREF], dgq[NREF], dg0[NREF];
+  int rn = 0;
+  float zn = 0.f, z0n = 0.f, z0nl = 0.f;
 #pragma unroll
   for (int r = 0; r < NREF; ++r) gq[r] = g0[r] = dgc[r] = dgq[r] = dg0[r] = 0.f;
   if (live) {
@@ -156,7 +169,7 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
     const float4 *R = c.w.ref32 + zi * NREF;
     const float *Z0L = c.w.z0lo + zi * NREF;
     float4 rv[NREF];
-    float dcn[NREF], cf[NREF], dq[NREF], ua[NREF], zq[NREF];
+    float dcn[NREF], cf[NREF], ua[NREF], zq[NREF];
     double y64[NREF];
     double best = INFINITY;
     // charge scaling argument gam gc (q - q_ref) / (q + zeff) in FP64, rounded
@@ -173,7 +186,6 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       y64[r] = cfr * d * d;
       dcn[r] = (float)d;
       cf[r] = (float)cfr;
-      dq[r] = (float)(q - c.tab.refq[zi * NREF + r]);
       // zeta(q) = exp(-ga expm1(u)) with the outer exponential in FP64,
       // rounded once: FP32 expf carries a mean relative error of ~+5e-9,
       // which C6 ~ zeta_i zeta_j would double into a bias shared by every pair
@@ -181,7 +193,10 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       const double u64 = qmod64 > 0.0 ? gam64 * (q - c.tab.refq[zi * NREF + r]) / qmod64 : 0.0;
       ua[r] = (float)u64;
       zq[r] = (float)exp(-c.cfg.ga * (double)expm1f((float)u64));
-      if (refc > 0) best = fmin(best, y64[r]);
+      if (refc > 0 && y64[r] < best) {
+        best = y64[r];
+        rn = r;
+      }
     }
     if (best < INFINITY) {
       float e[NREF], de[NREF];
@@ -209,6 +224,7 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       const float2 el = c.w.el32[zi];
       const float qmod = (float)q + el.x;
       const float ga = c.pf.ga, gam = el.y;
+      float G = 0.f;  // sum of the other references' weights
 #pragma unroll
       for (int r = 0; r < NREF; ++r) {
         if ((int)rv[r].z <= 0) continue;
@@ -225,18 +241,32 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
           dz = 0.f;
         }
         const float z0 = rv[r].w, z0l = Z0L[r];  // zeta(q = 0) as a double-float
-        gq[r] = z * gw;
-        g0[r] = fmaf(z0l, gw, z0 * gw);
+        if (r == rn) {
+          zn = z;
+          z0n = z0;
+          z0nl = z0l;
+        } else {
+          G += gw;
+          gq[r] = z * gw;
+          g0[r] = fmaf(z0l, gw, z0 * gw);
+        }
         dgc[r] = z * dgw;
         dgq[r] = dz * gw;
         dg0[r] = fmaf(z0l, dgw, z0 * dgw);
       }
+#pragma unroll
+      for (int r = 0; r < NREF; ++r)  // static indices: the arrays stay in registers
+        if (r == rn) {
+          gq[r] = -G * zn;
+          g0[r] = -G * (z0n + z0nl);
+        }
     }
   }
-  // A'(w) = sqrt((3/pi) w_w) sum_r g_r alpha_r(w): the Casimir-Polder weight
-  // is folded into A so that C6 = sum_w A'_i A'_j carries no rounded weight;
-  // alpha and the scale are double-floats, so the only roundings are the
-  // FP32 sums of each atom (no bias shared by all atoms of an element)
+  // A'(w) = sqrt((3/pi) w_w) A(w): the Casimir-Polder weight is folded into
+  // A so that C6 = sum_w A'_i A'_j carries no rounded weight; alpha and the
+  // scale are double-floats, the nearest reference's term zeta_n alpha_n is
+  // a double-float, and the corrections are FP32 sums (no bias shared by all
+  // atoms of an element)
   const float *al = c.w.alpha32 + (size_t)zi * NREF * NFREQ;
   const float *all = c.w.alpha32lo + (size_t)zi * NREF * NFREQ;
   for (int w = 0; w < NFREQ; ++w) {
@@ -253,10 +283,17 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       da_dq = fmaf(dgq[r], v, da_dq);
       da0_dcn = fmaf(dg0[r], v, da0_dcn);
     }
+    // the nearest reference's term, exact products as double-floats
+    const float vn = al[rn * NFREQ + w], vnl = all[rn * NFREQ + w];
+    const float bh = zn * vn, b0h = z0n * vn;
+    const dfl A = df_two_sum(bh, a);
+    const float Al = A.lo + (fmaf(zn, vn, -bh) + fmaf(zn, vnl, al_));
+    const dfl A0 = df_two_sum(b0h, a0);
+    const float A0l = A0.lo + (fmaf(z0n, vn, -b0h) + fmaf(z0nl, vn, fmaf(z0n, vnl, al0)));
     const float2 f = c.w.sfw[w];
     const size_t t = a32_index(b, i, s, w, N, S);
-    c.w.A32[t] = fmaf(a, f.x, fmaf(a, f.y, al_ * f.x));
-    c.w.A032[t] = fmaf(a0, f.x, fmaf(a0, f.y, al0 * f.x));
+    c.w.A32[t] = fmaf(A.hi, f.x, fmaf(A.hi, f.y, Al * f.x));
+    c.w.A032[t] = fmaf(A0.hi, f.x, fmaf(A0.hi, f.y, A0l * f.x));
     if (grad) {
       float *d = c.w.dA32 + 3 * ((ai * S + s) * NFREQ + w);
       d[0] = da_dcn * f.x;
@@ -296,7 +333,6 @@ __global__ void __launch_bounds__(256) cn_mixed_kernel(Ctx c) {
   }
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *PL = c.w.pos32lo + (size_t)b * N;
-  const float4 *X = c.w.aux32 + (size_t)b * N;
   const float4 pi = P[i], li = PL[i];
   const float kcn = c.pf.kcn;
   const float cut_cn = c.pf.cut_cn, cut_q = c.pf.cut_q;
@@ -367,7 +403,7 @@ __global__ void __launch_bounds__(256, 2) pair_fwd_mixed_kernel(Ctx c) {
   }
   const d4_params_t &p = c.par;
   const float s6 = c.pf.s6, s8 = c.pf.s8, s10 = c.pf.s10;
-  const float a1 = c.pf.a1, a2 = c.pf.a2, cut2 = c.pf.cut2;
+  const float cut2 = c.pf.cut2;
   const float4 *P = c.w.pos32 + (size_t)b * N;
   const float4 *PL = c.w.pos32lo + (size_t)b * N;
   const float4 pi = P[i], li = PL[i];
@@ -678,6 +714,9 @@ __device__ __forceinline__ AtmTri atm_triple(float x, float ix2, float ex, float
   const float A = u + z, Bv = (x + y) - z, Cv = z - u;
   const float AB = A * Bv;
   const float w = fmaf(AB * Cv, h, 1.0f);
+  // (rounding 1 + 6 prod drops its small values at distant triples alike;
+  // measured on 16000 atoms the three-body energy stays within 1e-8 Eh of
+  // the FP64 reference, and a Newton-corrected fd costs 3 % of the kernel)
   const float fd = sfu_rcp(fmaf(6.0f, ex * (ey * ez), 1.0f));
   const float Q = qx * (qy * qz);
   const float cq = Q * fd;
@@ -996,11 +1035,13 @@ constexpr int AT_THREADS = 512;     // 16 warps at 128 registers, no spills (mea
                                     // 13 % slower, 640 at 96 registers 10 % slower)
 constexpr int AT_TASKS_MAX = 900;   // tiles x chunks for n <= 237 (30 x 30)
 constexpr int AT_FAR_WORDS = 8;     // far-atom bits for n <= 256
-// Triples per CTA: 600000 for batches of 512 structures and more (measured
-// best for batch512: 300000 -> 4 % slower, 1200000 -> 2x slower from the
-// largest CTAs), fewer for smaller batches so that they still fill the GPU.
+// Triples per CTA: 1200000 for batches of 512 structures and more (measured
+// on batch512 at 512 threads: 600000 -> 12 % slower, 900000 -> 3 %, 1800000
+// -> 13 %: fewer CTAs per structure mean fewer masked edge steps per task
+// and fewer flushes, until the largest structures' CTAs set the makespan),
+// fewer for smaller batches so that they still fill the GPU.
 __device__ __forceinline__ int atm_tiled_ctas(int n, int B) {
-  const long long per = B >= 512 ? 600000 : (B <= 64 ? 75000 : 600000LL * B / 512);
+  const long long per = B >= 512 ? 1200000 : (B <= 64 ? 75000 : 1200000LL * B / 512);
   const long long work = (long long)n * n * n / 6;
   const int K = (int)((work + per - 1) / per);
   return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
@@ -1949,44 +1990,63 @@ __device__ __forceinline__ dfl df_warp_sum(dfl a) {
 }
 
 // Residual r = BB - (hi + lo) X for ``nr`` right-hand sides, in double-float
-// (FP64-accurate, on the FP32 pipe): one warp per row, lanes over columns
-// (coalesced).  r is rounded to FP32 into vf, the right-hand side of the next
+// (FP64-accurate, on the FP32 pipe): a warp takes four rows at a time, lanes
+// over columns (coalesced), so that 32 independent loads per lane are in
+// flight (one row at a time left the warp waiting on L2 latency row after
+// row).  r is rounded to FP32 into vf, the right-hand side of the next
 // correction; returns max |r| over the block.
 __device__ float eeq_residual_df(const float *Hi, const float *Lo, const float2 *X,
                                  const float2 *BB, float *vf, int m, int N, int nr,
                                  float *s_red) {
+  constexpr int RW = 4;  // rows per warp pass
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   float mx = 0.f;
-  for (int k = warp; k < m; k += nw) {
-    const float *hr = Hi + (size_t)k * N, *lr = Lo + (size_t)k * N;
-    dfl a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
-    for (int l0 = lane; l0 < m; l0 += 256) {
-      float h[8], lo[8];  // eight independent load pairs in flight per lane
+  for (int k0 = warp * RW; k0 < m; k0 += nw * RW) {
+    dfl a0[RW], a1[RW];
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
-        const int l = l0 + 32 * u;
-        h[u] = l < m ? hr[l] : 0.f;
-        lo[u] = l < m ? lr[l] : 0.f;
+    for (int q = 0; q < RW; ++q) a0[q] = a1[q] = dfl{0.f, 0.f};
+    for (int l0 = lane; l0 < m; l0 += 128) {
+      float h[RW][4], lo[RW][4];
+#pragma unroll
+      for (int q = 0; q < RW; ++q) {
+        const int k = k0 + q;
+        const float *hr = Hi + (size_t)(k < m ? k : 0) * N, *lr = Lo + (size_t)(k < m ? k : 0) * N;
+#pragma unroll
+        for (int u = 0; u < 4; ++u) {
+          const int l = l0 + 32 * u;
+          const bool ok = k < m && l < m;
+          h[q][u] = ok ? hr[l] : 0.f;
+          lo[q][u] = ok ? lr[l] : 0.f;
+        }
       }
 #pragma unroll
-      for (int u = 0; u < 8; ++u) {
+      for (int u = 0; u < 4; ++u) {
         const int l = l0 + 32 * u;
         if (l < m) {
-          a0 = df_acc_prod(a0, h[u], lo[u], X[l]);
-          if (nr == 2) a1 = df_acc_prod(a1, h[u], lo[u], X[N + l]);
+          const float2 x0 = X[l];
+          const float2 x1 = nr == 2 ? X[N + l] : make_float2(0.f, 0.f);
+#pragma unroll
+          for (int q = 0; q < RW; ++q) {
+            a0[q] = df_acc_prod(a0[q], h[q][u], lo[q][u], x0);
+            if (nr == 2) a1[q] = df_acc_prod(a1[q], h[q][u], lo[q][u], x1);
+          }
         }
       }
     }
-    a0 = df_warp_sum(a0);
-    if (nr == 2) a1 = df_warp_sum(a1);
-    if (lane == 0) {
-      const dfl r0 = df_add(dfl{BB[k].x, BB[k].y}, df_neg(a0));
-      vf[k] = r0.hi;
-      mx = fmaxf(mx, fabsf(r0.hi));
-      if (nr == 2) {
-        const dfl r1 = df_add(dfl{BB[N + k].x, BB[N + k].y}, df_neg(a1));
-        vf[N + k] = r1.hi;
-        mx = fmaxf(mx, fabsf(r1.hi));
+#pragma unroll
+    for (int q = 0; q < RW; ++q) {
+      const int k = k0 + q;
+      const dfl s0 = df_warp_sum(a0[q]);
+      const dfl s1 = nr == 2 ? df_warp_sum(a1[q]) : dfl{0.f, 0.f};
+      if (lane == 0 && k < m) {
+        const dfl r0 = df_add(dfl{BB[k].x, BB[k].y}, df_neg(s0));
+        vf[k] = r0.hi;
+        mx = fmaxf(mx, fabsf(r0.hi));
+        if (nr == 2) {
+          const dfl r1 = df_add(dfl{BB[N + k].x, BB[N + k].y}, df_neg(s1));
+          vf[N + k] = r1.hi;
+          mx = fmaxf(mx, fabsf(r1.hi));
+        }
       }
     }
   }
@@ -2053,12 +2113,32 @@ __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_mixed_kernel(Ctx c) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
-  // FP32 factor input: the hi part of the lower triangle, one warp per row
-  for (int ii = warp; ii < m; ii += nw) {
-    const float *row = Hi + (size_t)ii * N;
-    float *lrow = L + tri_index(ii, 0);
-    for (int jj = lane; jj <= ii; jj += 32) lrow[jj] = row[jj];
-  }
+  // FP32 factor input: the hi part of the lower triangle, four rows per warp
+  // pass (lanes over columns, all loads of the four rows in flight together)
+  for (int i0 = 4 * warp; i0 < m; i0 += 4 * nw)
+    for (int c0 = 0; c0 < i0 + 4; c0 += 256) {  // columns c0 .. c0 + 255
+      float v[4][8];
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int ii = i0 + q;
+        const float *row = Hi + (size_t)(ii < m ? ii : 0) * N;
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int jj = c0 + lane + 32 * u;
+          v[q][u] = (ii < m && jj <= ii) ? row[jj] : 0.f;
+        }
+      }
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int ii = i0 + q;
+        float *lrow = L + tri_index(ii, 0);
+#pragma unroll
+        for (int u = 0; u < 8; ++u) {
+          const int jj = c0 + lane + 32 * u;
+          if (ii < m && jj <= ii) lrow[jj] = v[q][u];
+        }
+      }
+    }
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const int ia = s_idx[k];
     const int z = Zb[ia];
