@@ -11,69 +11,65 @@ constexpr int PB = 32;  // panel width of the blocked factorisation and solves
 constexpr unsigned FULL = 0xffffffffu;
 
 // Diagonal 32 x 32 block (rows / columns k0 .. k0+kb-1) of the packed lower
-// matrix L, by one warp, in registers: the Cholesky factor (lane r holds row
-// r; rows beyond the matrix are padded with the identity), then the inverse
-// of the factor (lane c computes column c), which replaces the block in
-// place: the panel and the triangular solves only need the inverse.  A
-// non-positive pivot sets *bad and goes on with pivot 1.  The inverse runs
-// column-oriented (x_k /= L_kk, then x_r -= L_rk x_k for all r > k: 32 short
-// steps whose updates are independent) with the pivots' reciprocals kept
-// from the factorisation, instead of 32 row sums that each wait for the
-// previous row and a division.
-static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
+// matrix L, by one warp: the Cholesky factor, then the inverse of the factor,
+// which replaces the block in place (the panel and the triangular solves
+// only need the inverse).  A non-positive pivot sets *bad and goes on with
+// pivot 1.  The factor is formed in a padded copy in ``scratch`` (32 x 33
+// floats of shared memory, row stride 33: a column is conflict-free across
+// lanes; the caller's panel buffer, idle at this point), the inverse in the
+// block's place in L, and both phases are short rolled loops over the
+// block's kb columns: fully unrolled register code for this one warp ran
+// from the instruction cache's misses (it is executed once per panel) at
+// ~9 us per block.
+static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad, float *scratch) {
   __shared__ float s_dinv[PB];
-  const int r = threadIdx.x & 31;
-  const bool live = r < kb;
-  float *row = L + tri_index(k0 + (live ? r : 0), k0);
-  float a[PB];
-#pragma unroll
-  for (int j = 0; j < PB; ++j) a[j] = live ? (j <= r ? row[j] : 0.f) : (j == r ? 1.f : 0.f);
-#pragma unroll
-  for (int c = 0; c < PB; ++c) {
-    float d = __shfl_sync(FULL, a[c], c);
+  float(*s_b)[PB + 1] = reinterpret_cast<float(*)[PB + 1]>(scratch);  // factor, row r in s_b[r]
+  const int lane = threadIdx.x & 31;
+  if (lane < kb) {
+    const float *row = L + tri_index(k0 + lane, k0);
+    for (int j = 0; j <= lane; ++j) s_b[lane][j] = row[j];
+  }
+  __syncwarp();
+  // right-looking factorisation: column c, then the rank-1 update of rows
+  // r > c (lane r), columns c < j <= r
+  for (int c = 0; c < kb; ++c) {
+    float d = s_b[c][c];
     if (!(d > 0.f)) {
-      if (r == 0) *bad = 1;
+      if (lane == 0) *bad = 1;
       d = 1.f;
     }
     const float inv = rsqrtf(d);
-    if (r == c) {
-      a[c] = d * inv;
-      s_dinv[c] = inv;  // 1 / L_cc
-    } else if (r > c) {
-      a[c] *= inv;
+    __syncwarp();
+    float lrc = 0.f;
+    if (lane == c) {
+      s_b[c][c] = d * inv;
+      s_dinv[c] = inv;
+    } else if (lane > c && lane < kb) {
+      lrc = s_b[lane][c] * inv;
+      s_b[lane][c] = lrc;
     }
-#pragma unroll
-    for (int j = 0; j < PB; ++j) {
-      if (j > c) {
-        const float lj = __shfl_sync(FULL, a[c], j);
-        if (r >= j) a[j] = fmaf(-a[c], lj, a[j]);
+    __syncwarp();
+    if (lane > c && lane < kb)
+      for (int j = c + 1; j <= lane; ++j) s_b[lane][j] = fmaf(-lrc, s_b[j][c], s_b[lane][j]);
+    __syncwarp();
+  }
+  // inverse into the block of L, column c = lane: solve L x = e_c by columns
+  // of L (x_k /= L_kk, then x_r -= L_rk x_k for r > k; consecutive lanes
+  // hit consecutive words of a packed row)
+  if (lane < kb)
+    for (int rr = lane; rr < kb; ++rr) L[tri_index(k0 + rr, k0 + lane)] = rr == lane ? 1.f : 0.f;
+  __syncwarp();
+  for (int k = 0; k < kb; ++k) {
+    if (lane <= k) {
+      float *xk_at = L + tri_index(k0 + k, k0 + lane);
+      const float xk = *xk_at * s_dinv[k];
+      *xk_at = xk;
+      for (int rr = k + 1; rr < kb; ++rr) {
+        float *xr = L + tri_index(k0 + rr, k0 + lane);
+        *xr = fmaf(-s_b[rr][k], xk, *xr);
       }
     }
   }
-#pragma unroll
-  for (int j = 0; j < PB; ++j)
-    if (live && j <= r) row[j] = a[j];
-  __syncwarp();
-  // inverse, column c = lane: solve L x = e_c by columns of L
-  const int c = r;
-  float x[PB];
-#pragma unroll
-  for (int rr = 0; rr < PB; ++rr) x[rr] = rr == c ? 1.f : 0.f;
-#pragma unroll
-  for (int k = 0; k < PB; ++k) {
-    x[k] *= s_dinv[k];
-#pragma unroll
-    for (int rr = 0; rr < PB; ++rr) {  // static bounds: x stays in registers
-      if (rr > k) {
-        const float lrk = rr < kb ? L[tri_index(k0 + rr, k0) + k] : 0.f;
-        x[rr] = fmaf(-lrk, x[k], x[rr]);
-      }
-    }
-  }
-  __syncwarp();
-#pragma unroll
-  for (int rr = 0; rr < PB; ++rr)
-    if (rr < kb && rr >= c) L[tri_index(k0 + rr, k0 + c)] = x[rr];
   __syncwarp();
 }
 
@@ -87,19 +83,18 @@ static __device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
 
 // Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
 // m x m FP32 matrix L, in place, except that each diagonal block holds the
-// inverse of its factor.  Per panel: the diagonal block by warp 0 in
-// registers, the panel L21 = A21 X^T (X the block inverse; one warp per row,
-// lane = column), and the trailing update A22 -= L21 L21^T.  With a panel
-// buffer PT (shared memory, 32 x ldp) the panel is also stored transposed and
+// inverse of its factor.  Per panel: the diagonal block by warp 0, the
+// panel L21 = A21 X^T (X the block inverse; one warp per row, lane =
+// column), and the trailing update A22 -= L21 L21^T.  The panel buffer PT
+// (shared memory, 32 x ldp, ldp >= 36) holds the panel transposed, so that
 // the update runs on 8 x 8 register tiles read as float4 (64 FMAs per four
-// 16-byte loads); without it (PT == nullptr) on 4 x 4 tiles read from the
-// packed rows.
+// 16-byte loads), and serves the diagonal block as its scratch.
 static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   const int nw = nt >> 5;
   for (int k0 = 0; k0 < m; k0 += PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) chol_diag_block(L, k0, kb, bad);
+    if (warp == 0) chol_diag_block(L, k0, kb, bad, PT);  // PT idle until the panel
     __syncthreads();
     const int t0 = k0 + kb;
     // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T; the
@@ -126,13 +121,13 @@ static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *ba
         __syncwarp();
         if (lane < kb) {
           row[lane] = v;
-          if (PT) PT[lane * ldp + (i - t0)] = v;
+          PT[lane * ldp + (i - t0)] = v;
         }
       }
     }
     __syncthreads();
     const int nrem = m - t0;
-    if (PT) {
+    {
       const int T8 = (nrem + 7) >> 3;
       const int ntile = T8 * (T8 + 1) / 2;
       for (int t = tid; t < ntile; t += nt) {
@@ -167,44 +162,6 @@ static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *ba
             }
           }
         }
-      }
-    } else {
-      const int T4 = (nrem + 3) >> 2;
-      const int ntile = T4 * (T4 + 1) / 2;
-      for (int t = tid; t < ntile; t += nt) {
-        int ti, tj;
-        tri_tile(t, ti, tj);
-        const int i0 = t0 + 4 * ti, j0 = t0 + 4 * tj;
-        size_t ri[4], rj[4];  // offsets of the panel segments of rows i0+q, j0+q
-#pragma unroll
-        for (int q = 0; q < 4; ++q) {
-          ri[q] = tri_index(min(i0 + q, m - 1), k0);
-          rj[q] = tri_index(min(j0 + q, m - 1), k0);
-        }
-        float acc[4][4];
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int u = 0; u < 4; ++u) acc[q][u] = 0.f;
-        for (int cc = 0; cc < kb; ++cc) {
-          float x[4], y[4];
-#pragma unroll
-          for (int q = 0; q < 4; ++q) {
-            x[q] = L[ri[q] + cc];
-            y[q] = L[rj[q] + cc];
-          }
-#pragma unroll
-          for (int q = 0; q < 4; ++q)
-#pragma unroll
-            for (int u = 0; u < 4; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
-        }
-#pragma unroll
-        for (int q = 0; q < 4; ++q)
-#pragma unroll
-          for (int u = 0; u < 4; ++u) {
-            const int i = i0 + q, j = j0 + u;
-            if (i < m && j <= i) L[tri_index(i, j)] -= acc[q][u];
-          }
       }
     }
     __syncthreads();

@@ -30,10 +30,12 @@ __host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {  // multiple of 
 }
 // Leading dimension of the transposed panel PT[32][ldp] of chol_blocked:
 // rows of at most N - 32 entries, rounded up to 8 (the 8-wide tiles read up
-// to there) plus 4 (16-byte rows, spread banks).
+// to there) plus 4 (16-byte rows, spread banks); at least 36, so that PT also
+// holds the 32 x 33 scratch of the diagonal blocks.
 __host__ __device__ inline int chol_panel_ld(int N) {
   const int n = N > 40 ? N - 32 : 8;
-  return ((n + 7) & ~7) + 4;
+  const int ld = ((n + 7) & ~7) + 4;
+  return ld < 36 ? 36 : ld;
 }
 __host__ __device__ inline size_t eeq_small_bytes(int N) {
   return 4 * (eeq_mixed_vec_floats(N) + (size_t)32 * chol_panel_ld(N) +
