@@ -246,6 +246,15 @@ int d4_properties(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
 int d4_read_status(void *d_workspace, void *stream);
 
 /*
+ * Queue a copy of the device status word of a workspace into ``h_status``
+ * (host memory that stays valid until the copy has run; page-locked for the
+ * copy to be asynchronous) behind the work already on ``stream``, without
+ * waiting.  Returns D4_OK or D4_ERR_CUDA.  (No reference counterpart: the
+ * host layer uses it to read an autograd forward's status later.)
+ */
+int d4_status_async(void *d_workspace, int32_t *h_status, void *stream);
+
+/*
  * Kernel timing.  Between d4_timing_begin and d4_timing_end, every
  * d4_dispersion call on this host thread records a pair of CUDA events
  * around each of its kernels, on the stream it launches them on (at most

@@ -2,8 +2,35 @@
 #include <stdio.h>
 #include <string.h>
 
+#include <mutex>
+#include <utility>
+#include <vector>
+
 #include "d4_common.cuh"
 #include "d4_kernels.cuh"
+
+namespace d4 {
+
+// (device, kernel) -> dynamic shared-memory limit already set
+void ensure_smem_impl(const void *func, size_t bytes) {
+  static std::mutex mu;
+  static std::vector<std::pair<std::pair<int, const void *>, size_t>> done;
+  int dev = 0;
+  cudaGetDevice(&dev);
+  std::lock_guard<std::mutex> lock(mu);
+  for (auto &e : done)
+    if (e.first.first == dev && e.first.second == func) {
+      if (bytes > e.second) {
+        cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+        e.second = bytes;
+      }
+      return;
+    }
+  cudaFuncSetAttribute(func, cudaFuncAttributeMaxDynamicSharedMemorySize, (int)bytes);
+  done.push_back({{dev, func}, bytes});
+}
+
+}  // namespace d4
 
 namespace {
 thread_local char g_cuda_error[256] = "";
@@ -159,6 +186,13 @@ int d4_properties(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   cudaStream_t st = static_cast<cudaStream_t>(stream);
   d4::launch_properties(c, out->d_c6, out->d_alpha, out->d_charges, st);
   return check_cuda(cudaGetLastError());
+}
+
+int d4_status_async(void *d_workspace, int32_t *h_status, void *stream) {
+  if (!d_workspace || !h_status) return D4_ERR_ARGUMENT;
+  d4::Workspace w = d4::carve_workspace(d_workspace, 1, 1, 1, 0);
+  return check_cuda(cudaMemcpyAsync(h_status, w.status, sizeof(int32_t), cudaMemcpyDeviceToHost,
+                                    static_cast<cudaStream_t>(stream)));
 }
 
 int d4_read_status(void *d_workspace, void *stream) {

@@ -529,16 +529,13 @@ void launch_pair_fwd_tc(const Ctx &c, cudaStream_t st) {
     }
   }
   if (pgrad) {
-    cudaFuncSetAttribute(pair_fwd_tc_kernel<true, true>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    ensure_smem(pair_fwd_tc_kernel<true, true>, smem);
     pair_fwd_tc_kernel<true, true><<<grid, TC_THREADS, smem, st>>>(c);
   } else if (grad) {
-    cudaFuncSetAttribute(pair_fwd_tc_kernel<true, false>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    ensure_smem(pair_fwd_tc_kernel<true, false>, smem);
     pair_fwd_tc_kernel<true, false><<<grid, TC_THREADS, smem, st>>>(c);
   } else {
-    cudaFuncSetAttribute(pair_fwd_tc_kernel<false, false>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+    ensure_smem(pair_fwd_tc_kernel<false, false>, smem);
     pair_fwd_tc_kernel<false, false><<<grid, TC_THREADS, smem, st>>>(c);
   }
 }
@@ -827,7 +824,7 @@ bool pair_atm_bwd_tc_ok(const Ctx &c) { return c.cfg.kind == D4_MODEL_D4 && c.S 
 
 void launch_pair_atm_bwd_tc(const Ctx &c, cudaStream_t st) {
   const int smem = (int)sizeof(BwSmem);
-  cudaFuncSetAttribute(pair_atm_bwd_tc_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, smem);
+  ensure_smem(pair_atm_bwd_tc_kernel, smem);
   // few tiles (large structures): a tile's partners are split over several
   // CTAs so that every SM gets about four
   int dev = 0, nsm = 0;

@@ -11,65 +11,65 @@ constexpr int PB = 32;  // panel width of the blocked factorisation and solves
 constexpr unsigned FULL = 0xffffffffu;
 
 // Diagonal 32 x 32 block (rows / columns k0 .. k0+kb-1) of the packed lower
-// matrix L, by one warp: the Cholesky factor, then the inverse of the factor,
-// which replaces the block in place (the panel and the triangular solves
-// only need the inverse).  A non-positive pivot sets *bad and goes on with
-// pivot 1.  The factor is formed in a padded copy in ``scratch`` (32 x 33
-// floats of shared memory, row stride 33: a column is conflict-free across
-// lanes; the caller's panel buffer, idle at this point), the inverse in the
-// block's place in L, and both phases are short rolled loops over the
-// block's kb columns: fully unrolled register code for this one warp ran
-// from the instruction cache's misses (it is executed once per panel) at
-// ~9 us per block.
-static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad, float *scratch) {
-  __shared__ float s_dinv[PB];
-  float(*s_b)[PB + 1] = reinterpret_cast<float(*)[PB + 1]>(scratch);  // factor, row r in s_b[r]
-  const int lane = threadIdx.x & 31;
-  if (lane < kb) {
-    const float *row = L + tri_index(k0 + lane, k0);
-    for (int j = 0; j <= lane; ++j) s_b[lane][j] = row[j];
-  }
-  __syncwarp();
-  // right-looking factorisation: column c, then the rank-1 update of rows
-  // r > c (lane r), columns c < j <= r
-  for (int c = 0; c < kb; ++c) {
-    float d = s_b[c][c];
+// matrix L, by one warp, in registers: the Cholesky factor (lane r holds row
+// r; rows beyond the matrix are padded with the identity), then the inverse
+// of the factor (lane c computes column c), which replaces the block in
+// place: the panel and the triangular solves only need the inverse.  A
+// non-positive pivot sets *bad and goes on with pivot 1.  (Measured at
+// ~9 us per block on batch512, one warp while the other seven wait; a
+// column-oriented inverse was no faster, and rolled shared-memory loops
+// were 3x slower: their loads and stores serialise.)
+static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
+  const int r = threadIdx.x & 31;
+  const bool live = r < kb;
+  float *row = L + tri_index(k0 + (live ? r : 0), k0);
+  float a[PB];
+#pragma unroll
+  for (int j = 0; j < PB; ++j) a[j] = live ? (j <= r ? row[j] : 0.f) : (j == r ? 1.f : 0.f);
+#pragma unroll
+  for (int c = 0; c < PB; ++c) {
+    float d = __shfl_sync(FULL, a[c], c);
     if (!(d > 0.f)) {
-      if (lane == 0) *bad = 1;
+      if (r == 0) *bad = 1;
       d = 1.f;
     }
     const float inv = rsqrtf(d);
-    __syncwarp();
-    float lrc = 0.f;
-    if (lane == c) {
-      s_b[c][c] = d * inv;
-      s_dinv[c] = inv;
-    } else if (lane > c && lane < kb) {
-      lrc = s_b[lane][c] * inv;
-      s_b[lane][c] = lrc;
-    }
-    __syncwarp();
-    if (lane > c && lane < kb)
-      for (int j = c + 1; j <= lane; ++j) s_b[lane][j] = fmaf(-lrc, s_b[j][c], s_b[lane][j]);
-    __syncwarp();
-  }
-  // inverse into the block of L, column c = lane: solve L x = e_c by columns
-  // of L (x_k /= L_kk, then x_r -= L_rk x_k for r > k; consecutive lanes
-  // hit consecutive words of a packed row)
-  if (lane < kb)
-    for (int rr = lane; rr < kb; ++rr) L[tri_index(k0 + rr, k0 + lane)] = rr == lane ? 1.f : 0.f;
-  __syncwarp();
-  for (int k = 0; k < kb; ++k) {
-    if (lane <= k) {
-      float *xk_at = L + tri_index(k0 + k, k0 + lane);
-      const float xk = *xk_at * s_dinv[k];
-      *xk_at = xk;
-      for (int rr = k + 1; rr < kb; ++rr) {
-        float *xr = L + tri_index(k0 + rr, k0 + lane);
-        *xr = fmaf(-s_b[rr][k], xk, *xr);
+    if (r == c) a[c] = d * inv;
+    else if (r > c) a[c] *= inv;
+#pragma unroll
+    for (int j = 0; j < PB; ++j) {
+      if (j > c) {
+        const float lj = __shfl_sync(FULL, a[c], j);
+        if (r >= j) a[j] = fmaf(-a[c], lj, a[j]);
       }
     }
   }
+#pragma unroll
+  for (int j = 0; j < PB; ++j)
+    if (live && j <= r) row[j] = a[j];
+  __syncwarp();
+  // inverse: X[rr][c] = -(sum_{k=c}^{rr-1} L[rr][k] X[k][c]) / L[rr][rr]; x = column c
+  const int c = r;
+  float x[PB];
+#pragma unroll
+  for (int rr = 0; rr < PB; ++rr) {
+    x[rr] = 0.f;
+    if (rr < kb) {
+      const float *lr = L + tri_index(k0 + rr, k0);
+      float acc0 = 0.f, acc1 = 0.f;
+#pragma unroll
+      for (int k = 0; k < rr; ++k) {
+        if (k & 1) acc1 = fmaf(lr[k], x[k], acc1);
+        else acc0 = fmaf(lr[k], x[k], acc0);
+      }
+      const float dii = 1.0f / lr[rr];
+      x[rr] = rr == c ? dii : (rr > c ? -(acc0 + acc1) * dii : 0.f);
+    }
+  }
+  __syncwarp();
+#pragma unroll
+  for (int rr = 0; rr < PB; ++rr)
+    if (rr < kb && rr >= c) L[tri_index(k0 + rr, k0 + c)] = x[rr];
   __syncwarp();
 }
 
@@ -86,15 +86,15 @@ static __device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
 // inverse of its factor.  Per panel: the diagonal block by warp 0, the
 // panel L21 = A21 X^T (X the block inverse; one warp per row, lane =
 // column), and the trailing update A22 -= L21 L21^T.  The panel buffer PT
-// (shared memory, 32 x ldp, ldp >= 36) holds the panel transposed, so that
-// the update runs on 8 x 8 register tiles read as float4 (64 FMAs per four
-// 16-byte loads), and serves the diagonal block as its scratch.
+// (shared memory, 32 x ldp) holds the panel transposed, so that the update
+// runs on 8 x 8 register tiles read as float4 (64 FMAs per four 16-byte
+// loads).
 static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   const int nw = nt >> 5;
   for (int k0 = 0; k0 < m; k0 += PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) chol_diag_block(L, k0, kb, bad, PT);  // PT idle until the panel
+    if (warp == 0) chol_diag_block(L, k0, kb, bad);
     __syncthreads();
     const int t0 = k0 + kb;
     // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T; the

@@ -30,12 +30,10 @@ __host__ __device__ inline size_t eeq_mixed_vec_floats(int N) {  // multiple of 
 }
 // Leading dimension of the transposed panel PT[32][ldp] of chol_blocked:
 // rows of at most N - 32 entries, rounded up to 8 (the 8-wide tiles read up
-// to there) plus 4 (16-byte rows, spread banks); at least 36, so that PT also
-// holds the 32 x 33 scratch of the diagonal blocks.
+// to there) plus 4 (16-byte rows, spread banks).
 __host__ __device__ inline int chol_panel_ld(int N) {
   const int n = N > 40 ? N - 32 : 8;
-  const int ld = ((n + 7) & ~7) + 4;
-  return ld < 36 ? 36 : ld;
+  return ((n + 7) & ~7) + 4;
 }
 __host__ __device__ inline size_t eeq_small_bytes(int N) {
   return 4 * (eeq_mixed_vec_floats(N) + (size_t)32 * chol_panel_ld(N) +
@@ -166,6 +164,15 @@ struct Workspace {
 };
 
 inline size_t align_up(size_t x, size_t a) { return (x + a - 1) / a * a; }
+
+// Raise a kernel's dynamic shared-memory limit once per device and size:
+// cudaFuncSetAttribute costs microseconds of host time, which every call of
+// the library would otherwise pay again (d4_api.cu).
+void ensure_smem_impl(const void *func, size_t bytes);
+template <typename F>
+inline void ensure_smem(F *func, size_t bytes) {
+  ensure_smem_impl(reinterpret_cast<const void *>(func), bytes);
+}
 
 // Layout of the workspace; ``base == nullptr`` only measures it.
 inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags) {

@@ -763,12 +763,9 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int npan = (N + BNB - 1) / BNB;
   if (!adjoint) {
     cudaMemcpyAsync(c.w.eeq_F, c.w.eeq_hi, (size_t)4 * B * N * N, cudaMemcpyDeviceToDevice, st);
-    cudaFuncSetAttribute(eeq_big_diag_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)eeq_big_diag_smem());
-    cudaFuncSetAttribute(eeq_big_panel_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)eeq_big_panel_smem());
-    cudaFuncSetAttribute(eeq_big_syrk_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)eeq_big_syrk_smem());
+    ensure_smem(eeq_big_diag_kernel, (int)eeq_big_diag_smem());
+    ensure_smem(eeq_big_panel_kernel, (int)eeq_big_panel_smem());
+    ensure_smem(eeq_big_syrk_kernel, (int)eeq_big_syrk_smem());
     for (int p = 0; p < npan; ++p) {
       const int k0 = p * BNB;
       eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), st>>>(c, k0);
@@ -782,8 +779,7 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int nsb = eeq_nsb(N);
   if (!adjoint) {  // inverses of the 512-blocks, kept for the adjoint solve
     eeq_blkinv_init_kernel<<<dim3(nsb, B), 256, 0, st>>>(c);
-    cudaFuncSetAttribute(eeq_blkinv_step_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)eeq_blkinv_smem());
+    ensure_smem(eeq_blkinv_step_kernel, (int)eeq_blkinv_smem());
     for (int r = 1; r < SBP; ++r)
       eeq_blkinv_step_kernel<<<dim3(nsb * r, B), 256, eeq_blkinv_smem(), st>>>(c, r);
   }

@@ -1223,12 +1223,10 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
   stage_begin(ST_EEQ, st);
   if (eeq) {
     if (vec_bytes + tri_bytes <= 220 * 1024) {
-      cudaFuncSetAttribute(eeq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(vec_bytes + tri_bytes));
+      ensure_smem(eeq_kernel<true>, (int)(vec_bytes + tri_bytes));
       eeq_kernel<true><<<B, 256, vec_bytes + tri_bytes, st>>>(c);
     } else {
-      cudaFuncSetAttribute(eeq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)vec_bytes);
+      ensure_smem(eeq_kernel<false>, (int)vec_bytes);
       eeq_kernel<false><<<B, 256, vec_bytes, st>>>(c);
     }
   } else {
@@ -1262,8 +1260,7 @@ int launch_fp64(const Ctx &c, cudaStream_t st) {
     stage_end(ST_PAIR_ATM_BWD, st);
     if (eeq) {
       stage_begin(ST_EEQ_ADJ, st);
-      cudaFuncSetAttribute(eeq_adjoint_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)vec_bytes);
+      ensure_smem(eeq_adjoint_kernel, (int)vec_bytes);
       eeq_adjoint_kernel<<<B, 256, vec_bytes, st>>>(c);
       stage_end(ST_EEQ_ADJ, st);
     }
@@ -1328,12 +1325,10 @@ int launch_properties(const Ctx &c, double *c6out, double *alpha_out, double *q_
   const size_t vec_bytes = (size_t)8 * ((N + 1) / 2 + 1 + 2 * N);
   const size_t tri_bytes = (size_t)8 * ((size_t)N * (N + 1) / 2);
   if (vec_bytes + tri_bytes <= 220 * 1024) {
-    cudaFuncSetAttribute(eeq_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)(vec_bytes + tri_bytes));
+    ensure_smem(eeq_kernel<true>, (int)(vec_bytes + tri_bytes));
     eeq_kernel<true><<<B, 256, vec_bytes + tri_bytes, st>>>(c);
   } else {
-    cudaFuncSetAttribute(eeq_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                         (int)vec_bytes);
+    ensure_smem(eeq_kernel<false>, (int)vec_bytes);
     eeq_kernel<false><<<B, 256, vec_bytes, st>>>(c);
   }
   launch_weights(c, st);

@@ -703,7 +703,9 @@ struct AtmTri {
   float eu, dex, dey, dez, qwg;
 };
 
-template <bool GRAD>
+// EZ6: ez arrives multiplied by 6 (a caller that holds the (j, k) record for
+// many triples scales it once).
+template <bool GRAD, bool EZ6 = false>
 __device__ __forceinline__ AtmTri atm_triple(float x, float ix2, float ex, float qx, float y,
                                              float iy2, float ey, float qy, float z, float iz2,
                                              float ez, float qz, float alp3h) {
@@ -717,21 +719,22 @@ __device__ __forceinline__ AtmTri atm_triple(float x, float ix2, float ex, float
   // (rounding 1 + 6 prod drops its small values at distant triples alike;
   // measured on 16000 atoms the three-body energy stays within 1e-8 Eh of
   // the FP64 reference, and a Newton-corrected fd costs 3 % of the kernel)
-  const float fd = sfu_rcp(fmaf(6.0f, ex * (ey * ez), 1.0f));
+  const float fd = EZ6 ? sfu_rcp(fmaf(ex, ey * ez, 1.0f))
+                      : sfu_rcp(fmaf(6.0f, ex * (ey * ez), 1.0f));
   const float Q = qx * (qy * qz);
   const float cq = Q * fd;
   r.eu = cq * w;
   if (GRAD) {
     // U = 3/8 C9 fd / R^5, V = C9 / (2 R^3) (fd (2 - 5 w) + w alp/3 fd (1 - fd))
-    const float g = fmaf(-fd, fd, fd);
+    //   = C9 fd / R^3 (1 + w (alp/6 (1 - fd) - 5/2))
     const float U = cq * h;
-    const float V = Q * fmaf(fd, fmaf(-2.5f, w, 1.0f), w * (alp3h * g));
+    const float V = cq * fmaf(w, fmaf(-alp3h, fd, alp3h - 2.5f), 1.0f);
     const float AC = A * Cv, BC = Bv * Cv;
     const float Sg = AB + AC + BC;
     r.dex = fmaf(U, fmaf(-2.0f, AB, Sg), V * ix2);
     r.dey = fmaf(U, fmaf(-2.0f, BC, Sg), V * iy2);
     r.dez = fmaf(U, fmaf(-2.0f, AC, Sg), V * iz2);
-    r.qwg = Q * w * g;
+    r.qwg = Q * w * fmaf(-fd, fd, fd);
   } else {
     r.dex = r.dey = r.dez = r.qwg = 0.f;
   }
@@ -768,7 +771,7 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
   const int k = kc + lane;
   const bool kok = k < n && in.Zb[k] != 0;
   const float4 pjk = kok ? T[(size_t)j * N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
-  const float zjk = pjk.x, izjk = pjk.y, ejk = pjk.z, qjk = pjk.w;
+  const float zjk = pjk.x, izjk = pjk.y, ejk6 = 6.0f * pjk.z, qjk = pjk.w;
   const float alp3h = 0.5f * alp3;
   const bool mjk = kok && zjk <= cut2;
   float4 dajk = make_float4(0.f, 0.f, 0.f, 0.f);
@@ -789,8 +792,8 @@ __device__ __forceinline__ void atm_task(const AtmIn &in, const AtmAcc<SMEM> &ac
       const float4 pik = *Tik;
       const bool mij = pij.x <= cut2, mik = pik.x <= cut2;
       if ((int)mij + (int)mik + (int)mjk >= 2) {
-        const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y, pik.z,
-                                           pik.w, zjk, izjk, ejk, qjk, alp3h);
+        const AtmTri tr = atm_triple<GRAD, true>(pij.x, pij.y, pij.z, pij.w, pik.x, pik.y,
+                                                 pik.z, pik.w, zjk, izjk, ejk6, qjk, alp3h);
         const float eu = tr.eu;  // triple energy without s9
         const float e = s9m * eu;
         float wgt;
@@ -1125,8 +1128,8 @@ __device__ __forceinline__ void atm_tile_step(const AtTile &a, int j0, int jend,
       const int m = (int)fij + (int)fik + (int)fjk;
       qij *= m == 3 ? 1.f : (m == 2 ? (1.0f / 3.0f) : 0.f);
     }
-    const AtmTri tr = atm_triple<GRAD>(pij.x, pij.y, pij.z, qij, pik.x, pik.y, pik.z, pik.w,
-                                       zjk[t], izjk[t], ejk[t], qjk[t], a.alp3h);
+    const AtmTri tr = atm_triple<GRAD, true>(pij.x, pij.y, pij.z, qij, pik.x, pik.y, pik.z,
+                                             pik.w, zjk[t], izjk[t], ejk[t], qjk[t], a.alp3h);
     if (MASK && !(fij & fik & fjk) && tr.eu != 0.f) {
       // a 1/3 triple: -2 eu_w to the atom of both inside pairs, +eu_w to the others
       atomicAdd(&a.sE[i], fjk ? tr.eu : -2.f * tr.eu);
@@ -1199,7 +1202,7 @@ __device__ __forceinline__ void atm_tile_task(const AtTile &a, bool any_far, int
     const float4 r = ok ? a.T[(size_t)jt * a.N + k] : make_float4(0.f, 0.f, 0.f, 0.f);
     zjk[t] = r.x;
     izjk[t] = r.y;
-    ejk[t] = r.z;
+    ejk[t] = 6.0f * r.z;  // prescaled for atm_triple<., true>
     qjk[t] = r.w;  // 0 also zeroes every product of a (j, k) that is not a pair
     Sjk[t] = 0.f;
     Pjk[t] = 0.f;
@@ -2272,8 +2275,7 @@ static unsigned build_blocks(const Ctx &c) {
 template <bool SMEM, bool GRAD, bool PGRAD>
 static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
   if (SMEM)
-    cudaFuncSetAttribute(atm_mixed_kernel<SMEM, GRAD, PGRAD>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, (int)smem);
+    ensure_smem(atm_mixed_kernel<SMEM, GRAD, PGRAD>, (int)smem);
   const int threads = PGRAD ? ATM_THREADS_PGRAD : ATM_THREADS;
   const int K = SMEM ? ATM_KMAX : atm_ctas_big(c.N);
   if (!SMEM) {
@@ -2281,14 +2283,13 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
     int P = 1;
     while (P < c.N && P < ATM_ORDER_MAX) P <<= 1;
     const int osm = 8 * P;
-    cudaFuncSetAttribute(atm_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, osm);
+    ensure_smem(atm_order_kernel, osm);
     atm_order_kernel<<<c.B, 1024, osm, st>>>(c);
   }
   atm_mixed_kernel<SMEM, GRAD, PGRAD><<<dim3(K, c.B), threads, smem, st>>>(c);
   if (!SMEM) {  // neighbour-triple variant; returns at once for dense structures
     const int sp = ATM_SPARSE_DMAX * (16 + 4 * 4);
-    cudaFuncSetAttribute(atm_sparse_kernel<GRAD, PGRAD>,
-                         cudaFuncAttributeMaxDynamicSharedMemorySize, sp);
+    ensure_smem(atm_sparse_kernel<GRAD, PGRAD>, sp);
     atm_sparse_kernel<GRAD, PGRAD><<<dim3(c.N, c.B), ATM_SPARSE_THREADS, sp, st>>>(c);
   }
   if (!SMEM && GRAD) {
@@ -2312,7 +2313,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
     while (P < B && P < SORDER_MAX) P <<= 1;
     const int osm = 8 * P;
     if (osm > 48 * 1024)
-      cudaFuncSetAttribute(size_order_kernel, cudaFuncAttributeMaxDynamicSharedMemorySize, osm);
+      ensure_smem(size_order_kernel, osm);
     size_order_kernel<<<1, 1024, osm, st>>>(c);
   }
   stage_end(ST_PREP, st);
@@ -2327,8 +2328,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   if (eeq) {
     eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
     if (eeq_smem) {
-      cudaFuncSetAttribute(eeq_mixed_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)(vec_bytes + pt_bytes + tri_bytes));
+      ensure_smem(eeq_mixed_kernel<true>, (int)(vec_bytes + pt_bytes + tri_bytes));
       eeq_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + pt_bytes + tri_bytes, st>>>(c);
     } else {
       launch_eeq_big(c, st, false);
@@ -2357,12 +2357,10 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   if (atm_sm && !pgrad && c.weights == nullptr) {  // register-tiled triples
     const size_t sm = atm_tiled_smem_bytes(N);
     if (grad) {
-      cudaFuncSetAttribute(atm_tiled_kernel<true>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm);
+      ensure_smem(atm_tiled_kernel<true>, (int)sm);
       atm_tiled_kernel<true><<<dim3(ATM_KMAX, B), AT_THREADS, sm, st>>>(c);
     } else {
-      cudaFuncSetAttribute(atm_tiled_kernel<false>, cudaFuncAttributeMaxDynamicSharedMemorySize,
-                           (int)sm);
+      ensure_smem(atm_tiled_kernel<false>, (int)sm);
       atm_tiled_kernel<false><<<dim3(ATM_KMAX, B), AT_THREADS, sm, st>>>(c);
     }
   } else if (atm_sm) {
@@ -2391,9 +2389,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
     if (eeq) {
       stage_begin(ST_EEQ_ADJ, st);
       if (eeq_smem) {
-        cudaFuncSetAttribute(eeq_adjoint_mixed_kernel<true>,
-                             cudaFuncAttributeMaxDynamicSharedMemorySize,
-                             (int)(vec_bytes + tri_bytes));
+        ensure_smem(eeq_adjoint_mixed_kernel<true>, (int)(vec_bytes + tri_bytes));
         eeq_adjoint_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + tri_bytes, st>>>(c);
       } else {
         launch_eeq_big(c, st, true);

@@ -185,7 +185,8 @@ class Runner:
             self.token = None
             if CHECK_STATUS and defer_status:  # the status word stays in the stream
                 word = torch.empty(1, dtype=torch.int32, pin_memory=True)
-                word.copy_(work[:4].view(torch.int32), non_blocking=True)
+                _lib.check(lib.d4_status_async(work.data_ptr(), word.data_ptr(), stream),
+                           "d4_status_async")
                 ev = torch.cuda.Event()
                 ev.record(cur)
                 _CALLS[0] += 1
@@ -240,12 +241,16 @@ class _D4Function(torch.autograd.Function):
             gpos = (w0.unsqueeze(-1) * grad).to(ctx.positions.dtype)
         if ctx.needs_input_grad[1]:
             gpar = (w0 * pgrad).sum(0)[: len(PARAM_ORDER)]
-        # the forward's status word, read after the gradient's own launches
-        # so that the GPU does not idle while the host waits for it
+        # the forward's status word: read here if the forward has finished,
+        # else left to the next library call or check_status() -- the host
+        # does not wait for the GPU in the backward (whatever the caller
+        # queues next, e.g. the copies of the results, follows the kernels
+        # directly), the way CUDA reports asynchronous errors
         for idx, token in enumerate(_PENDING):
             if token is ctx.token:
-                del _PENDING[idx]
-                _read_token(token)
+                if token[1].query():
+                    del _PENDING[idx]
+                    _read_token(token)
                 break
         return gpos, gpar, None
 
