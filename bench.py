@@ -352,6 +352,7 @@ def run_large(pkg, disp, lib, dev, steps: int = 3, natoms: int = 16000,
     pkg._lib.check(lib.d4_timing_end(ms_stage, nstage, ncalls), "timing")
     ms = [ev[k].elapsed_time(ev[k + 1]) for k in range(steps)]
     fsum = g[0].sum(0).abs().max().item()
+    res = runner.eeq_residuals()  # final refinement residuals of the last timed call
     _, _, _, q, _ = runner.run(pt, gradient=False, charges_out=True)
     torch.cuda.synchronize()
     out = {
@@ -365,6 +366,8 @@ def run_large(pkg, disp, lib, dev, steps: int = 3, natoms: int = 16000,
                      for i in range(nstage)},
         "energy_eh": float(e.sum()),
         "max_abs_sum_of_forces_eh_bohr": fsum,
+        "eeq_refinement_residual": {"charges": float(res[0, 0]), "adjoint": float(res[0, 1]),
+                                    "tolerance": 1e-10},
         "peak_device_gb": torch.cuda.max_memory_allocated(dev) / 1e9,
     }
     e_prod = e[0].detach().clone()
@@ -554,6 +557,7 @@ def run_ours(args, world, rank, local):
     err_p = oracle_errors(batch, param, e_p.cpu().numpy(), g_p.cpu().numpy())
     e_all = (e_m.sum(-1) - e_p.sum(-1)).abs().max().item()
     f_all = (g_m - g_p).abs().max().item()
+    res_m = mixed.eeq_residuals()  # final refinement residuals of that call
 
     # ---- end to end through the public API, host buffers
     e2e_steps = args.e2e_steps or max(3, args.steps // 2)
@@ -679,7 +683,11 @@ def run_ours(args, world, rank, local):
             "error_plain_fp64_vs_oracle": err_p,
             "error_precision_vs_plain_all_structures": {"max_abs_dE_eh": e_all,
                                                         "max_abs_dF_eh_bohr": f_all},
+            "eeq_refinement_residual_max": {"charges": float(res_m[:, 0].max()),
+                                            "adjoint": float(res_m[:, 1].max()),
+                                            "tolerance": 1e-10},
             "large16k_error_vs_fp64": (large or {}).get("error_vs_fp64_reference"),
+            "large16k_eeq_refinement_residual": (large or {}).get("eeq_refinement_residual"),
         }
         print(json.dumps(line), flush=True)
 

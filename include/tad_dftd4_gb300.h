@@ -246,6 +246,19 @@ int d4_properties(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
 int d4_read_status(void *d_workspace, void *stream);
 
 /*
+ * Final residuals max |A x - b| of the EEQ refinement of the last
+ * d4_dispersion call that used this workspace, per structure: h_out[2 b]
+ * for the charges (forward), h_out[2 b + 1] for the adjoint solve of a
+ * gradient call.  Precision form only: its FP32 factorisation is refined in
+ * double-float until the residual is below 1e-10 (or the iteration limit);
+ * the entries stay 0 where no refinement ran (plain FP64 method, given
+ * charges, energy-only calls for the adjoint).  ``n_struct`` is the batch
+ * size of that call.  Synchronous on ``stream``.  (No reference counterpart:
+ * the reference solves the EEQ system directly in its working precision.)
+ */
+int d4_eeq_residuals(void *d_workspace, int32_t n_struct, float *h_out, void *stream);
+
+/*
  * Queue a copy of the device status word of a workspace into ``h_status``
  * (host memory that stays valid until the copy has run; page-locked for the
  * copy to be asynchronous) behind the work already on ``stream``, without

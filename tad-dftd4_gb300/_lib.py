@@ -155,6 +155,7 @@ SIGNATURES = {
          ctypes.POINTER(Outputs), c_void_p],
     ),
     "d4_read_status": (c_int, [c_void_p, c_void_p]),
+    "d4_eeq_residuals": (c_int, [c_void_p, c_int32, c_void_p, c_void_p]),
     "d4_status_async": (c_int, [c_void_p, c_void_p, c_void_p]),
     "d4_timing_begin": (c_int, [c_int32]),
     "d4_timing_end": (c_int, [ctypes.POINTER(ctypes.c_float), c_int32,

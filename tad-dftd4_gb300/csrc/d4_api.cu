@@ -195,6 +195,16 @@ int d4_status_async(void *d_workspace, int32_t *h_status, void *stream) {
                                     static_cast<cudaStream_t>(stream)));
 }
 
+int d4_eeq_residuals(void *d_workspace, int32_t n_struct, float *h_out, void *stream) {
+  if (!d_workspace || !h_out || n_struct <= 0) return D4_ERR_ARGUMENT;
+  d4::Workspace w = d4::carve_workspace(d_workspace, n_struct, 1, 1, 0);
+  cudaStream_t st = static_cast<cudaStream_t>(stream);
+  int rc = check_cuda(cudaMemcpyAsync(h_out, w.eeq_final, sizeof(float) * 2 * (size_t)n_struct,
+                                      cudaMemcpyDeviceToHost, st));
+  if (rc != D4_OK) return rc;
+  return check_cuda(cudaStreamSynchronize(st));
+}
+
 int d4_read_status(void *d_workspace, void *stream) {
   if (!d_workspace) return D4_ERR_ARGUMENT;
   cudaStream_t st = static_cast<cudaStream_t>(stream);

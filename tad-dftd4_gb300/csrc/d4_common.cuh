@@ -68,6 +68,7 @@ constexpr int ATM_ORDER_MAX = 16384;
 
 struct Workspace {
   int *status;      // [1]
+  float *eeq_final; // [B][2] final EEQ refinement residual (forward, adjoint); fixed offset
   int *n_eff;       // [B]   highest real atom index + 1
   int *n_slots;     // [B]   distinct-element slots (D4S), 1 for D4
   int *z;           // [B*N] validated atomic numbers (0: padding or invalid)
@@ -191,6 +192,7 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
   const bool grad = (flags & D4_FLAG_GRADIENT) != 0;
   const bool mixed = (flags & D4_FLAG_MIXED) != 0;
   w.status = (int *)take(sizeof(int) * 4);
+  w.eeq_final = (float *)take(sizeof(float) * 2 * (size_t)B);  // at byte 256 for every B
   w.n_eff = (int *)take(sizeof(int) * B);
   w.n_slots = (int *)take(sizeof(int) * B);
   w.z = (int *)take(sizeof(int) * BN);

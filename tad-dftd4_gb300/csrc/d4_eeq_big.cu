@@ -25,6 +25,8 @@
 // size n_real[b].
 #include <float.h>
 
+#include <mutex>
+
 #include "d4_chol.cuh"
 #include "d4_common.cuh"
 #include "d4_kernels.cuh"
@@ -192,7 +194,12 @@ __device__ __forceinline__ int sy_off(int r, int k) {  // bytes
   return (r >> 3) * SY_SBO + (k >> 2) * SY_LBO + (r & 7) * 16 + (k & 3) * 4;
 }
 
-__global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0) {
+// Which tiles a launch updates (tile coordinates relative to the trailing
+// matrix): every lower tile, only the first tile column (the next panel's
+// columns, on the factorisation's critical path), or every tile right of it.
+enum SyrkTiles : int { SYRK_ALL = 0, SYRK_FIRST_COLUMN = 1, SYRK_REST = 2 };
+
+__global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int tiles) {
   extern __shared__ __align__(128) unsigned char s_raw[];
   unsigned char *planes = s_raw;  // A hi, A lo, B hi, B lo
   __shared__ unsigned long long s_mbar;
@@ -203,7 +210,16 @@ __global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0) {
   const int kb = min(BNB, m - k0);
   const int t0 = k0 + kb;
   int ti, tj;
-  tri_tile(blockIdx.x, ti, tj);
+  if (tiles == SYRK_FIRST_COLUMN) {
+    ti = blockIdx.x;
+    tj = 0;
+  } else {
+    tri_tile(blockIdx.x, ti, tj);
+    if (tiles == SYRK_REST) {
+      ++ti;
+      ++tj;
+    }
+  }
   const int i0 = t0 + BNB * ti, j0 = t0 + BNB * tj;
   if (i0 >= m) return;
   const int N = c.N;
@@ -708,6 +724,14 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
   }
   __syncthreads();
   if (tid == 0) {
+    // final refinement residual: that of the first iteration below the
+    // tolerance (later iterations were skipped), else of the last one
+    float fin = 0.f;
+    for (int it = 0; it < EEQ_BIG_REFINE; ++it) {
+      fin = __uint_as_float(c.w.eeq_res[b * EEQ_BIG_REFINE + it]);
+      if (fin < BIG_TOL) break;
+    }
+    c.w.eeq_final[2 * b + (adjoint ? 1 : 0)] = fin;
     double ta = 0.0, tb = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
       ta += s_a[w];
@@ -756,16 +780,58 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
 
 // ---------------------------------------------------------------- launch
 
-// Forward (adjoint = 0: factorisation, two right-hand sides, charges) or
-// adjoint (reuses the factor; one right-hand side dE/dq) multi-CTA EEQ.
-void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
+// Look-ahead of the factorisation.  The chain diagonal block -> panel ->
+// update of the next panel's columns is the critical path; it runs on a
+// high-priority stream of the library (one per device) while the caller's
+// stream carries the bulk of each trailing update, so that panel p + 1 is
+// factored while the columns right of it still receive panel p's update.
+// Events order the two streams:
+//   critical  diag(p), panel(p), record PANEL, wait BULK(p - 1),
+//             syrk(p, first column)            [columns of panel p + 1]
+//   caller    wait PANEL, syrk(p, rest), record BULK(p)   [columns >= p + 2]
+// BULK(p - 1) covers panel p + 1's columns, so the critical stream waits for
+// it before adding panel p's update to them (both read-modify-write those
+// tiles); diag(p + 1) and panel(p + 1) touch no column that syrk(p, rest)
+// writes.  The two events of BULK alternate with the parity of p.  Calls
+// that enqueue this schedule are serialised by a mutex (the events are
+// shared); the caller's stream waits for the critical stream at the end,
+// so the schedule also holds inside a stream capture.
+struct LookAhead {
+  cudaStream_t crit = nullptr;
+  cudaEvent_t fork = nullptr, panel = nullptr, bulk[2] = {nullptr, nullptr}, done = nullptr;
+  bool ok = false, tried = false;
+};
+static std::mutex g_la_mutex;
+static LookAhead g_la[64];
+
+// The device's look-ahead stream and events (created once; nullptr if the
+// runtime refuses them, in which case the factorisation runs on one stream).
+static LookAhead *lookahead_for_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  LookAhead &la = g_la[dev & 63];
+  if (!la.tried) {
+    la.tried = true;
+    int lo = 0, hi = 0;
+    bool ok = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&la.crit, cudaStreamNonBlocking, hi) == cudaSuccess;
+    cudaEvent_t *evs[5] = {&la.fork, &la.panel, &la.bulk[0], &la.bulk[1], &la.done};
+    for (cudaEvent_t *e : evs)
+      ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    la.ok = ok;
+    if (!ok) cudaGetLastError();  // clear the failed call's error
+  }
+  return la.ok ? &la : nullptr;
+}
+
+static void launch_factor(const Ctx &c, cudaStream_t st) {
   const int B = c.B, N = c.N;
   const int npan = (N + BNB - 1) / BNB;
-  if (!adjoint) {
-    cudaMemcpyAsync(c.w.eeq_F, c.w.eeq_hi, (size_t)4 * B * N * N, cudaMemcpyDeviceToDevice, st);
-    ensure_smem(eeq_big_diag_kernel, (int)eeq_big_diag_smem());
-    ensure_smem(eeq_big_panel_kernel, (int)eeq_big_panel_smem());
-    ensure_smem(eeq_big_syrk_kernel, (int)eeq_big_syrk_smem());
+  ensure_smem(eeq_big_diag_kernel, (int)eeq_big_diag_smem());
+  ensure_smem(eeq_big_panel_kernel, (int)eeq_big_panel_smem());
+  ensure_smem(eeq_big_syrk_kernel, (int)eeq_big_syrk_smem());
+  LookAhead *la = npan > 2 ? lookahead_for_device() : nullptr;
+  if (!la) {
     for (int p = 0; p < npan; ++p) {
       const int k0 = p * BNB;
       eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), st>>>(c, k0);
@@ -773,8 +839,47 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
       if (rest <= 0) break;
       eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), st>>>(c, k0);
       const int T = (rest + BNB - 1) / BNB;
-      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0);
+      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0,
+                                                                                  SYRK_ALL);
     }
+    return;
+  }
+  std::lock_guard<std::mutex> lock(g_la_mutex);
+  cudaStream_t cs = la->crit;
+  cudaEventRecord(la->fork, st);
+  cudaStreamWaitEvent(cs, la->fork, 0);
+  bool bulk_prev = false;  // whether BULK(p - 1) was recorded
+  for (int p = 0; p < npan; ++p) {
+    const int k0 = p * BNB;
+    eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), cs>>>(c, k0);
+    const int rest = N - k0 - BNB;
+    if (rest <= 0) break;
+    eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), cs>>>(c, k0);
+    const int T = (rest + BNB - 1) / BNB;
+    bool bulk_now = false;
+    if (T > 1) {
+      cudaEventRecord(la->panel, cs);
+      cudaStreamWaitEvent(st, la->panel, 0);
+      eeq_big_syrk_kernel<<<dim3((T - 1) * T / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0,
+                                                                                   SYRK_REST);
+      cudaEventRecord(la->bulk[p & 1], st);
+      bulk_now = true;
+    }
+    if (bulk_prev) cudaStreamWaitEvent(cs, la->bulk[(p - 1) & 1], 0);
+    eeq_big_syrk_kernel<<<dim3(T, B), BNB, eeq_big_syrk_smem(), cs>>>(c, k0, SYRK_FIRST_COLUMN);
+    bulk_prev = bulk_now;
+  }
+  cudaEventRecord(la->done, cs);
+  cudaStreamWaitEvent(st, la->done, 0);
+}
+
+// Forward (adjoint = 0: factorisation, two right-hand sides, charges) or
+// adjoint (reuses the factor; one right-hand side dE/dq) multi-CTA EEQ.
+void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
+  const int B = c.B, N = c.N;
+  if (!adjoint) {
+    cudaMemcpyAsync(c.w.eeq_F, c.w.eeq_hi, (size_t)4 * B * N * N, cudaMemcpyDeviceToDevice, st);
+    launch_factor(c, st);
   }
   const int nsb = eeq_nsb(N);
   if (!adjoint) {  // inverses of the 512-blocks, kept for the adjoint solve

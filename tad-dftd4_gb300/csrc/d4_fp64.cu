@@ -31,6 +31,8 @@ __global__ void __launch_bounds__(256) prep_kernel(Ctx c) {
   if (threadIdx.x == 0) {
     s_neff = 0;
     s_first = N;
+    c.w.eeq_final[2 * b] = 0.f;  // stays 0 where no refinement runs
+    c.w.eeq_final[2 * b + 1] = 0.f;
   }
   for (int e = threadIdx.x; e < MAX_ELEM_ID; e += blockDim.x) s_present[e] = 0;
   __syncthreads();

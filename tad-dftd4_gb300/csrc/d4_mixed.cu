@@ -2067,16 +2067,18 @@ __device__ float eeq_residual_df(const float *Hi, const float *Lo, const float2 
 }
 
 // FP32 factor + double-float refinement: X (nr columns) <- A^-1 BB to an
-// FP64-level residual below 1e-10.
-__device__ void eeq_refined_solve(const float *L, const float *Hi, const float *Lo, float2 *X,
-                                  const float2 *BB, float *vf, int m, int N, int nr,
-                                  float *s_red) {
+// FP64-level residual below 1e-10.  Returns the last residual max |r|
+// (uniform over the block).
+__device__ float eeq_refined_solve(const float *L, const float *Hi, const float *Lo, float2 *X,
+                                   const float2 *BB, float *vf, int m, int N, int nr,
+                                   float *s_red) {
   for (int t = threadIdx.x; t < m * nr; t += blockDim.x) {
     const int o = (t / m) * N + t % m;
     X[o] = make_float2(0.f, 0.f);
     vf[o] = BB[o].x;
   }
   __syncthreads();
+  float res = 0.f;
   for (int it = 0; it < EEQ_REFINE_MAX; ++it) {
     fwd_solve_blocked(L, vf, N, m, nr);
     bwd_solve_blocked(L, vf, N, m, nr);
@@ -2086,8 +2088,10 @@ __device__ void eeq_refined_solve(const float *L, const float *Hi, const float *
       X[o] = make_float2(s.hi, s.lo);
     }
     __syncthreads();
-    if (eeq_residual_df(Hi, Lo, X, BB, vf, m, N, nr, s_red) < EEQ_RESIDUAL_TOL) break;
+    res = eeq_residual_df(Hi, Lo, X, BB, vf, m, N, nr, s_red);
+    if (res < EEQ_RESIDUAL_TOL) break;
   }
+  return res;
 }
 
 template <bool SMEM>
@@ -2154,7 +2158,8 @@ __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_mixed_kernel(Ctx c) {
   __syncthreads();
   chol_blocked(L, PT, ldp, m, &s_bad);
   if (threadIdx.x == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
-  eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 2, s_red);
+  const float res = eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 2, s_red);
+  if (threadIdx.x == 0) c.w.eeq_final[2 * b] = res;
   if (warp == 0) {
     double sx = 0.0, sy = 0.0;
     for (int k = lane; k < m; k += 32) {
@@ -2225,7 +2230,8 @@ __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_adjoint_mixed_kernel(Ctx c
     BB[k] = make_float2(g.hi, g.lo);
   }
   __syncthreads();
-  eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 1, s_red);
+  const float res = eeq_refined_solve(L, Hi, Lo, X, BB, vf, m, N, 1, s_red);
+  if (threadIdx.x == 0) c.w.eeq_final[2 * b + 1] = res;
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31;
   if (warp == 0) {
     double su = 0.0;

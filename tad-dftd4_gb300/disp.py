@@ -115,6 +115,7 @@ class Runner:
     mixed: bool = False
     rvdw: torch.Tensor | None = None  # (B, N, N) pair radii of rvdw-type damping
     exact_c9: bool = False            # ATM with the exact C9 (DispD4Exact)
+    last_work: torch.Tensor | None = None  # workspace of the last call (residuals)
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
@@ -147,7 +148,9 @@ class Runner:
                   if cn_eeq_out else None)
         w = None if weights is None else weights.to(torch.float64).contiguous()
         ws_bytes = lib.d4_workspace_size(B, N, self.n_slots, flags)
+        self.last_work = None
         work = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
+        self.last_work = work
         p = self.params
         params = _lib.Params(
             s6=p["s6"], s8=p["s8"], s10=p["s10"], a1=p["a1"], a2=p["a2"], s9=p["s9"],
@@ -199,6 +202,22 @@ class Runner:
         if cn_eeq_out:
             return energy, grad, pgrad, qout, cnout, cnqout
         return energy, grad, pgrad, qout, cnout
+
+
+    def eeq_residuals(self) -> torch.Tensor:
+        """(B, 2) final EEQ refinement residuals max |A x - b| of the last
+        call (forward charges, adjoint solve) of the precision form; zeros
+        where no refinement ran.  Waits for the call to finish."""
+        if self.last_work is None:
+            raise RuntimeError("no call has run yet")
+        B = self.numbers.shape[0]
+        out = torch.empty((B, 2), dtype=torch.float32, pin_memory=True)
+        stream = torch.cuda.current_stream(self.last_work.device).cuda_stream
+        with torch.cuda.device(self.last_work.device):
+            _lib.check(_lib.load().d4_eeq_residuals(self.last_work.data_ptr(), B,
+                                                    out.data_ptr(), stream),
+                       "d4_eeq_residuals")
+        return out.clone()
 
 
 class _D4Function(torch.autograd.Function):

@@ -105,6 +105,9 @@ def test_charges_refined_to_fp64(d4):
                                  None, None, None, "mixed")
     out = runner.run(pt, charges_out=True, cn_eeq_out=True)
     q, cnq = out[3].cpu(), out[5].cpu()
+    res = runner.eeq_residuals()  # the refinement's own final residuals
+    assert (res[:, 0] < 1e-10).all() and res[:, 0].max() > 0, res
+    assert (res[:, 1] == 0).all()  # no adjoint solve in an energy-only call
     tables = oracle.load_tables()
     for k in range(len(b.numbers)):
         q_ref = _eeq_fp64(torch.from_numpy(b.numbers[k]), torch.from_numpy(b.positions[k]),
@@ -180,8 +183,10 @@ def test_multi_cta_eeq_and_atm_match_fp64_path(d4, sizes, pad):
     charge = np.array([1.0, -1.0][:B])
     dev = torch.device("cuda")
     nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (numbers, positions, charge))
-    mixed = _runner(nt, pt, ct, "mixed").run(pt, gradient=True, charges_out=True,
-                                             cn_eeq_out=True)
+    mixed_runner = _runner(nt, pt, ct, "mixed")
+    mixed = mixed_runner.run(pt, gradient=True, charges_out=True, cn_eeq_out=True)
+    res = mixed_runner.eeq_residuals()  # forward and adjoint refinements converged
+    assert (res < 1e-10).all() and res.max() > 0, res
     plain = _runner(nt, pt, ct, "fp64").run(pt, gradient=True, charges_out=True)
     e, g, q, cnq = mixed[0], mixed[1], mixed[3].cpu(), mixed[5].cpu()
     _check(e.cpu().numpy(), g.cpu().numpy(), plain[0].cpu().numpy(), plain[1].cpu().numpy())
