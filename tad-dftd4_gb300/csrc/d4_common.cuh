@@ -45,6 +45,13 @@ __host__ __device__ inline bool eeq_small_fits(int N) { return eeq_small_bytes(N
 constexpr int EEQ_BIG_REFINE = 4;  // refinement iterations of the multi-CTA path at most
 constexpr int EEQ_SB = 512;        // diagonal blocks inverted for the multi-CTA solves
 __host__ __device__ inline int eeq_nsb(int N) { return (N + EEQ_SB - 1) / EEQ_SB; }
+constexpr int EEQ_BNB = 128;       // panel width of the multi-CTA factorisation
+__host__ __device__ inline int eeq_nblk(int N) { return (N + EEQ_BNB - 1) / EEQ_BNB; }
+// Row stride (floats) of the multi-CTA factor: 16-byte rows for bulk copies.
+__host__ __device__ inline int eeq_ldf(int N) { return (N + 3) & ~3; }
+// Bytes of one row block's split panel operands: 8 chunks of 16 columns,
+// hi and lo planes of 128 rows x 16 TF32 values in the MMA's K-major layout.
+constexpr size_t EEQ_OPND_BLOCK = (size_t)8 * 2 * 8192;
 
 // ---------------------------------------------------------------- ATM sizes
 
@@ -144,7 +151,8 @@ struct Workspace {
   float4 *ptf;      // [B*N*N] (r^2, 1/r^2, (R0/r)^(alp/3), sqrt(C6(q=0)) / r^3)
   float4 *ptf_da;   // [B*N*N] (d log R0/d a1, d log R0/d a2, log(R0/r), 0)
   float *eeq_L32;   // [B*N*(N+1)/2] packed FP32 Cholesky factor (one-CTA path)
-  float *eeq_F;     // [B*N*N] dense FP32 factor, block inverses on the diagonal (multi-CTA)
+  float *eeq_F;     // [B][N][eeq_ldf(N)] dense FP32 factor, block inverses on the diagonal
+  unsigned char *eeq_P;  // [2][B][eeq_nblk(N)] split panel operands (EEQ_OPND_BLOCK each)
   float *eeq_V;     // [B*2*N] FP32 residual / correction (multi-CTA)
   float2 *eeq_X;    // [B*2*N] double-float solution (multi-CTA)
   float2 *eeq_B;    // [B*2*N] double-float right-hand sides (multi-CTA)
@@ -270,7 +278,8 @@ inline Workspace carve_workspace(void *base, int B, int N, int S, uint32_t flags
     if (eeq_small_fits(N)) {
       w.eeq_L32 = (float *)take(4 * (size_t)B * ((size_t)N * (N + 1) / 2));
     } else {
-      w.eeq_F = (float *)take(4 * BNN);
+      w.eeq_F = (float *)take(4 * BN * eeq_ldf(N));
+      w.eeq_P = (unsigned char *)take(2 * (size_t)B * eeq_nblk(N) * EEQ_OPND_BLOCK);
       w.eeq_V = (float *)take(4 * 2 * BN);
       w.eeq_X = (float2 *)take(8 * 2 * BN);
       w.eeq_B = (float2 *)take(8 * 2 * BN);

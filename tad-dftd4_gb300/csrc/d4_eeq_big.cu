@@ -59,13 +59,14 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   if (k0 >= m) return;
   const int kb = min(BNB, m - k0);
   const int N = c.N;
-  float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int NF = eeq_ldf(N);
+  float *F = c.w.eeq_F + (size_t)b * N * NF;
   const int tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) s_bad = 0;
   for (int t = tid; t < kb * (kb + 1) / 2; t += nt) {
     int i, j;
     tri_tile(t, i, j);
-    P[t] = F[(size_t)(k0 + i) * N + k0 + j];
+    P[t] = F[(size_t)(k0 + i) * NF + k0 + j];
   }
   __syncthreads();
   chol_blocked(P, PT, ldp, kb, &s_bad);
@@ -100,7 +101,7 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   }
   for (int t = tid; t < kb * kb; t += nt) {
     const int i = t / kb, j = t % kb;
-    if (j <= i) F[(size_t)(k0 + i) * N + k0 + j] = Xs[i * LX + j];
+    if (j <= i) F[(size_t)(k0 + i) * NF + k0 + j] = Xs[i * LX + j];
   }
 }
 
@@ -109,9 +110,29 @@ size_t eeq_big_diag_smem() {
   return 4 * (p + (size_t)32 * chol_panel_ld(BNB) + (size_t)BNB * (BNB + 1));
 }
 
-// Panel rows [t0 + 64 blockIdx.x, +64): L21 = A21 X^T (X lower, kb x kb).
-// Thread tile 4 rows x 8 columns; both operands transposed in shared memory.
-__global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
+// Split panel operands of the trailing updates: the rows of L21 as TF32
+// pairs hi = tf32(v), lo = tf32(v - hi), in 128-row blocks (relative to the
+// first trailing row), each block 8 chunks of 16 columns, each chunk a hi and
+// a lo plane of 128 rows x 16 values in the canonical K-major layout of the
+// MMA (LBO 128 bytes, SBO 512 bytes), so that a trailing-update CTA copies
+// its operands as contiguous 8 KB planes.  Two buffers, alternating with the
+// panel's parity (the look-ahead writes panel p + 1 while panel p is read).
+constexpr int SY_KC = 16;                       // K per chunk of the trailing update
+constexpr int SY_LBO = 128;                     // bytes between core matrices along K
+constexpr int SY_SBO = (SY_KC / 4) * SY_LBO;    // bytes between groups of 8 rows
+constexpr int SY_PLANE = (BNB / 8) * SY_SBO;    // bytes of one 128 x 16 plane (8192)
+constexpr int SY_NCH = BNB / SY_KC;             // chunks per panel
+static_assert(EEQ_BNB == BNB && (size_t)SY_NCH * 2 * SY_PLANE == EEQ_OPND_BLOCK,
+              "operand block layout");
+
+__device__ __forceinline__ unsigned char *opnd_block(const Ctx &c, int par, int b, int rb) {
+  return c.w.eeq_P + (((size_t)par * c.B + b) * eeq_nblk(c.N) + rb) * EEQ_OPND_BLOCK;
+}
+
+// Panel rows [t0 + 64 blockIdx.x, +64): L21 = A21 X^T (X lower, kb x kb),
+// written to F and, split, to the operand buffer ``par``.  Thread tile 4
+// rows x 8 columns; both operands transposed in shared memory.
+__global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int par) {
   extern __shared__ float4 s_dyn4[];
   constexpr int LXT = BNB + 4, LAT = 64 + 4;
   float *XT = reinterpret_cast<float *>(s_dyn4);  // XT[cc][col] = X[col][cc]
@@ -124,17 +145,18 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
   const int r0 = t0 + 64 * blockIdx.x;
   if (r0 >= m) return;
   const int N = c.N;
-  float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int NF = eeq_ldf(N);
+  float *F = c.w.eeq_F + (size_t)b * N * NF;
   const int tid = threadIdx.x;
   for (int t = tid; t < BNB * BNB; t += 256) {
     const int col = t / BNB, cc = t % BNB;  // coalesced over cc
     XT[cc * LXT + col] =
-        (col < kb && cc <= col) ? F[(size_t)(k0 + col) * N + k0 + cc] : 0.f;
+        (col < kb && cc <= col) ? F[(size_t)(k0 + col) * NF + k0 + cc] : 0.f;
   }
   for (int t = tid; t < 64 * BNB; t += 256) {
     const int row = t / BNB, cc = t % BNB;
     const int i = r0 + row;
-    AT[cc * LAT + row] = (i < m && cc < kb) ? F[(size_t)i * N + k0 + cc] : 0.f;
+    AT[cc * LAT + row] = (i < m && cc < kb) ? F[(size_t)i * NF + k0 + cc] : 0.f;
   }
   __syncthreads();
   const int ty = tid >> 4, tx = tid & 15;  // rows 4 ty .. +4, columns 8 tx .. +8
@@ -154,6 +176,9 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
 #pragma unroll
       for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], xv[u], acc[q][u]);
   }
+  // split operands only where a trailing update follows (full panels)
+  const bool split = kb == BNB;
+  const int ch = (8 * tx) / SY_KC, kk0 = (8 * tx) % SY_KC;  // 8 columns of one chunk
 #pragma unroll
   for (int q = 0; q < 4; ++q) {
     const int i = r0 + 4 * ty + q;
@@ -161,7 +186,25 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0) {
 #pragma unroll
     for (int u = 0; u < 8; ++u) {
       const int col = 8 * tx + u;
-      if (col < kb) F[(size_t)i * N + k0 + col] = acc[q][u];
+      if (col < kb) F[(size_t)i * NF + k0 + col] = acc[q][u];
+    }
+    if (split) {
+      const int rr = i - t0, r = rr & (BNB - 1);
+      unsigned char *blk = opnd_block(c, par, b, rr / BNB) + (size_t)ch * 2 * SY_PLANE +
+                           (r >> 3) * SY_SBO + (r & 7) * 16;
+#pragma unroll
+      for (int g = 0; g < 2; ++g) {  // columns kk0 + 4 g .. + 3: one 16-byte core-matrix row
+        float h[4], l[4];
+#pragma unroll
+        for (int e = 0; e < 4; ++e) {
+          const float v = acc[q][4 * g + e];
+          h[e] = tc::to_tf32(v);
+          l[e] = tc::to_tf32(v - h[e]);
+        }
+        const int off = ((kk0 + 4 * g) >> 2) * SY_LBO;
+        *reinterpret_cast<float4 *>(blk + off) = make_float4(h[0], h[1], h[2], h[3]);
+        *reinterpret_cast<float4 *>(blk + SY_PLANE + off) = make_float4(l[0], l[1], l[2], l[3]);
+      }
     }
   }
 }
@@ -170,45 +213,39 @@ size_t eeq_big_panel_smem() { return 4 * ((size_t)BNB * (BNB + 4) + (size_t)BNB 
 
 // Trailing update A22 -= L21 L21^T of the lower 128 x 128 tiles (ti >= tj)
 // right of the panel, on the tensor cores.  One CTA (128 threads) per tile:
-//  - the two 128 x kb row blocks of the panel are staged in chunks of 32
-//    columns, a warp reading one row per step (lanes over columns, 128-byte
-//    coalesced loads), split hi = tf32(v), lo = tf32(v - hi), into the
-//    canonical K-major layout with padded core-matrix strides (LBO = 144
-//    bytes, so the 32 lanes of a row store to 32 different banks);
-//  - one thread issues tcgen05 kind::tf32 MMAs (M = N = 128, lo hi, hi lo,
-//    hi hi per k-step) into a 128-column tensor-memory accumulator;
-//  - the tile goes from tensor memory through shared memory (thread = row)
-//    so that the warps update the matrix row by row with coalesced accesses.
+//  - the split operands of the tile's two row blocks (written by the panel
+//    kernel) arrive in chunks of 16 columns -- four 8 KB planes (A hi, A lo,
+//    B hi, B lo) -- by 16-byte asynchronous copies, double-buffered: the
+//    copies of chunk k + 1 are in flight while the tensor cores work on k;
+//  - one thread issues tcgen05 kind::tf32 MMAs (M = N = 128: lo hi, hi lo,
+//    hi hi per k-step of 8) into a 128-column tensor-memory accumulator;
+//  - the tile goes from tensor memory to shared memory (thread = row,
+//    negated) and every row is added to the matrix by one bulk reduction
+//    (cp.reduce.async.bulk .add.f32, performed at L2: no read of the matrix
+//    into the SM).  Diagonal tiles update their upper half too, which no
+//    later step reads; rows beyond the structure are skipped, columns
+//    beyond it receive sums of padding (never read).
 // The split products keep the update at about FP32 accuracy (a few 1e-7
 // relative), which the FP64 refinement of the solves absorbs.
-constexpr int SY_KC = 32;                    // panel columns per chunk
-constexpr int SY_LBO = 144;                  // bytes between core matrices along K (128 + 16)
-constexpr int SY_SBO = (SY_KC / 4) * SY_LBO; // bytes between groups of 8 rows
-constexpr int SY_PLANE = (BNB / 8) * SY_SBO; // bytes of one 128 x 32 operand
-constexpr int SY_COLS = 128;                 // tensor memory: the 128 x 128 tile
-constexpr int SY_TLD = BNB + 1;              // row stride (floats) of the staged result tile
-
-static_assert(4 * SY_PLANE >= 4 * BNB * SY_TLD, "the result tile reuses the operand planes");
-
-__device__ __forceinline__ int sy_off(int r, int k) {  // bytes
-  return (r >> 3) * SY_SBO + (k >> 2) * SY_LBO + (r & 7) * 16 + (k & 3) * 4;
-}
+constexpr int SY_STAGE = 4 * SY_PLANE;          // A hi, A lo, B hi, B lo of one chunk
+constexpr int SY_COLS = 128;                    // tensor memory: the 128 x 128 tile
+constexpr int SY_TLD = BNB + 4;                 // row stride (floats) of the staged tile
+constexpr int SY_SMEM =
+    (2 * SY_STAGE > 4 * BNB * SY_TLD) ? 2 * SY_STAGE : 4 * BNB * SY_TLD;
 
 // Which tiles a launch updates (tile coordinates relative to the trailing
 // matrix): every lower tile, only the first tile column (the next panel's
 // columns, on the factorisation's critical path), or every tile right of it.
 enum SyrkTiles : int { SYRK_ALL = 0, SYRK_FIRST_COLUMN = 1, SYRK_REST = 2 };
 
-__global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int tiles) {
-  extern __shared__ __align__(128) unsigned char s_raw[];
-  unsigned char *planes = s_raw;  // A hi, A lo, B hi, B lo
+__global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int tiles, int par) {
+  extern __shared__ __align__(1024) unsigned char s_raw[];
   __shared__ unsigned long long s_mbar;
   __shared__ uint32_t s_tmem;
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
-  if (k0 >= m) return;
-  const int kb = min(BNB, m - k0);
-  const int t0 = k0 + kb;
+  if (k0 + BNB >= m) return;  // no trailing matrix (a last, partial panel has none)
+  const int t0 = k0 + BNB;
   int ti, tj;
   if (tiles == SYRK_FIRST_COLUMN) {
     ti = blockIdx.x;
@@ -223,8 +260,11 @@ __global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int ti
   const int i0 = t0 + BNB * ti, j0 = t0 + BNB * tj;
   if (i0 >= m) return;
   const int N = c.N;
-  float *F = c.w.eeq_F + (size_t)b * N * N;
-  const int tid = threadIdx.x, warp = tid >> 5, lane = tid & 31;
+  const int NF = eeq_ldf(N);
+  float *F = c.w.eeq_F + (size_t)b * N * NF;
+  const unsigned char *PA = opnd_block(c, par, b, ti);
+  const unsigned char *PB = opnd_block(c, par, b, tj);
+  const int tid = threadIdx.x, warp = tid >> 5;
   const uint32_t mbar = tc::smem_u32(&s_mbar);
   if (warp == 0) tc::tmem_alloc(tc::smem_u32(&s_tmem), SY_COLS);
   if (tid == 0) tc::mbar_init(mbar, 1);
@@ -233,66 +273,67 @@ __global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int ti
   tc::fence_after_sync();
   const uint32_t tmem = s_tmem;
   constexpr uint32_t IDESC = tc::idesc_tf32(BNB, BNB);
-  const uint32_t p_base = tc::smem_u32(planes);
-  uint32_t parity = 0;
-  bool timed_out = false;
-  // a warp stages rows warp, warp + 4, ...; the loads of the next chunk are
-  // issued before the wait for the current chunk's MMAs
-  constexpr int RW = BNB / 4;  // rows per warp
-  float va[RW], vb[RW];
-  auto load_chunk = [&](int kc) {
-    const int k = kc + lane;
-    const bool kok = k < kb;
+  // chunk ch -> stage st: 32 KB, 16 bytes per thread and step
+  auto issue = [&](int ch, int st) {
+    unsigned char *dst = s_raw + st * SY_STAGE;
 #pragma unroll
-    for (int q = 0; q < RW; ++q) {
-      const int r = warp + 4 * q;
-      const int ia = i0 + r, jb = j0 + r;
-      va[q] = (kok && ia < m) ? F[(size_t)ia * N + k0 + k] : 0.f;
-      vb[q] = (kok && jb < m) ? F[(size_t)jb * N + k0 + k] : 0.f;
+    for (int q = 0; q < SY_STAGE / (16 * BNB); ++q) {
+      const int byte = (q * BNB + tid) * 16;
+      const int plane = byte / SY_PLANE, off = byte % SY_PLANE;  // A hi, A lo, B hi, B lo
+      const unsigned char *src =
+          (plane < 2 ? PA : PB) + ((size_t)ch * 2 + (plane & 1)) * SY_PLANE + off;
+      tc::cp_async16(dst + byte, src);
     }
+    tc::cp_async_commit();
   };
-  load_chunk(0);
-  for (int kc = 0; kc < kb; kc += SY_KC) {
-#pragma unroll
-    for (int q = 0; q < RW; ++q) {
-      const int off = sy_off(warp + 4 * q, lane);
-      const float ah = tc::to_tf32(va[q]), bh = tc::to_tf32(vb[q]);
-      *reinterpret_cast<float *>(planes + off) = ah;
-      *reinterpret_cast<float *>(planes + SY_PLANE + off) = tc::to_tf32(va[q] - ah);
-      *reinterpret_cast<float *>(planes + 2 * SY_PLANE + off) = bh;
-      *reinterpret_cast<float *>(planes + 3 * SY_PLANE + off) = tc::to_tf32(vb[q] - bh);
+  issue(0, 0);
+  bool timed_out = false;
+  int last = -1;  // last chunk whose MMAs were committed (uniform over the CTA)
+  for (int ch = 0; ch < SY_NCH; ++ch) {
+    // stage (ch + 1) & 1 was read by the MMAs of chunk ch - 1
+    if (ch > 0) {
+      const bool done = tc::mbar_wait(mbar, (uint32_t)((ch - 1) & 1));
+      if (__syncthreads_or(!done)) {
+        timed_out = true;
+        break;
+      }
+    }
+    if (ch + 1 < SY_NCH) {
+      issue(ch + 1, (ch + 1) & 1);
+      tc::cp_async_wait<1>();
+    } else {
+      tc::cp_async_wait<0>();
     }
     tc::fence_async_smem();
     __syncthreads();
     if (tid == 0) {
       tc::fence_after_sync();
+      const uint32_t base = tc::smem_u32(s_raw + (ch & 1) * SY_STAGE);
 #pragma unroll
       for (int pr = 0; pr < 3; ++pr) {  // lo hi, hi lo, hi hi
-        const uint32_t ab = p_base + (pr == 0 ? SY_PLANE : 0);
-        const uint32_t bb = p_base + 2 * SY_PLANE + (pr == 1 ? SY_PLANE : 0);
+        const uint32_t ab = base + (pr == 0 ? SY_PLANE : 0);
+        const uint32_t bb = base + 2 * SY_PLANE + (pr == 1 ? SY_PLANE : 0);
 #pragma unroll
-        for (int s = 0; s < SY_KC / 8; ++s)
-          tc::mma_tf32(tmem, tc::desc_kmajor(ab + 2 * SY_LBO * s, SY_LBO, SY_SBO),
-                       tc::desc_kmajor(bb + 2 * SY_LBO * s, SY_LBO, SY_SBO), IDESC,
-                       (kc > 0 || pr > 0 || s > 0) ? 1u : 0u);
+        for (int s8 = 0; s8 < SY_KC / 8; ++s8)
+          tc::mma_tf32(tmem, tc::desc_kmajor(ab + 2 * SY_LBO * s8, SY_LBO, SY_SBO),
+                       tc::desc_kmajor(bb + 2 * SY_LBO * s8, SY_LBO, SY_SBO), IDESC,
+                       (ch > 0 || pr > 0 || s8 > 0) ? 1u : 0u);
       }
       tc::commit(mbar);
     }
-    if (kc + SY_KC < kb) load_chunk(kc + SY_KC);
-    const bool done = tc::mbar_wait(mbar, parity);
-    parity ^= 1u;
-    if (__syncthreads_or(!done)) {
-      timed_out = true;
-      break;
-    }
+    last = ch;
   }
-  if (timed_out) {
+  tc::cp_async_wait<0>();  // nothing of ours may land in shared memory after we leave
+  const bool last_done = !timed_out && tc::mbar_wait(mbar, (uint32_t)(last & 1));
+  if (__syncthreads_or(!last_done)) {
     if (tid == 0) set_status(c.w.status, D4_ERR_DEVICE_TIMEOUT);
-    tc::mbar_wait(mbar, parity ^ 1u);
+    // one more bounded wait for the last committed MMAs, then release
+    if (last >= 0) tc::mbar_wait(mbar, (uint32_t)(last & 1));
   } else {
-    // tensor memory -> shared tile (thread = row) -> row-wise coalesced update
+    // tensor memory -> shared tile (thread = row, negated) -> one bulk
+    // reduction per row into the matrix
     tc::fence_after_sync();
-    float *T = reinterpret_cast<float *>(planes);
+    float *T = reinterpret_cast<float *>(s_raw);
     const uint32_t t_lane = (uint32_t)(warp * 32) << 16;
 #pragma unroll 1
     for (int cc = 0; cc < BNB; cc += 16) {
@@ -300,31 +341,18 @@ __global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int ti
       tc::tmem_ld16(tmem + t_lane + cc, v);
       tc::tmem_ld_wait();
 #pragma unroll
-      for (int u = 0; u < 16; ++u) T[tid * SY_TLD + cc + u] = __uint_as_float(v[u]);
+      for (int u = 0; u < 16; u += 4)
+        *reinterpret_cast<float4 *>(T + tid * SY_TLD + cc + u) =
+            make_float4(-__uint_as_float(v[u]), -__uint_as_float(v[u + 1]),
+                        -__uint_as_float(v[u + 2]), -__uint_as_float(v[u + 3]));
     }
-    __syncthreads();
-    // 8 rows per step with all their loads in flight before the stores
-#pragma unroll 1
-    for (int r0 = warp; r0 < BNB; r0 += 32) {
-      float cur[8][BNB / 32];
-#pragma unroll
-      for (int h = 0; h < 8; ++h) {
-        const int i = i0 + r0 + 4 * h;
-#pragma unroll
-        for (int q = 0; q < BNB / 32; ++q) {
-          const int j = j0 + q * 32 + lane;
-          cur[h][q] = (i < m && j < m && j <= i) ? F[(size_t)i * N + j] : 0.f;
-        }
-      }
-#pragma unroll
-      for (int h = 0; h < 8; ++h) {
-        const int r = r0 + 4 * h, i = i0 + r;
-#pragma unroll
-        for (int q = 0; q < BNB / 32; ++q) {
-          const int jl = q * 32 + lane, j = j0 + jl;
-          if (i < m && j < m && j <= i) F[(size_t)i * N + j] = cur[h][q] - T[r * SY_TLD + jl];
-        }
-      }
+    const int i = i0 + tid;
+    if (i < m) {
+      tc::fence_async_smem();
+      const int ncol = min(BNB, NF - j0);  // a multiple of 4: NF and j0 are
+      tc::bulk_reduce_add_f32(F + (size_t)i * NF + j0, T + tid * SY_TLD, (uint32_t)(4 * ncol));
+      tc::bulk_commit();
+      tc::bulk_wait_read();
     }
   }
   tc::fence_before_sync();
@@ -335,7 +363,7 @@ __global__ void __launch_bounds__(BNB) eeq_big_syrk_kernel(Ctx c, int k0, int ti
   }
 }
 
-size_t eeq_big_syrk_smem() { return (size_t)4 * SY_PLANE; }
+size_t eeq_big_syrk_smem() { return (size_t)SY_SMEM; }
 
 // ---------------------------------------------------------------- solves
 
@@ -387,13 +415,14 @@ __global__ void __launch_bounds__(256) eeq_blkinv_init_kernel(Ctx c) {
   const int s0 = sblk * EEQ_SB;
   if (s0 >= m) return;
   const int N = c.N;
-  const float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int NF = eeq_ldf(N);
+  const float *F = c.w.eeq_F + (size_t)b * N * NF;
   float *X = xd_block(c, b, sblk);
   for (int t = threadIdx.x; t < EEQ_SB * EEQ_SB; t += blockDim.x) {
     const int i = t / EEQ_SB, j = t % EEQ_SB;
     const int gi = s0 + i, gj = s0 + j;
     const bool diag = (i / BNB) == (j / BNB) && j <= i && gi < m;
-    X[t] = diag ? F[(size_t)gi * N + gj] : 0.f;
+    X[t] = diag ? F[(size_t)gi * NF + gj] : 0.f;
   }
 }
 
@@ -413,7 +442,8 @@ __global__ void __launch_bounds__(256) eeq_blkinv_step_kernel(Ctx c, int r) {
   const int s0 = sblk * EEQ_SB;
   if (s0 + r * BNB >= m) return;  // sub-block row r does not exist
   const int N = c.N;
-  const float *F = c.w.eeq_F + (size_t)b * N * N;
+  const int NF = eeq_ldf(N);
+  const float *F = c.w.eeq_F + (size_t)b * N * NF;
   float *X = xd_block(c, b, sblk);
   const int tid = threadIdx.x, ty = tid >> 4, tx = tid & 15;
   const int lrow = tid >> 1, lcol = (tid & 1) * 8;
@@ -430,7 +460,7 @@ __global__ void __launch_bounds__(256) eeq_blkinv_step_kernel(Ctx c, int r) {
       for (int q = 0; q < 8; ++q) {
         const int kk = lcol + q;
         const int gi = gr0 + lrow, gk = s0 + j * BNB + k0 + kk;
-        As[kk * LD + lrow] = (gi < m && gk < m) ? F[(size_t)gi * N + gk] : 0.f;
+        As[kk * LD + lrow] = (gi < m && gk < m) ? F[(size_t)gi * NF + gk] : 0.f;
         Bs[kk * LD + lrow] = X[(size_t)(j * BNB + k0 + kk) * EEQ_SB + cc * BNB + lrow];
       }
       __syncthreads();
@@ -554,7 +584,8 @@ __global__ void __launch_bounds__(256) eeq_sweep_below_kernel(Ctx c, int sblk, i
   if (i >= m) return;
   const int lane = threadIdx.x & 31;
   const int N = c.N;
-  const float *row = c.w.eeq_F + (size_t)b * N * N + (size_t)i * N + s0;
+  const int NF = eeq_ldf(N);
+  const float *row = c.w.eeq_F + (size_t)b * N * NF + (size_t)i * NF + s0;
   const float *Y = c.w.eeq_Y + (size_t)b * 2 * N + s0;
   float *V = c.w.eeq_V + (size_t)b * 2 * N;
   float a0 = 0.f, a1 = 0.f;
@@ -595,13 +626,14 @@ __global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, i
   const int i = blockIdx.x * AB_ROWS + rr;
   float a0 = 0.f, a1 = 0.f;
   if (i < s0) {
-    const float *F = c.w.eeq_F + (size_t)b * N * N + (size_t)s0 * N + i;
+    const int NF = eeq_ldf(N);
+    const float *F = c.w.eeq_F + (size_t)b * N * NF + (size_t)s0 * NF + i;
     const int kq = EEQ_SB / 4;
     const int k_lo = qk * kq, k_hi = min(kb, k_lo + kq);
     float b0 = 0.f, b1 = 0.f;
 #pragma unroll 4
     for (int k = k_lo; k < k_hi; ++k) {
-      const float x = F[(size_t)k * N];
+      const float x = F[(size_t)k * NF];
       if (k & 1) {
         b0 = fmaf(x, s_v[0][k], b0);
         if (nr == 2) b1 = fmaf(x, s_v[1][k], b1);
@@ -837,10 +869,11 @@ static void launch_factor(const Ctx &c, cudaStream_t st) {
       eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), st>>>(c, k0);
       const int rest = N - k0 - BNB;
       if (rest <= 0) break;
-      eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), st>>>(c, k0);
+      eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), st>>>(c, k0,
+                                                                                       p & 1);
       const int T = (rest + BNB - 1) / BNB;
-      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0,
-                                                                                  SYRK_ALL);
+      eeq_big_syrk_kernel<<<dim3(T * (T + 1) / 2, B), BNB, eeq_big_syrk_smem(), st>>>(
+          c, k0, SYRK_ALL, p & 1);
     }
     return;
   }
@@ -854,19 +887,21 @@ static void launch_factor(const Ctx &c, cudaStream_t st) {
     eeq_big_diag_kernel<<<B, 512, eeq_big_diag_smem(), cs>>>(c, k0);
     const int rest = N - k0 - BNB;
     if (rest <= 0) break;
-    eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), cs>>>(c, k0);
+    eeq_big_panel_kernel<<<dim3((rest + 63) / 64, B), 256, eeq_big_panel_smem(), cs>>>(c, k0,
+                                                                                     p & 1);
     const int T = (rest + BNB - 1) / BNB;
     bool bulk_now = false;
     if (T > 1) {
       cudaEventRecord(la->panel, cs);
       cudaStreamWaitEvent(st, la->panel, 0);
-      eeq_big_syrk_kernel<<<dim3((T - 1) * T / 2, B), BNB, eeq_big_syrk_smem(), st>>>(c, k0,
-                                                                                   SYRK_REST);
+      eeq_big_syrk_kernel<<<dim3((T - 1) * T / 2, B), BNB, eeq_big_syrk_smem(), st>>>(
+          c, k0, SYRK_REST, p & 1);
       cudaEventRecord(la->bulk[p & 1], st);
       bulk_now = true;
     }
     if (bulk_prev) cudaStreamWaitEvent(cs, la->bulk[(p - 1) & 1], 0);
-    eeq_big_syrk_kernel<<<dim3(T, B), BNB, eeq_big_syrk_smem(), cs>>>(c, k0, SYRK_FIRST_COLUMN);
+    eeq_big_syrk_kernel<<<dim3(T, B), BNB, eeq_big_syrk_smem(), cs>>>(c, k0, SYRK_FIRST_COLUMN,
+                                                                      p & 1);
     bulk_prev = bulk_now;
   }
   cudaEventRecord(la->done, cs);
@@ -878,7 +913,8 @@ static void launch_factor(const Ctx &c, cudaStream_t st) {
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int B = c.B, N = c.N;
   if (!adjoint) {
-    cudaMemcpyAsync(c.w.eeq_F, c.w.eeq_hi, (size_t)4 * B * N * N, cudaMemcpyDeviceToDevice, st);
+    cudaMemcpy2DAsync(c.w.eeq_F, (size_t)4 * eeq_ldf(N), c.w.eeq_hi, (size_t)4 * N,
+                      (size_t)4 * N, (size_t)B * N, cudaMemcpyDeviceToDevice, st);
     launch_factor(c, st);
   }
   const int nsb = eeq_nsb(N);

@@ -168,5 +168,40 @@ __device__ __forceinline__ void tmem_ld_wait() {
   asm volatile("tcgen05.wait::ld.sync.aligned;" ::: "memory");
 }
 
+// 16-byte asynchronous copy global -> shared (bypassing L1), completed by
+// cp_async_wait; commit groups the copies issued so far by this thread.
+__device__ __forceinline__ void cp_async16(void *smem_dst, const void *gmem_src) {
+  asm volatile("cp.async.cg.shared.global [%0], [%1], 16;" ::"r"(smem_u32(smem_dst)),
+               "l"(gmem_src)
+               : "memory");
+}
+__device__ __forceinline__ void cp_async_commit() {
+  asm volatile("cp.async.commit_group;" ::: "memory");
+}
+// Wait until at most N of this thread's committed groups are still in flight.
+template <int N>
+__device__ __forceinline__ void cp_async_wait() {
+  asm volatile("cp.async.wait_group %0;" ::"n"(N) : "memory");
+}
+
+// dst[0 .. bytes/4) += src[...] (FP32, element-wise, performed at L2) from
+// shared memory, asynchronously; bytes a multiple of 16, both addresses
+// 16-byte aligned.  bulk_commit groups the operations issued so far by this
+// thread and bulk_wait_read waits until their shared-memory sources have been
+// read (the writes to global memory complete before the kernel ends).
+__device__ __forceinline__ void bulk_reduce_add_f32(float *gmem_dst, const float *smem_src,
+                                                    uint32_t bytes) {
+  asm volatile(
+      "cp.reduce.async.bulk.global.shared::cta.bulk_group.add.f32 [%0], [%1], %2;" ::"l"(gmem_dst),
+      "r"(smem_u32(smem_src)), "r"(bytes)
+      : "memory");
+}
+__device__ __forceinline__ void bulk_commit() {
+  asm volatile("cp.async.bulk.commit_group;" ::: "memory");
+}
+__device__ __forceinline__ void bulk_wait_read() {
+  asm volatile("cp.async.bulk.wait_group.read 0;" ::: "memory");
+}
+
 }  // namespace tc
 }  // namespace d4

@@ -163,8 +163,9 @@ def _runner(nt, pt, ct, precision):
     return runner
 
 
-@pytest.mark.parametrize("sizes,pad", [((330, 380), 400), ((700,), 700)],
-                         ids=["two-structures-N400", "one-structure-N700"])
+@pytest.mark.parametrize("sizes,pad", [((330, 380), 400), ((700,), 700), ((299,), 301)],
+                         ids=["two-structures-N400", "one-structure-N700",
+                              "odd-row-stride-N301"])
 def test_multi_cta_eeq_and_atm_match_fp64_path(d4, sizes, pad):
     """Structures padded beyond the one-CTA EEQ limit (N > 290) take the
     multi-CTA factorisation (128-column panels, SYRK trailing updates, block
