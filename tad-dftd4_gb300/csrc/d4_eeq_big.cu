@@ -43,16 +43,17 @@ __device__ __forceinline__ bool big_skip(const Ctx &c, int b, int it) {
 
 // ---------------------------------------------------------------- factor
 
-// Diagonal block [k0, k0 + kb) of structure b: Cholesky in shared memory,
-// then the full inverse X of the kb x kb factor by block forward
-// substitution (X_cc = D_c^-1, X_rc = -D_r^-1 sum_k L_rk X_kc), written over
-// the block (lower part).
+// Diagonal block [k0, k0 + kb) of structure b: Cholesky in shared memory
+// (chol_blocked), written back over the block in the form the panel solve
+// works from: the factor below the 32 x 32 diagonal blocks and the inverses
+// of those blocks in their place.  The full inverse of the block, which the
+// sweeps need, is formed after the factorisation for all panels at once
+// (eeq_big_pinv_kernel), off the factorisation's critical path.
 __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   extern __shared__ float4 s_dyn4[];
   float *P = reinterpret_cast<float *>(s_dyn4);  // packed kb x kb
   const int ldp = chol_panel_ld(BNB);
-  float *PT = P + ((BNB * (BNB + 1) / 2 + 3) & ~3);  // 32 x ldp, also the T scratch
-  float *Xs = PT + 32 * ldp;                        // dense [BNB][BNB + 1]
+  float *PT = P + ((BNB * (BNB + 1) / 2 + 3) & ~3);  // 32 x ldp
   __shared__ int s_bad;
   const int b = blockIdx.x;
   const int m = c.w.n_real[b];
@@ -63,7 +64,8 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   float *F = c.w.eeq_F + (size_t)b * N * NF;
   const int tid = threadIdx.x, nt = blockDim.x;
   if (tid == 0) s_bad = 0;
-  for (int t = tid; t < kb * (kb + 1) / 2; t += nt) {
+  const int tri = kb * (kb + 1) / 2;
+  for (int t = tid; t < tri; t += nt) {
     int i, j;
     tri_tile(t, i, j);
     P[t] = F[(size_t)(k0 + i) * NF + k0 + j];
@@ -71,6 +73,43 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   __syncthreads();
   chol_blocked(P, PT, ldp, kb, &s_bad);
   if (tid == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
+  for (int t = tid; t < tri; t += nt) {
+    int i, j;
+    tri_tile(t, i, j);
+    F[(size_t)(k0 + i) * NF + k0 + j] = P[t];
+  }
+}
+
+size_t eeq_big_diag_smem() {
+  const size_t p = (BNB * (BNB + 1) / 2 + 3) & ~3;
+  return 4 * (p + (size_t)32 * chol_panel_ld(BNB));
+}
+
+// Full inverse X of every panel's diagonal block (grid: panels x
+// structures), from the diagonal kernel's form: block forward substitution
+// (X_cc = D_c^-1, X_rc = -D_r^-1 sum_k L_rk X_kc), written over the block
+// (lower part).  The block sweeps and the 512-block inverses use it.
+__global__ void __launch_bounds__(512) eeq_big_pinv_kernel(Ctx c) {
+  extern __shared__ float4 s_dyn4[];
+  float *P = reinterpret_cast<float *>(s_dyn4);  // packed kb x kb
+  const int ldp = chol_panel_ld(BNB);
+  float *PT = P + ((BNB * (BNB + 1) / 2 + 3) & ~3);  // T scratch, 32 x ldp
+  float *Xs = PT + 32 * ldp;                         // dense [BNB][BNB + 1]
+  const int k0 = blockIdx.x * BNB, b = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (k0 >= m) return;
+  const int kb = min(BNB, m - k0);
+  const int N = c.N;
+  const int NF = eeq_ldf(N);
+  float *F = c.w.eeq_F + (size_t)b * N * NF;
+  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tri = kb * (kb + 1) / 2;
+  for (int t = tid; t < tri; t += nt) {
+    int i, j;
+    tri_tile(t, i, j);
+    P[t] = F[(size_t)(k0 + i) * NF + k0 + j];
+  }
+  __syncthreads();
   constexpr int LX = BNB + 1;
   // X = 0, diagonal 32-blocks = their inverses (held by P)
   for (int t = tid; t < BNB * BNB; t += nt) {
@@ -105,7 +144,7 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   }
 }
 
-size_t eeq_big_diag_smem() {
+size_t eeq_big_pinv_smem() {
   const size_t p = (BNB * (BNB + 1) / 2 + 3) & ~3;
   return 4 * (p + (size_t)32 * chol_panel_ld(BNB) + (size_t)BNB * (BNB + 1));
 }
@@ -129,14 +168,18 @@ __device__ __forceinline__ unsigned char *opnd_block(const Ctx &c, int par, int 
   return c.w.eeq_P + (((size_t)par * c.B + b) * eeq_nblk(c.N) + rb) * EEQ_OPND_BLOCK;
 }
 
-// Panel rows [t0 + 64 blockIdx.x, +64): L21 = A21 X^T (X lower, kb x kb),
-// written to F and, split, to the operand buffer ``par``.  Thread tile 4
-// rows x 8 columns; both operands transposed in shared memory.
+// Panel rows [t0 + 64 blockIdx.x, +64): L21 solves L21 L11^T = A21, by
+// block substitution over the panel's 32-column blocks with the diagonal
+// kernel's form of L11 (factor below the 32 x 32 diagonal blocks, their
+// inverses D^-1 on them):  Y_c = (A_c - sum_{k < c} Y_k L_ck^T) D_c^-T.
+// Written to F and, split, to the operand buffer ``par``.  Thread tile 2
+// rows x 4 columns of the current 32-column block; L11 transposed and the
+// rows transposed in shared memory.
+constexpr int PN_LLT = BNB + 4, PN_LAT = 64 + 2;
 __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int par) {
   extern __shared__ float4 s_dyn4[];
-  constexpr int LXT = BNB + 4, LAT = 64 + 4;
-  float *XT = reinterpret_cast<float *>(s_dyn4);  // XT[cc][col] = X[col][cc]
-  float *AT = XT + BNB * LXT;                      // AT[cc][row] = A21[row][cc]
+  float *LT = reinterpret_cast<float *>(s_dyn4);  // LT[k][col] = L11[col][k], 0 for k > col
+  float *AT = LT + BNB * PN_LLT;                   // AT[cc][row] = A21[row][cc], then L21
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   if (k0 >= m) return;
@@ -149,67 +192,98 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int p
   float *F = c.w.eeq_F + (size_t)b * N * NF;
   const int tid = threadIdx.x;
   for (int t = tid; t < BNB * BNB; t += 256) {
-    const int col = t / BNB, cc = t % BNB;  // coalesced over cc
-    XT[cc * LXT + col] =
-        (col < kb && cc <= col) ? F[(size_t)(k0 + col) * NF + k0 + cc] : 0.f;
+    const int col = t / BNB, k = t % BNB;  // coalesced over k
+    LT[k * PN_LLT + col] = (col < kb && k <= col) ? F[(size_t)(k0 + col) * NF + k0 + k] : 0.f;
   }
   for (int t = tid; t < 64 * BNB; t += 256) {
     const int row = t / BNB, cc = t % BNB;
     const int i = r0 + row;
-    AT[cc * LAT + row] = (i < m && cc < kb) ? F[(size_t)i * NF + k0 + cc] : 0.f;
+    AT[cc * PN_LAT + row] = (i < m && cc < kb) ? F[(size_t)i * NF + k0 + cc] : 0.f;
   }
   __syncthreads();
-  const int ty = tid >> 4, tx = tid & 15;  // rows 4 ty .. +4, columns 8 tx .. +8
-  float acc[4][8];
+  const int ty = tid >> 3, tx = tid & 7;  // rows 2 ty, 2 ty + 1; columns 4 tx .. + 3 of a block
+  const int nb32 = (kb + 31) >> 5;
+  for (int cb = 0; cb < nb32; ++cb) {
+    const int c0 = 32 * cb + 4 * tx;
+    float acc[2][4];
 #pragma unroll
-  for (int q = 0; q < 4; ++q)
+    for (int v = 0; v < 2; ++v)
 #pragma unroll
-    for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
-  for (int cc = 0; cc < kb; ++cc) {
-    const float4 a = *reinterpret_cast<const float4 *>(AT + cc * LAT + 4 * ty);
-    const float4 x0 = *reinterpret_cast<const float4 *>(XT + cc * LXT + 8 * tx);
-    const float4 x1 = *reinterpret_cast<const float4 *>(XT + cc * LXT + 8 * tx + 4);
-    const float av[4] = {a.x, a.y, a.z, a.w};
-    const float xv[8] = {x0.x, x0.y, x0.z, x0.w, x1.x, x1.y, x1.z, x1.w};
+      for (int u = 0; u < 4; ++u) acc[v][u] = 0.f;
+    // sum_{k < 32 cb} Y_k L_ck^T (Y of the earlier blocks is in AT)
+    for (int k = 0; k < 32 * cb; ++k) {
+      const float2 y = *reinterpret_cast<const float2 *>(AT + k * PN_LAT + 2 * ty);
+      const float4 l = *reinterpret_cast<const float4 *>(LT + k * PN_LLT + c0);
+      const float lv[4] = {l.x, l.y, l.z, l.w};
 #pragma unroll
-    for (int q = 0; q < 4; ++q)
-#pragma unroll
-      for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(av[q], xv[u], acc[q][u]);
-  }
-  // split operands only where a trailing update follows (full panels)
-  const bool split = kb == BNB;
-  const int ch = (8 * tx) / SY_KC, kk0 = (8 * tx) % SY_KC;  // 8 columns of one chunk
-#pragma unroll
-  for (int q = 0; q < 4; ++q) {
-    const int i = r0 + 4 * ty + q;
-    if (i >= m) continue;
-#pragma unroll
-    for (int u = 0; u < 8; ++u) {
-      const int col = 8 * tx + u;
-      if (col < kb) F[(size_t)i * NF + k0 + col] = acc[q][u];
-    }
-    if (split) {
-      const int rr = i - t0, r = rr & (BNB - 1);
-      unsigned char *blk = opnd_block(c, par, b, rr / BNB) + (size_t)ch * 2 * SY_PLANE +
-                           (r >> 3) * SY_SBO + (r & 7) * 16;
-#pragma unroll
-      for (int g = 0; g < 2; ++g) {  // columns kk0 + 4 g .. + 3: one 16-byte core-matrix row
-        float h[4], l[4];
-#pragma unroll
-        for (int e = 0; e < 4; ++e) {
-          const float v = acc[q][4 * g + e];
-          h[e] = tc::to_tf32(v);
-          l[e] = tc::to_tf32(v - h[e]);
-        }
-        const int off = ((kk0 + 4 * g) >> 2) * SY_LBO;
-        *reinterpret_cast<float4 *>(blk + off) = make_float4(h[0], h[1], h[2], h[3]);
-        *reinterpret_cast<float4 *>(blk + SY_PLANE + off) = make_float4(l[0], l[1], l[2], l[3]);
+      for (int u = 0; u < 4; ++u) {
+        acc[0][u] = fmaf(y.x, lv[u], acc[0][u]);
+        acc[1][u] = fmaf(y.y, lv[u], acc[1][u]);
       }
+    }
+    // Z_c = A_c - that, in place (each entry read and written by its thread)
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float *z = AT + (c0 + u) * PN_LAT + 2 * ty;
+      z[0] -= acc[0][u];
+      z[1] -= acc[1][u];
+    }
+    __syncthreads();
+    // Y_c = Z_c D_c^-T: Y[r][c] = sum_q Z[r][q] D^-1[c][q] (LT is 0 above)
+    float y[2][4];
+#pragma unroll
+    for (int v = 0; v < 2; ++v)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) y[v][u] = 0.f;
+#pragma unroll 4
+    for (int q = 32 * cb; q < 32 * cb + 32; ++q) {
+      const float2 zr = *reinterpret_cast<const float2 *>(AT + q * PN_LAT + 2 * ty);
+      const float4 l = *reinterpret_cast<const float4 *>(LT + q * PN_LLT + c0);
+      const float lv[4] = {l.x, l.y, l.z, l.w};
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        y[0][u] = fmaf(zr.x, lv[u], y[0][u]);
+        y[1][u] = fmaf(zr.y, lv[u], y[1][u]);
+      }
+    }
+    __syncthreads();  // every thread has read Z_c
+#pragma unroll
+    for (int u = 0; u < 4; ++u) {
+      float *z = AT + (c0 + u) * PN_LAT + 2 * ty;
+      z[0] = y[0][u];
+      z[1] = y[1][u];
+    }
+    __syncthreads();
+  }
+  // L21 rows to F (warp per row, lanes over 4-column groups) and, split, to
+  // the operands of the trailing update (only full panels have one)
+  const bool split = kb == BNB;
+  const int warp = tid >> 5, lane = tid & 31;
+  const int col = 4 * lane;
+  for (int rr = warp; rr < 64; rr += 8) {
+    const int i = r0 + rr;
+    if (i >= m || col >= kb) continue;
+    float v[4];
+#pragma unroll
+    for (int e = 0; e < 4; ++e) v[e] = AT[(col + e) * PN_LAT + rr];
+    *reinterpret_cast<float4 *>(F + (size_t)i * NF + k0 + col) = make_float4(v[0], v[1], v[2], v[3]);
+    if (split) {
+      const int q = i - t0, r = q & (BNB - 1);
+      unsigned char *dst = opnd_block(c, par, b, q / BNB) + (size_t)(col / SY_KC) * 2 * SY_PLANE +
+                           (r >> 3) * SY_SBO + ((col % SY_KC) >> 2) * SY_LBO + (r & 7) * 16;
+      float h[4], l[4];
+#pragma unroll
+      for (int e = 0; e < 4; ++e) {
+        h[e] = tc::to_tf32(v[e]);
+        l[e] = tc::to_tf32(v[e] - h[e]);
+      }
+      *reinterpret_cast<float4 *>(dst) = make_float4(h[0], h[1], h[2], h[3]);
+      *reinterpret_cast<float4 *>(dst + SY_PLANE) = make_float4(l[0], l[1], l[2], l[3]);
     }
   }
 }
 
-size_t eeq_big_panel_smem() { return 4 * ((size_t)BNB * (BNB + 4) + (size_t)BNB * (64 + 4)); }
+size_t eeq_big_panel_smem() { return 4 * ((size_t)BNB * PN_LLT + (size_t)BNB * PN_LAT); }
 
 // Trailing update A22 -= L21 L21^T of the lower 128 x 128 tiles (ti >= tj)
 // right of the panel, on the tensor cores.  One CTA (128 threads) per tile:
@@ -918,7 +992,9 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
     launch_factor(c, st);
   }
   const int nsb = eeq_nsb(N);
-  if (!adjoint) {  // inverses of the 512-blocks, kept for the adjoint solve
+  if (!adjoint) {  // inverses of the 128- and 512-blocks, kept for the adjoint solve
+    ensure_smem(eeq_big_pinv_kernel, (int)eeq_big_pinv_smem());
+    eeq_big_pinv_kernel<<<dim3((N + BNB - 1) / BNB, B), 512, eeq_big_pinv_smem(), st>>>(c);
     eeq_blkinv_init_kernel<<<dim3(nsb, B), 256, 0, st>>>(c);
     ensure_smem(eeq_blkinv_step_kernel, (int)eeq_blkinv_smem());
     for (int r = 1; r < SBP; ++r)
