@@ -121,7 +121,7 @@ int d4_dispersion(const d4_tables_t *tables, const d4_model_cfg_t *cfg,
   d4::Workspace w = d4::carve_workspace(d_workspace, batch->n_struct, batch->n_pad, n_slots,
                                         flags);
   if (workspace_bytes < w.bytes) return D4_ERR_WORKSPACE;
-  d4::Ctx c;
+  d4::Ctx c{};
   c.tab = *tables;
   c.cfg = *cfg;
   c.par = *params;

@@ -886,6 +886,32 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
 
 // ---------------------------------------------------------------- launch
 
+// The library's second stream per device (see SideStream): the multi-CTA
+// factorisation's look-ahead runs on it.
+static std::mutex g_side_mutex;
+static SideStream g_side[64];
+
+std::mutex &side_stream_mutex() { return g_side_mutex; }
+
+SideStream *side_stream_for_device() {
+  int dev = 0;
+  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
+  std::lock_guard<std::mutex> lock(g_side_mutex);
+  SideStream &ss = g_side[dev & 63];
+  if (!ss.tried) {
+    ss.tried = true;
+    int lo = 0, hi = 0;
+    bool ok = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess &&
+              cudaStreamCreateWithPriority(&ss.s, cudaStreamNonBlocking, hi) == cudaSuccess;
+    cudaEvent_t *evs[5] = {&ss.fork, &ss.panel, &ss.bulk[0], &ss.bulk[1], &ss.done};
+    for (cudaEvent_t *e : evs)
+      ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
+    ss.ok = ok;
+    if (!ok) cudaGetLastError();  // clear the failed call's error
+  }
+  return ss.ok ? &ss : nullptr;
+}
+
 // Look-ahead of the factorisation.  The chain diagonal block -> panel ->
 // update of the next panel's columns is the critical path; it runs on a
 // high-priority stream of the library (one per device) while the caller's
@@ -902,41 +928,13 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
 // that enqueue this schedule are serialised by a mutex (the events are
 // shared); the caller's stream waits for the critical stream at the end,
 // so the schedule also holds inside a stream capture.
-struct LookAhead {
-  cudaStream_t crit = nullptr;
-  cudaEvent_t fork = nullptr, panel = nullptr, bulk[2] = {nullptr, nullptr}, done = nullptr;
-  bool ok = false, tried = false;
-};
-static std::mutex g_la_mutex;
-static LookAhead g_la[64];
-
-// The device's look-ahead stream and events (created once; nullptr if the
-// runtime refuses them, in which case the factorisation runs on one stream).
-static LookAhead *lookahead_for_device() {
-  int dev = 0;
-  if (cudaGetDevice(&dev) != cudaSuccess) return nullptr;
-  LookAhead &la = g_la[dev & 63];
-  if (!la.tried) {
-    la.tried = true;
-    int lo = 0, hi = 0;
-    bool ok = cudaDeviceGetStreamPriorityRange(&lo, &hi) == cudaSuccess &&
-              cudaStreamCreateWithPriority(&la.crit, cudaStreamNonBlocking, hi) == cudaSuccess;
-    cudaEvent_t *evs[5] = {&la.fork, &la.panel, &la.bulk[0], &la.bulk[1], &la.done};
-    for (cudaEvent_t *e : evs)
-      ok = ok && cudaEventCreateWithFlags(e, cudaEventDisableTiming) == cudaSuccess;
-    la.ok = ok;
-    if (!ok) cudaGetLastError();  // clear the failed call's error
-  }
-  return la.ok ? &la : nullptr;
-}
-
 static void launch_factor(const Ctx &c, cudaStream_t st) {
   const int B = c.B, N = c.N;
   const int npan = (N + BNB - 1) / BNB;
   ensure_smem(eeq_big_diag_kernel, (int)eeq_big_diag_smem());
   ensure_smem(eeq_big_panel_kernel, (int)eeq_big_panel_smem());
   ensure_smem(eeq_big_syrk_kernel, (int)eeq_big_syrk_smem());
-  LookAhead *la = npan > 2 ? lookahead_for_device() : nullptr;
+  SideStream *la = npan > 2 ? side_stream_for_device() : nullptr;
   if (!la) {
     for (int p = 0; p < npan; ++p) {
       const int k0 = p * BNB;
@@ -951,8 +949,8 @@ static void launch_factor(const Ctx &c, cudaStream_t st) {
     }
     return;
   }
-  std::lock_guard<std::mutex> lock(g_la_mutex);
-  cudaStream_t cs = la->crit;
+  std::lock_guard<std::mutex> lock(side_stream_mutex());
+  cudaStream_t cs = la->s;
   cudaEventRecord(la->fork, st);
   cudaStreamWaitEvent(cs, la->fork, 0);
   bool bulk_prev = false;  // whether BULK(p - 1) was recorded

@@ -1,6 +1,8 @@
 // Host-side launchers of the kernel families.
 #pragma once
 
+#include <mutex>
+
 #include "d4_common.cuh"
 
 namespace d4 {
@@ -18,6 +20,18 @@ enum Stage {
   ST_FINISH,
   ST_COUNT
 };
+
+// The library's second stream of a device (high priority, non-blocking) and
+// the events that order it against the caller's stream; created on first use
+// (nullptr if the runtime refuses them: callers then stay on one stream).
+// Enqueue sequences that use the events hold side_stream_mutex().
+struct SideStream {
+  cudaStream_t s = nullptr;
+  cudaEvent_t fork = nullptr, panel = nullptr, bulk[2] = {nullptr, nullptr}, done = nullptr;
+  bool ok = false, tried = false;
+};
+SideStream *side_stream_for_device();
+std::mutex &side_stream_mutex();
 
 // Stage timing hooks (no-ops unless d4_timing_begin was called).
 void stage_begin(int stage, cudaStream_t st);
