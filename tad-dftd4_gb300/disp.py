@@ -15,6 +15,7 @@ sums); any other weighting re-runs the adjoint with those per-atom weights.
 
 from __future__ import annotations
 
+import contextlib
 import ctypes
 from dataclasses import dataclass
 
@@ -56,6 +57,15 @@ def _read_token(token) -> None:
 
 
 _CALLS = [0]  # public calls with deferred status so far (labels their errors)
+_WS_BYTES: dict = {}  # (B, N, slots, flags) -> workspace bytes
+
+
+def _on_device(device: torch.device):
+    """``torch.cuda.device(device)`` unless it is the current device already
+    (the library launches on the current device)."""
+    if device.index is None or device.index == torch.cuda.current_device():
+        return contextlib.nullcontext()
+    return torch.cuda.device(device)
 
 
 def check_status() -> None:
@@ -116,6 +126,27 @@ class Runner:
     rvdw: torch.Tensor | None = None  # (B, N, N) pair radii of rvdw-type damping
     exact_c9: bool = False            # ATM with the exact C9 (DispD4Exact)
     last_work: torch.Tensor | None = None  # workspace of the last call (residuals)
+    ct_params: object = None  # ctypes parameter / model blocks shared by calls of one
+    ct_cfg: object = None     # configuration (built on first use)
+
+    def run_blocks(self) -> None:
+        """Build the ctypes parameter and model blocks of this configuration
+        (once; calls of the same configuration share them)."""
+        if self.ct_params is None:
+            p = self.params
+            self.ct_params = _lib.Params(
+                s6=p["s6"], s8=p["s8"], s10=p["s10"], a1=p["a1"], a2=p["a2"], s9=p["s9"],
+                alp=p["alp"], has_s8=int(p["has_s8"]), has_s10=int(p["has_s10"]),
+                cut_disp2=self.cut["disp2"], cut_disp3=self.cut["disp3"],
+                cut_cn=self.cut["cn"], cut_cn_eeq=self.cut["cn_eeq"],
+                cn_eeq_max=D4_CN_EEQ_MAX, kcn=D4_KCN, k4=D4_K4, k5=D4_K5, k6=D4_K6,
+                damping=p["damping"], rs6=p["rs6"], rs8=p["rs8"], bet=p["bet"],
+            )
+        if self.ct_cfg is None:
+            self.ct_cfg = _lib.ModelCfg(
+                kind=_lib.MODEL_D4S if self.model.kind == "d4s" else _lib.MODEL_D4,
+                ga=self.model.ga, gc=self.model.gc,
+                wf=self.model.wf if self.model.wf is not None else 6.0)
 
     def run(self, positions: torch.Tensor, gradient: bool = False, param_grad: bool = False,
             weights: torch.Tensor | None = None, charges_out: bool = False,
@@ -147,19 +178,18 @@ class Runner:
         cnqout = (torch.empty((B, N), dtype=torch.float64, device=device)
                   if cn_eeq_out else None)
         w = None if weights is None else weights.to(torch.float64).contiguous()
-        ws_bytes = lib.d4_workspace_size(B, N, self.n_slots, flags)
+        wkey = (B, N, self.n_slots, flags)
+        ws_bytes = _WS_BYTES.get(wkey)
+        if ws_bytes is None:
+            ws_bytes = lib.d4_workspace_size(B, N, self.n_slots, flags)
+            if len(_WS_BYTES) > 256:
+                _WS_BYTES.clear()
+            _WS_BYTES[wkey] = ws_bytes
         self.last_work = None
         work = torch.empty(ws_bytes, dtype=torch.uint8, device=device)
         self.last_work = work
-        p = self.params
-        params = _lib.Params(
-            s6=p["s6"], s8=p["s8"], s10=p["s10"], a1=p["a1"], a2=p["a2"], s9=p["s9"],
-            alp=p["alp"], has_s8=int(p["has_s8"]), has_s10=int(p["has_s10"]),
-            cut_disp2=self.cut["disp2"], cut_disp3=self.cut["disp3"],
-            cut_cn=self.cut["cn"], cut_cn_eeq=self.cut["cn_eeq"],
-            cn_eeq_max=D4_CN_EEQ_MAX, kcn=D4_KCN, k4=D4_K4, k5=D4_K5, k6=D4_K6,
-            damping=p["damping"], rs6=p["rs6"], rs8=p["rs8"], bet=p["bet"],
-        )
+        self.run_blocks()
+        params, cfg = self.ct_params, self.ct_cfg
         batch = _lib.Batch(
             n_struct=B, n_pad=N, d_numbers=self.numbers.data_ptr(), d_positions=pos.data_ptr(),
             d_charge=self.charge.data_ptr(),
@@ -176,12 +206,9 @@ class Runner:
             d_param_grad=pgrad.data_ptr() if pgrad is not None else None,
             d_cn_eeq=cnqout.data_ptr() if cnqout is not None else None,
         )
-        cfg = _lib.ModelCfg(kind=_lib.MODEL_D4S if self.model.kind == "d4s" else _lib.MODEL_D4,
-                            ga=self.model.ga, gc=self.model.gc,
-                            wf=self.model.wf if self.model.wf is not None else 6.0)
         cur = torch.cuda.current_stream(device)
         stream = cur.cuda_stream
-        with torch.cuda.device(device):
+        with _on_device(device):
             _lib.check(lib.d4_dispersion(self.tables.struct, cfg, batch, params, flags,
                                          self.n_slots, work.data_ptr(), ws_bytes, outs, stream),
                        "d4_dispersion")
@@ -304,12 +331,61 @@ def _damping(fn) -> Damping:
     return cls()
 
 
+# Configurations of plain calls (D4 model given by name, parameters as plain
+# numbers, default CN / damping, no per-atom overrides), so that a repeated
+# call skips the parameter resolution, the model and table look-ups and the
+# ctypes parameter blocks: key -> (model, resolved, tables, cutoffs, pvec,
+# precision, ctypes params, ctypes model block).
+_CONFIGS: dict = {}
+_CONFIGS_MAX = 64
+
+
+def _config_key(param, model, cutoff, precision, device, dtype):
+    if type(model) is not str or model.casefold() != "d4":
+        return None
+    if cutoff is not None and not isinstance(cutoff, Cutoff):
+        return None
+    items = []
+    for k, v in param.items():
+        if type(v) is not float and type(v) is not int:
+            return None
+        items.append((k, v))
+    ck = None if cutoff is None else tuple(sorted(cutoff.host_values().items()))
+    return (device, dtype, ck, precision, tuple(items))
+
+
 def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cutoff,
              cn_function, counting_function, damping_function, precision=None,
              exact_c9: bool = False):
     _drain_pending()
     device = positions.device
     dtype = positions.dtype
+    ckey = None
+    if (rcov is None and r4r2 is None and rvdw is None and q is None and cn_function is None
+            and counting_function is None and damping_function is None and not exact_c9):
+        ckey = _config_key(param, model, cutoff, precision, device, dtype)
+        hit = _CONFIGS.get(ckey) if ckey is not None else None
+        if hit is not None:
+            mdl, resolved, tab, cut, pvec, prec, ct_params, ct_cfg = hit
+            if numbers.shape != positions.shape[:-1]:
+                raise ValueError(
+                    f"Shape of positions ({positions.shape}) is not consistent with atomic "
+                    f"numbers ({numbers.shape})."
+                )
+            shape = numbers.shape
+            N = shape[-1]
+            nums = numbers.reshape(-1, N).to(device=device, dtype=torch.int64).contiguous()
+            B = nums.shape[0]
+            charge = _as_tensor(charge, device, dtype)
+            if charge.dim() == 0:
+                chg = charge.to(torch.float64).expand(B).contiguous()
+            else:
+                chg = charge.reshape(-1).to(torch.float64).contiguous()
+                if chg.numel() != B:
+                    raise ValueError(f"charge of shape {tuple(charge.shape)} for {B} structures")
+            runner = Runner(numbers=nums, charge=chg, tables=tab, model=mdl, params=resolved,
+                            cut=cut, mixed=prec == "mixed", ct_params=ct_params, ct_cfg=ct_cfg)
+            return runner, pvec, shape
     charge = _as_tensor(charge, device, dtype)
     if numbers.shape != positions.shape[:-1]:
         raise ValueError(
@@ -401,6 +477,12 @@ def _prepare(numbers, positions, charge, param, model, rcov, r4r2, rvdw, q, cuto
             if len(_PVEC) > 64:
                 _PVEC.clear()
             _PVEC[key] = pvec
+    if ckey is not None:  # a plain configuration: remember it for the next call
+        runner.run_blocks()
+        if len(_CONFIGS) >= _CONFIGS_MAX:
+            _CONFIGS.clear()
+        _CONFIGS[ckey] = (mdl, resolved, tab, cut, pvec, precision, runner.ct_params,
+                          runner.ct_cfg)
     return runner, pvec, shape
 
 

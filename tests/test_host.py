@@ -128,3 +128,23 @@ def test_deferred_status_words():
         assert all(t[1].waited for t in toks[:3])
     finally:
         disp._PENDING.clear()
+
+
+def test_configuration_cache_keys():
+    """Plain configurations (D4 by name, parameters as numbers) get a
+    hashable cache key; parameter tensors, other models and custom cutoff
+    objects do not (they take the full preparation on every call)."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    Cutoff = package().Cutoff
+    dev, dt = torch.device("cuda", 0), torch.float64
+    p = {"s6": 1.0, "s8": 1.2, "a1": 0.4, "a2": 5.0}
+    k1 = disp._config_key(p, "d4", None, "mixed", dev, dt)
+    k2 = disp._config_key(dict(p), "D4", None, "mixed", dev, dt)
+    assert k1 is not None and k1 == k2 and hash(k1) == hash(k2)
+    assert disp._config_key(dict(p, a1=0.41), "d4", None, "mixed", dev, dt) != k1
+    assert disp._config_key(p, "d4", None, "fp64", dev, dt) != k1
+    assert disp._config_key(p, "d4", Cutoff(disp3=25.0), "mixed", dev, dt) != k1
+    assert disp._config_key(dict(p, s8=torch.tensor(1.2)), "d4", None, "mixed", dev, dt) is None
+    assert disp._config_key(p, "d4s", None, "mixed", dev, dt) is None
+    assert disp._config_key(p, object(), None, "mixed", dev, dt) is None
