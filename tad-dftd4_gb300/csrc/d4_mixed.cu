@@ -2120,32 +2120,55 @@ __global__ void __launch_bounds__(EEQ_THREADS, 2) eeq_mixed_kernel(Ctx c) {
   const int warp = threadIdx.x >> 5, lane = threadIdx.x & 31, nw = blockDim.x >> 5;
   __shared__ int s_bad;
   if (threadIdx.x == 0) s_bad = 0;
-  // FP32 factor input: the hi part of the lower triangle, four rows per warp
-  // pass (lanes over columns, all loads of the four rows in flight together)
-  for (int i0 = 4 * warp; i0 < m; i0 += 4 * nw)
-    for (int c0 = 0; c0 < i0 + 4; c0 += 256) {  // columns c0 .. c0 + 255
-      float v[4][8];
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int ii = i0 + q;
-        const float *row = Hi + (size_t)(ii < m ? ii : 0) * N;
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int jj = c0 + lane + 32 * u;
-          v[q][u] = (ii < m && jj <= ii) ? row[jj] : 0.f;
+  // The Coulomb matrix of the structure in double-float (the arithmetic of
+  // eeq_build_df_kernel, which builds it for the multi-CTA solve): the FP32
+  // factor input straight into L, the hi / lo rows (both triangles) to global
+  // memory for the refinement residuals.  The structure's atoms are staged in
+  // the panel buffer, idle until the factorisation; a warp takes every
+  // (EEQ_THREADS / 32)-th row, lanes over its columns.
+  {
+    static_assert(SMEM, "the matrix is built into the shared-memory factor");
+    float4 *sp = reinterpret_cast<float4 *>(PT);  // positions (hi), then (lo), then Z
+    float4 *spl = sp + m;
+    int *sz = reinterpret_cast<int *>(spl + m);
+    for (int k = threadIdx.x; k < m; k += blockDim.x) {
+      const size_t a = (size_t)b * N + s_idx[k];
+      sp[k] = c.w.pos32[a];
+      spl[k] = c.w.pos32lo[a];
+      sz[k] = c.w.z[a];
+    }
+    __syncthreads();
+    float *Hw = c.w.eeq_hi + (size_t)b * N * N;
+    float *Lw = c.w.eeq_lo + (size_t)b * N * N;
+    const float4 *etab = c.w.erf_tab;
+    for (int k = warp; k < m; k += nw) {
+      const float4 pk = sp[k], pkl = spl[k];
+      const int zk = sz[k];
+      float *lrow = L + tri_index(k, 0);
+      for (int l = lane; l <= k; l += 32) {
+        dfl v;
+        if (l == k) {
+          const float2 d = c.w.eeq_diag[zk];
+          v = dfl{d.x, d.y};
+        } else {
+          const float4 pl = sp[l], pll = spl[l];
+          const dfl dx = df_add(dfl{pk.x, pkl.x}, dfl{-pl.x, -pll.x});
+          const dfl dy = df_add(dfl{pk.y, pkl.y}, dfl{-pl.y, -pll.y});
+          const dfl dz = df_add(dfl{pk.z, pkl.z}, dfl{-pl.z, -pll.z});
+          const dfl r2 = df_add(df_add(df_sq(dx), df_sq(dy)), df_sq(dz));
+          const dfl ir = df_rsqrt(r2);
+          const float2 g = c.w.igam[zk * MAX_ELEM_ID + sz[l]];
+          const dfl x = df_mul(df_mul(r2, ir), dfl{g.x, g.y});
+          v = df_mul(df_erf(x, etab), ir);
+          Hw[(size_t)l * N + k] = v.hi;  // the upper triangle (strided)
+          Lw[(size_t)l * N + k] = v.lo;
         }
-      }
-#pragma unroll
-      for (int q = 0; q < 4; ++q) {
-        const int ii = i0 + q;
-        float *lrow = L + tri_index(ii, 0);
-#pragma unroll
-        for (int u = 0; u < 8; ++u) {
-          const int jj = c0 + lane + 32 * u;
-          if (ii < m && jj <= ii) lrow[jj] = v[q][u];
-        }
+        lrow[l] = v.hi;
+        Hw[(size_t)k * N + l] = v.hi;
+        Lw[(size_t)k * N + l] = v.lo;
       }
     }
+  }
   for (int k = threadIdx.x; k < m; k += blockDim.x) {
     const int ia = s_idx[k];
     const int z = Zb[ia];
@@ -2332,8 +2355,8 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   const bool eeq_smem = eeq_small_fits(N);
   stage_begin(ST_EEQ, st);
   if (eeq) {
-    eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
-    if (eeq_smem) {
+    if (!eeq_smem) eeq_build_df_kernel<<<build_blocks(c), 256, 0, st>>>(c);
+    if (eeq_smem) {  // builds its matrix itself
       ensure_smem(eeq_mixed_kernel<true>, (int)(vec_bytes + pt_bytes + tri_bytes));
       eeq_mixed_kernel<true><<<B, EEQ_THREADS, vec_bytes + pt_bytes + tri_bytes, st>>>(c);
     } else {
