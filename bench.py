@@ -312,10 +312,10 @@ def probe_peak(lib, pkg, dev, fp64: bool) -> float:
 
 # Kernels of one precision-form energy + gradient call of the D4 model with
 # EEQ charges on structures that fit the one-CTA EEQ / shared-memory ATM
-# (N <= 234): prep, element tables, size order, CN, EEQ matrix, EEQ solve,
-# weights, pair (tensor-core C6), ATM, ATM / C6 adjoint (tensor cores), EEQ
-# adjoint, CN adjoint, finish.
-KERNELS_PER_CALL = 13
+# (N <= 234): prep with the element tables, size order, CN, EEQ (matrix and
+# solve), weights, pair (tensor-core C6), ATM, ATM / C6 adjoint (tensor
+# cores), EEQ adjoint, CN adjoint, finish.
+KERNELS_PER_CALL = 11
 
 
 def run_large(pkg, disp, lib, dev, steps: int = 3, natoms: int = 16000,

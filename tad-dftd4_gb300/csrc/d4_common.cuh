@@ -321,12 +321,28 @@ struct Ctx {
   const double *rvdw_in;  // [B*N*N] pairwise radii of the zero / modified-zero damping
   int B, N, S;
   uint32_t flags;
+  int atm_tiled;  // the register-tiled ATM runs (set by the precision form's launcher)
   Workspace w;
   d4_outputs_t out;
 };
 
 
 // ---------------------------------------------------------------- helpers
+
+constexpr int ATM_KMAX = 8;  // CTAs per structure at most (ATM kernels of the precision form)
+
+// CTAs of the register-tiled ATM for a structure of n atoms in a batch of B:
+// 1.2M triples per CTA for batches of 512 structures and more (measured on
+// batch512 at 512 threads: 600000 -> 12 % slower, 900000 -> 3 %, 1800000 ->
+// 13 %: fewer CTAs per structure mean fewer masked edge steps per task and
+// fewer flushes, until the largest structures' CTAs set the makespan), fewer
+// for smaller batches so that they still fill the GPU.
+__host__ __device__ inline int atm_tiled_ctas(int n, int B) {
+  const long long per = B >= 512 ? 1200000 : (B <= 64 ? 75000 : 1200000LL * B / 512);
+  const long long work = (long long)n * n * n / 6;
+  const int K = (int)((work + per - 1) / per);
+  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
+}
 
 __device__ __forceinline__ double atom_r4r2(const Ctx &c, size_t a, int64_t z) {
   return c.r4r2_in ? c.r4r2_in[a] : c.tab.r4r2[z];

@@ -50,6 +50,7 @@ int launch_properties(const Ctx &c, double *c6out, double *alpha_out, double *q_
 
 // stages shared by the FP64 method and the precision form (d4_fp64.cu)
 void launch_prep(const Ctx &c, cudaStream_t st);
+void launch_prep_memsets(const Ctx &c, cudaStream_t st);  // the memsets of launch_prep
 void launch_cn(const Ctx &c, cudaStream_t st);
 void launch_weights(const Ctx &c, cudaStream_t st);
 void launch_charges_in(const Ctx &c, cudaStream_t st);

@@ -10,12 +10,12 @@
 #include "d4_common.cuh"
 #include "d4_chol.cuh"
 #include "d4_kernels.cuh"
+#include "d4_prep.cuh"
 
 namespace d4 {
 
 constexpr float INV_SQRT_PI_F = 0.564189583547756f;
 constexpr int ATM_CTA_TRIPLES = 300000;  // target triples per ATM CTA
-constexpr int ATM_KMAX = 8;                   // CTAs per structure at most
 constexpr int ATM_THREADS = 1024;       // 32 warps: one CTA per SM (shared memory)
 constexpr int ATM_THREADS_PGRAD = 512;  // the parameter-gradient variant needs more registers
 
@@ -32,8 +32,7 @@ static_assert(TABLES32_THREADS >= MAX_ELEM_ID * MAX_ELEM_ID && TABLES32_THREADS 
 // gam * gc); the erf nodes and 1/sqrt(rad_a^2 + rad_b^2) per element pair as
 // double-floats for the EEQ matrix.  Rows of elements without references are
 // zero.
-__global__ void tables32_kernel(Ctx c) {
-  const int t = blockIdx.x * blockDim.x + threadIdx.x;
+static __device__ __forceinline__ void tables32_entry(const Ctx &c, int t) {
   const int nz = c.tab.n_ref_elem < MAX_ELEM_ID ? c.tab.n_ref_elem : MAX_ELEM_ID;
   if (t < MAX_ELEM_ID * NREF * NFREQ) {
     const int z = t / (NREF * NFREQ);
@@ -110,6 +109,15 @@ __global__ void tables32_kernel(Ctx c) {
     }
     c.w.igam[t] = make_float2(g.hi, g.lo);
   }
+}
+
+// The per-structure set-up (prep_structure: CTAs 0 .. B-1) and the per-call
+// FP32 tables (the other CTAs) in one launch: neither needs the other.
+__global__ void __launch_bounds__(256) prep_tables_kernel(Ctx c) {
+  if ((int)blockIdx.x < c.B)
+    prep_structure(c, blockIdx.x);
+  else
+    tables32_entry(c, ((int)blockIdx.x - c.B) * 256 + threadIdx.x);
 }
 
 // transposed index of (structure b, atom i, slot s, frequency w)
@@ -1038,18 +1046,6 @@ constexpr int AT_THREADS = 512;     // 16 warps at 128 registers, no spills (mea
                                     // 13 % slower, 640 at 96 registers 10 % slower)
 constexpr int AT_TASKS_MAX = 900;   // tiles x chunks for n <= 237 (30 x 30)
 constexpr int AT_FAR_WORDS = 8;     // far-atom bits for n <= 256
-// Triples per CTA: 1200000 for batches of 512 structures and more (measured
-// on batch512 at 512 threads: 600000 -> 12 % slower, 900000 -> 3 %, 1800000
-// -> 13 %: fewer CTAs per structure mean fewer masked edge steps per task
-// and fewer flushes, until the largest structures' CTAs set the makespan),
-// fewer for smaller batches so that they still fill the GPU.
-__device__ __forceinline__ int atm_tiled_ctas(int n, int B) {
-  const long long per = B >= 512 ? 1200000 : (B <= 64 ? 75000 : 1200000LL * B / 512);
-  const long long work = (long long)n * n * n / 6;
-  const int K = (int)((work + per - 1) / per);
-  return K < 1 ? 1 : (K > ATM_KMAX ? ATM_KMAX : K);
-}
-
 __host__ __device__ inline size_t atm_tiled_smem_bytes(int N) {
   return atm_smem_bytes(N) + sizeof(int) * AT_TASKS_MAX;
 }
@@ -2327,16 +2323,19 @@ static void launch_atm(const Ctx &c, cudaStream_t st, size_t smem) {
   }
 }
 
-int launch_mixed(const Ctx &c, cudaStream_t st) {
+int launch_mixed(const Ctx &c_in, cudaStream_t st) {
+  Ctx c = c_in;
   const int B = c.B, N = c.N;
   const dim3 atoms((N + 7) / 8, B);
   const bool grad = (c.flags & D4_FLAG_GRADIENT) != 0;
   const bool pgrad = (c.flags & D4_FLAG_PARAM_GRAD) != 0;
   const bool eeq = (c.flags & D4_FLAG_CHARGES_IN) == 0;
+  const bool atm_tiled = atm_smem_fits(N) && !pgrad && c.weights == nullptr;
+  c.atm_tiled = atm_tiled ? 1 : 0;  // (the prep skips zeroing what that kernel stores)
   timing_next_call();
   stage_begin(ST_PREP, st);
-  launch_prep(c, st);
-  tables32_kernel<<<TABLES32_THREADS / 256, 256, 0, st>>>(c);
+  launch_prep_memsets(c, st);
+  prep_tables_kernel<<<B + TABLES32_THREADS / 256, 256, 0, st>>>(c);
   {
     int P = 1;
     while (P < B && P < SORDER_MAX) P <<= 1;
@@ -2383,7 +2382,7 @@ int launch_mixed(const Ctx &c, cudaStream_t st) {
   const size_t atm_smem = atm_smem_bytes(N);
   const bool atm_sm = atm_smem_fits(N);
   stage_begin(ST_ATM, st);
-  if (atm_sm && !pgrad && c.weights == nullptr) {  // register-tiled triples
+  if (atm_tiled) {  // register-tiled triples
     const size_t sm = atm_tiled_smem_bytes(N);
     if (grad) {
       ensure_smem(atm_tiled_kernel<true>, (int)sm);
