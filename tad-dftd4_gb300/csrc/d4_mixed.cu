@@ -184,10 +184,15 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
     // once (an FP32-rounded gam would bias every atom of the element alike)
     const double qmod64 = q + (double)c.tab.zeff[zi];
     const double gam64 = c.tab.gam[zi] * c.cfg.gc;
+    // one FP64 division per atom (GB300 runs FP64 at 1/64 of the FP32 rate)
+    const double gq64 = qmod64 > 0.0 ? gam64 / qmod64 : 0.0;
 #pragma unroll
     for (int r = 0; r < NREF; ++r) {
       rv[r] = R[r];
       const int refc = (int)rv[r].z;
+      dcn[r] = cf[r] = ua[r] = zq[r] = 0.f;
+      y64[r] = 0.0;
+      if (refc <= 0) continue;  // no such reference: nothing below reads these
       const double d = cn - c.tab.refcovcn[zi * NREF + r];
       // D4: wf for 1 or 3 Gaussians, 1 otherwise; D4S: wf
       const double cfr = (d4s || refc == 1 || refc == 3) ? wf : 1.0;
@@ -198,10 +203,10 @@ __global__ void __launch_bounds__(128) weights_mixed_kernel(Ctx c) {
       // rounded once: FP32 expf carries a mean relative error of ~+5e-9,
       // which C6 ~ zeta_i zeta_j would double into a bias shared by every pair
       // of the structure (expm1f's error is scaled down by u ~ 0.1 there)
-      const double u64 = qmod64 > 0.0 ? gam64 * (q - c.tab.refq[zi * NREF + r]) / qmod64 : 0.0;
+      const double u64 = gq64 * (q - c.tab.refq[zi * NREF + r]);
       ua[r] = (float)u64;
       zq[r] = (float)exp(-c.cfg.ga * (double)expm1f((float)u64));
-      if (refc > 0 && y64[r] < best) {
+      if (y64[r] < best) {
         best = y64[r];
         rn = r;
       }
