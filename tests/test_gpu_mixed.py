@@ -318,3 +318,41 @@ def test_many_small_structures_padded_wide(d4):
     assert np.abs(em - ep).max() <= E_TOL
     assert np.all(em[b.numbers == 0] == 0.0)
     assert (mixed[1] - plain[1]).abs().max().item() <= F_TOL
+
+
+def test_large_structure_call_replays_from_a_cuda_graph(d4):
+    """A call on a structure large enough for the multi-CTA EEQ (its look-ahead
+    runs on a second stream, ordered by events) captured into a CUDA graph:
+    the replay gives the eager call's energies and forces."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    z, r = wl.structure(331, 420)
+    N = 423  # odd padding: the factor's row stride is rounded up
+    numbers = np.zeros((1, N), dtype=np.int64)
+    positions = np.zeros((1, N, 3))
+    numbers[0, :len(z)] = z
+    positions[0, :len(z)] = r
+    dev = torch.device("cuda")
+    nt, pt = torch.from_numpy(numbers).to(dev), torch.from_numpy(positions).to(dev)
+    ct = torch.zeros(1, dtype=torch.float64, device=dev)
+    runner = _runner(nt, pt, ct, "mixed")
+    e0, g0 = (x.clone() for x in runner.run(pt, gradient=True)[:2])
+    torch.cuda.synchronize()
+    check = disp.CHECK_STATUS
+    disp.CHECK_STATUS = False  # no host synchronisation inside a capture
+    try:
+        side = torch.cuda.Stream()
+        side.wait_stream(torch.cuda.current_stream())
+        graph = torch.cuda.CUDAGraph()
+        with torch.cuda.graph(graph, stream=side, capture_error_mode="relaxed"):
+            out = runner.run(pt, gradient=True)
+        graph.replay()
+        torch.cuda.synchronize()
+    finally:
+        disp.CHECK_STATUS = check
+    # (FP32 atomics of the partner-split kernels make the last bits order-dependent)
+    assert abs(out[0].sum().item() - e0.sum().item()) <= 1e-9
+    assert (out[1] - g0).abs().max().item() <= 1e-8
+    res = runner.eeq_residuals()
+    assert res[0, 0] < 1e-10 and res[0, 1] < 1e-10
