@@ -11,15 +11,10 @@ constexpr int PB = 32;  // panel width of the blocked factorisation and solves
 constexpr unsigned FULL = 0xffffffffu;
 
 // Diagonal 32 x 32 block (rows / columns k0 .. k0+kb-1) of the packed lower
-// matrix L, by one warp, in registers: the Cholesky factor (lane r holds row
-// r; rows beyond the matrix are padded with the identity), then the inverse
-// of the factor (lane c computes column c), which replaces the block in
-// place: the panel and the triangular solves only need the inverse.  A
-// non-positive pivot sets *bad and goes on with pivot 1.  (Measured at
-// ~9 us per block on batch512, one warp while the other seven wait; a
-// column-oriented inverse was no faster, and rolled shared-memory loops
-// were 3x slower: their loads and stores serialise.)
-static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
+// matrix L: the Cholesky factor by one warp, in registers (lane r holds row
+// r; rows beyond the matrix are padded with the identity).  A non-positive
+// pivot sets *bad and goes on with pivot 1.
+static __device__ void chol_diag_factor(float *L, int k0, int kb, int *bad) {
   const int r = threadIdx.x & 31;
   const bool live = r < kb;
   float *row = L + tri_index(k0 + (live ? r : 0), k0);
@@ -47,30 +42,45 @@ static __device__ void chol_diag_block(float *L, int k0, int kb, int *bad) {
 #pragma unroll
   for (int j = 0; j < PB; ++j)
     if (live && j <= r) row[j] = a[j];
-  __syncwarp();
-  // inverse: X[rr][c] = -(sum_{k=c}^{rr-1} L[rr][k] X[k][c]) / L[rr][rr]; x = column c
-  const int c = r;
-  float x[PB];
+}
+
+// The inverse X of the factored diagonal block, which replaces it in place
+// (the panel and the triangular solves only need the inverse), by all warps
+// of the CTA (at least eight; every thread calls it): warp w forms the
+// columns w, w + nw, ... by forward substitution down the column, lane r =
+// row r, X[r][c] = (delta_rc - sum_{k<r} L[r][k] X[k][c]) / L[r][r]; the
+// columns of a warp advance together, the finished value of row k reaching
+// the other lanes by a shuffle.  (One warp forming all 32 columns took ~12k
+// cycles per block, three times the factorisation; eight warps take ~2.7k.)
+static __device__ void chol_diag_inverse(float *L, int k0, int kb) {
+  constexpr int QMAX = 4;  // columns per warp for eight warps or more
+  const int w = threadIdx.x >> 5, r = threadIdx.x & 31, nw = blockDim.x >> 5;
+  const bool live = r < kb;
+  const float *lr = L + tri_index(k0 + (live ? r : 0), k0);
+  const float dinv = live ? 1.0f / lr[r] : 1.f;
+  float sq[QMAX], xr[QMAX];
 #pragma unroll
-  for (int rr = 0; rr < PB; ++rr) {
-    x[rr] = 0.f;
-    if (rr < kb) {
-      const float *lr = L + tri_index(k0 + rr, k0);
-      float acc0 = 0.f, acc1 = 0.f;
+  for (int q = 0; q < QMAX; ++q) sq[q] = xr[q] = 0.f;
+#pragma unroll 1
+  for (int k = 0; k < kb; ++k) {
+    float xk[QMAX];
 #pragma unroll
-      for (int k = 0; k < rr; ++k) {
-        if (k & 1) acc1 = fmaf(lr[k], x[k], acc1);
-        else acc0 = fmaf(lr[k], x[k], acc0);
-      }
-      const float dii = 1.0f / lr[rr];
-      x[rr] = rr == c ? dii : (rr > c ? -(acc0 + acc1) * dii : 0.f);
+    for (int q = 0; q < QMAX; ++q) {
+      const int cq = w + nw * q;
+      const float mine = r == cq ? dinv : (r > cq ? -sq[q] * dinv : 0.f);
+      if (r == k) xr[q] = mine;
+      xk[q] = __shfl_sync(FULL, mine, k);
     }
-  }
-  __syncwarp();
+    const float lrk = (live && r > k) ? lr[k] : 0.f;
 #pragma unroll
-  for (int rr = 0; rr < PB; ++rr)
-    if (rr < kb && rr >= c) L[tri_index(k0 + rr, k0 + c)] = x[rr];
-  __syncwarp();
+    for (int q = 0; q < QMAX; ++q) sq[q] = fmaf(lrk, xk[q], sq[q]);
+  }
+  __syncthreads();  // every warp has read the factor
+#pragma unroll
+  for (int q = 0; q < QMAX; ++q) {
+    const int cq = w + nw * q;
+    if (cq < PB && live && r >= cq) L[tri_index(k0 + r, k0 + cq)] = xr[q];
+  }
 }
 
 // (ti, tj), tj <= ti, of the t-th tile of a packed lower triangle of tiles
@@ -83,18 +93,20 @@ static __device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
 
 // Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
 // m x m FP32 matrix L, in place, except that each diagonal block holds the
-// inverse of its factor.  Per panel: the diagonal block by warp 0, the
-// panel L21 = A21 X^T (X the block inverse; one warp per row, lane =
-// column), and the trailing update A22 -= L21 L21^T.  The panel buffer PT
-// (shared memory, 32 x ldp) holds the panel transposed, so that the update
-// runs on 8 x 8 register tiles read as float4 (64 FMAs per four 16-byte
-// loads).
+// inverse of its factor.  Per panel: the diagonal block (factor by warp 0,
+// inverse by all warps), the panel L21 = A21 X^T (X the block inverse; one
+// warp per row, lane = column), and the trailing update A22 -= L21 L21^T.
+// The panel buffer PT (shared memory, 32 x ldp) holds the panel transposed,
+// so that the update runs on 8 x 8 register tiles read as float4 (64 FMAs
+// per four 16-byte loads).
 static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   const int nw = nt >> 5;
   for (int k0 = 0; k0 < m; k0 += PB) {
     const int kb = min(PB, m - k0);
-    if (warp == 0) chol_diag_block(L, k0, kb, bad);
+    if (warp == 0) chol_diag_factor(L, k0, kb, bad);
+    __syncthreads();
+    chol_diag_inverse(L, k0, kb);
     __syncthreads();
     const int t0 = k0 + kb;
     // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T; the
