@@ -5,27 +5,31 @@
 //
 //   factor (per panel k0):  diag   one CTA per structure: Cholesky of the
 //                                  128 x 128 diagonal block (chol_blocked in
-//                                  shared memory) and the full inverse X of
-//                                  its factor, stored over the block
-//                          panel   L21 = A21 X^T, 64-row tiles
+//                                  shared memory), stored over the block with
+//                                  the inverses of its 32 x 32 diagonal blocks
+//                          panel   L21 L11^T = A21 by block substitution,
+//                                  64-row tiles
 //                          syrk    A22 -= L21 L21^T, 128 x 128 lower tiles
 //                                  on the tensor cores (tcgen05, split TF32)
 //   inverse (once):         the 512 x 512 diagonal blocks of the factor
 //                          are inverted (block forward substitution over
-//                          their panels, 128 x 128 products)
+//                          their panels, 128 x 128 products) and stored with
+//                          their transposes above the diagonal
 //   solve  (per iteration): forward and backward sweeps in 512-row steps
 //                          (products with the block inverses, GEMV updates
 //                          off the diagonal), then x += v and the
 //                          double-float residual of (hi + lo) x, whose max
-//                          |r| per structure decides (on the device) whether
-//                          later iterations run.
+//                          |r| per structure decides whether later
+//                          iterations run.
 //
 // Rows and columns are in compact order (real atoms only, ``ridx``); the
 // structures of a batch are processed together (grid y), each up to its own
 // size n_real[b].
 #include <float.h>
 
+#include <cstring>
 #include <mutex>
+#include <vector>
 
 #include "d4_chol.cuh"
 #include "d4_common.cuh"
@@ -62,21 +66,43 @@ __global__ void __launch_bounds__(512) eeq_big_diag_kernel(Ctx c, int k0) {
   const int N = c.N;
   const int NF = eeq_ldf(N);
   float *F = c.w.eeq_F + (size_t)b * N * NF;
-  const int tid = threadIdx.x, nt = blockDim.x;
+  const int tid = threadIdx.x;
   if (tid == 0) s_bad = 0;
-  const int tri = kb * (kb + 1) / 2;
-  for (int t = tid; t < tri; t += nt) {
-    int i, j;
-    tri_tile(t, i, j);
-    P[t] = F[(size_t)(k0 + i) * NF + k0 + j];
+  // 512 threads: warp w takes rows w, w + 16, ...; lane l columns l, l + 32,
+  // ...: all of a thread's loads are issued before its first store
+  const int warp = tid >> 5, lane = tid & 31;
+  {
+    float v[BNB / 16][4];
+#pragma unroll
+    for (int s = 0; s < BNB / 16; ++s) {
+      const int i = warp + 16 * s;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = lane + 32 * q;
+        v[s][q] = (i < kb && j <= i) ? __ldcg(F + (size_t)(k0 + i) * NF + k0 + j) : 0.f;
+      }
+    }
+#pragma unroll
+    for (int s = 0; s < BNB / 16; ++s) {
+      const int i = warp + 16 * s;
+#pragma unroll
+      for (int q = 0; q < 4; ++q) {
+        const int j = lane + 32 * q;
+        if (i < kb && j <= i) P[tri_index(i, j)] = v[s][q];
+      }
+    }
   }
   __syncthreads();
   chol_blocked(P, PT, ldp, kb, &s_bad);
   if (tid == 0 && s_bad) set_status(c.w.status, D4_ERR_EEQ_SINGULAR);
-  for (int t = tid; t < tri; t += nt) {
-    int i, j;
-    tri_tile(t, i, j);
-    F[(size_t)(k0 + i) * NF + k0 + j] = P[t];
+#pragma unroll
+  for (int s = 0; s < BNB / 16; ++s) {
+    const int i = warp + 16 * s;
+#pragma unroll
+    for (int q = 0; q < 4; ++q) {
+      const int j = lane + 32 * q;
+      if (i < kb && j <= i) F[(size_t)(k0 + i) * NF + k0 + j] = P[tri_index(i, j)];
+    }
   }
 }
 
@@ -176,7 +202,7 @@ __device__ __forceinline__ unsigned char *opnd_block(const Ctx &c, int par, int 
 // rows x 4 columns of the current 32-column block; L11 transposed and the
 // rows transposed in shared memory.
 constexpr int PN_LLT = BNB + 4, PN_LAT = 64 + 2;
-__global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int par) {
+__global__ void __launch_bounds__(256, 1) eeq_big_panel_kernel(Ctx c, int k0, int par) {
   extern __shared__ float4 s_dyn4[];
   float *LT = reinterpret_cast<float *>(s_dyn4);  // LT[k][col] = L11[col][k], 0 for k > col
   float *AT = LT + BNB * PN_LLT;                   // AT[cc][row] = A21[row][cc], then L21
@@ -186,19 +212,48 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int p
   const int kb = min(BNB, m - k0);
   const int t0 = k0 + kb;
   const int r0 = t0 + 64 * blockIdx.x;
-  if (r0 >= m) return;
+  if (r0 >= m || kb != BNB) return;
   const int N = c.N;
   const int NF = eeq_ldf(N);
   float *F = c.w.eeq_F + (size_t)b * N * NF;
   const int tid = threadIdx.x;
-  for (int t = tid; t < BNB * BNB; t += 256) {
-    const int col = t / BNB, k = t % BNB;  // coalesced over k
-    LT[k * PN_LLT + col] = (col < kb && k <= col) ? F[(size_t)(k0 + col) * NF + k0 + k] : 0.f;
+  // Past the early returns the panel is full (kb = BNB: a shorter panel is
+  // the structure's last, with no rows below it).  L11 and the 64 rows of
+  // A21 arrive as 16-byte loads, eight in flight per thread before any is
+  // stored; the lanes of a warp take consecutive columns of L11 (rows of
+  // A21), so that the transposed stores hit consecutive banks.
+  for (int s0 = 0; s0 < BNB * BNB / 4 / 256; s0 += 8) {
+    float4 v[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int f = tid + 256 * (s0 + s), col = f & (BNB - 1), kg = f >> 7;
+      v[s] = __ldcg(reinterpret_cast<const float4 *>(F + (size_t)(k0 + col) * NF + k0 + 4 * kg));
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int f = tid + 256 * (s0 + s), col = f & (BNB - 1), kg = f >> 7;
+      const float e[4] = {v[s].x, v[s].y, v[s].z, v[s].w};
+#pragma unroll
+      for (int q = 0; q < 4; ++q) LT[(4 * kg + q) * PN_LLT + col] = 4 * kg + q <= col ? e[q] : 0.f;
+    }
   }
-  for (int t = tid; t < 64 * BNB; t += 256) {
-    const int row = t / BNB, cc = t % BNB;
-    const int i = r0 + row;
-    AT[cc * PN_LAT + row] = (i < m && cc < kb) ? F[(size_t)i * NF + k0 + cc] : 0.f;
+  {
+    float4 v[8];
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int f = tid + 256 * s, row = f & 63, cg = f >> 6;
+      const int i = r0 + row;
+      v[s] = i < m ? __ldcg(reinterpret_cast<const float4 *>(F + (size_t)i * NF + k0 + 4 * cg))
+                   : make_float4(0.f, 0.f, 0.f, 0.f);
+    }
+#pragma unroll
+    for (int s = 0; s < 8; ++s) {
+      const int f = tid + 256 * s, row = f & 63, cg = f >> 6;
+      AT[(4 * cg) * PN_LAT + row] = v[s].x;
+      AT[(4 * cg + 1) * PN_LAT + row] = v[s].y;
+      AT[(4 * cg + 2) * PN_LAT + row] = v[s].z;
+      AT[(4 * cg + 3) * PN_LAT + row] = v[s].w;
+    }
   }
   __syncthreads();
   const int ty = tid >> 3, tx = tid & 7;  // rows 2 ty, 2 ty + 1; columns 4 tx .. + 3 of a block
@@ -211,6 +266,7 @@ __global__ void __launch_bounds__(256) eeq_big_panel_kernel(Ctx c, int k0, int p
 #pragma unroll
       for (int u = 0; u < 4; ++u) acc[v][u] = 0.f;
     // sum_{k < 32 cb} Y_k L_ck^T (Y of the earlier blocks is in AT)
+#pragma unroll 4
     for (int k = 0; k < 32 * cb; ++k) {
       const float2 y = *reinterpret_cast<const float2 *>(AT + k * PN_LAT + 2 * ty);
       const float4 l = *reinterpret_cast<const float4 *>(LT + k * PN_LLT + c0);
@@ -599,13 +655,38 @@ __global__ void __launch_bounds__(256) eeq_blkinv_step_kernel(Ctx c, int r) {
 
 size_t eeq_blkinv_smem() { return 4 * ((size_t)2 * IK * (BNB + 4) + (size_t)BNB * (BNB + 4)); }
 
+// After the steps: the upper triangle of every block (zero until here)
+// receives the transpose of its lower triangle, so that the backward sweep
+// reads X_s^T by rows as the forward sweep reads X_s.  One CTA per pair of
+// 32 x 32 tiles (lower tile (ti, tj), ti >= tj, and its mirror), through
+// shared memory; grid (136, blocks, structures).
+constexpr int MIR_TILES = (EEQ_SB / 32) * (EEQ_SB / 32 + 1) / 2;
+__global__ void __launch_bounds__(256) eeq_blkinv_mirror_kernel(Ctx c) {
+  __shared__ float t[32][33];
+  const int b = blockIdx.z, sblk = blockIdx.y;
+  const int m = c.w.n_real[b];
+  if (sblk * EEQ_SB >= m) return;
+  int ti, tj;
+  tri_tile(blockIdx.x, ti, tj);
+  float *X = xd_block(c, b, sblk);
+  const int tx = threadIdx.x & 31, ty = threadIdx.x >> 5;
+  for (int r = ty; r < 32; r += 8) t[r][tx] = X[(size_t)(32 * ti + r) * EEQ_SB + 32 * tj + tx];
+  __syncthreads();
+  for (int r = ty; r < 32; r += 8) {
+    const int gi = 32 * tj + r, gk = 32 * ti + tx;
+    if (gk > gi) X[(size_t)gi * EEQ_SB + gk] = t[tx][r];
+  }
+}
+
 // ---------------------------------------------------------------- sweeps
 
-// Diagonal block s of a sweep, nr right-hand sides: dst_blk = X_s src_blk
-// (forward: warp per row, coalesced) or X_s^T src_blk (backward: warp per
-// column, lanes over the rows below the diagonal).
-__global__ void __launch_bounds__(256) eeq_sweep_diag_kernel(Ctx c, int sblk, int it, int trans,
-                                                             int nr, int src_y) {
+// Diagonal block s of a sweep, nr right-hand sides, warp per output row i:
+// forward dst_i = sum_{k <= i} X_s[i][k] src_k, backward
+// dst_i = sum_{k >= i} X_s^T[i][k] src_k -- both from row i of the block
+// (X_s below the diagonal, X_s^T above it).  A lane's sixteen loads of the
+// row are issued before the first product.
+__global__ void __launch_bounds__(256, 1) eeq_sweep_diag_kernel(Ctx c, int sblk, int it, int trans,
+                                                                int nr, int src_y) {
   __shared__ float s_v[2][EEQ_SB];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
@@ -616,28 +697,28 @@ __global__ void __launch_bounds__(256) eeq_sweep_diag_kernel(Ctx c, int sblk, in
   const float *src = (src_y ? c.w.eeq_Y : c.w.eeq_V) + (size_t)b * 2 * N;
   float *dst = (src_y ? c.w.eeq_V : c.w.eeq_Y) + (size_t)b * 2 * N;
   const float *X = xd_block(c, b, sblk);
-  for (int t = threadIdx.x; t < nr * EEQ_SB; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 2 * EEQ_SB; t += blockDim.x) {
     const int r = t / EEQ_SB, k = t % EEQ_SB;
-    s_v[r][k] = k < kb ? src[(size_t)r * N + s0 + k] : 0.f;
+    s_v[r][k] = (r < nr && k < kb) ? src[(size_t)r * N + s0 + k] : 0.f;
   }
   __syncthreads();
   const int lane = threadIdx.x & 31;
   const int i = blockIdx.x * 8 + (threadIdx.x >> 5);  // output index
   if (i >= kb) return;
+  const float *row = X + (size_t)i * EEQ_SB;
+  const int k_lo = trans ? i : 0, k_hi = trans ? kb - 1 : i;
+  float x[EEQ_SB / 32];
+#pragma unroll
+  for (int t = 0; t < EEQ_SB / 32; ++t) {
+    const int k = lane + 32 * t;
+    x[t] = (k >= k_lo && k <= k_hi) ? row[k] : 0.f;
+  }
   float a0 = 0.f, a1 = 0.f;
-  if (!trans) {
-    const float *row = X + (size_t)i * EEQ_SB;
-    for (int k = lane; k <= i; k += 32) {
-      const float x = row[k];
-      a0 = fmaf(x, s_v[0][k], a0);
-      if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
-    }
-  } else {
-    for (int k = i + lane; k < kb; k += 32) {
-      const float x = X[(size_t)k * EEQ_SB + i];
-      a0 = fmaf(x, s_v[0][k], a0);
-      if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
-    }
+#pragma unroll
+  for (int t = 0; t < EEQ_SB / 32; ++t) {
+    const int k = lane + 32 * t;
+    a0 = fmaf(x[t], s_v[0][k], a0);
+    a1 = fmaf(x[t], s_v[1][k], a1);
   }
   a0 = warp_sumf(a0);
   if (nr == 2) a1 = warp_sumf(a1);
@@ -647,42 +728,74 @@ __global__ void __launch_bounds__(256) eeq_sweep_diag_kernel(Ctx c, int sblk, in
   }
 }
 
-// Forward sweep update below block s: V_i -= F[i][blk] . Y_blk, warp per row.
-__global__ void __launch_bounds__(256) eeq_sweep_below_kernel(Ctx c, int sblk, int it, int nr) {
+// Forward sweep update below block s: V_i -= F[i][blk] . Y_blk.  Four rows
+// per warp, lanes over the block's columns: a lane's 64 matrix loads and
+// the old V entries of its rows are issued together (one round trip), Y_blk
+// is staged in shared memory once per CTA.
+constexpr int BL_ROWS = 4;
+__global__ void __launch_bounds__(256, 2) eeq_sweep_below_kernel(Ctx c, int sblk, int it, int nr) {
+  __shared__ float s_y[2][EEQ_SB];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   const int s0 = sblk * EEQ_SB;
   if (s0 >= m || big_skip(c, b, it)) return;
   const int kb = min(EEQ_SB, m - s0);
-  const int i = s0 + kb + blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (i >= m) return;
-  const int lane = threadIdx.x & 31;
+  const int i0 = s0 + kb + (blockIdx.x * 8 + (threadIdx.x >> 5)) * BL_ROWS;
+  if (s0 + kb + blockIdx.x * 8 * BL_ROWS >= m) return;  // the whole CTA is past the end
   const int N = c.N;
-  const int NF = eeq_ldf(N);
-  const float *row = c.w.eeq_F + (size_t)b * N * NF + (size_t)i * NF + s0;
-  const float *Y = c.w.eeq_Y + (size_t)b * 2 * N + s0;
-  float *V = c.w.eeq_V + (size_t)b * 2 * N;
-  float a0 = 0.f, a1 = 0.f;
-  for (int k = lane; k < kb; k += 32) {
-    const float x = row[k];
-    a0 = fmaf(x, Y[k], a0);
-    if (nr == 2) a1 = fmaf(x, Y[N + k], a1);
+  const float *Yg = c.w.eeq_Y + (size_t)b * 2 * N + s0;
+  for (int t = threadIdx.x; t < 2 * EEQ_SB; t += blockDim.x) {
+    const int r = t / EEQ_SB, k = t % EEQ_SB;
+    s_y[r][k] = (r < nr && k < kb) ? Yg[(size_t)r * N + k] : 0.f;
   }
-  a0 = warp_sumf(a0);
-  if (nr == 2) a1 = warp_sumf(a1);
-  if (lane == 0) {
-    V[i] -= a0;
-    if (nr == 2) V[N + i] -= a1;
+  __syncthreads();
+  if (i0 >= m) return;
+  const int lane = threadIdx.x & 31;
+  const int NF = eeq_ldf(N);
+  const float *base = c.w.eeq_F + (size_t)b * N * NF + (size_t)i0 * NF + s0;
+  float *V = c.w.eeq_V + (size_t)b * 2 * N;
+  float x[BL_ROWS][EEQ_SB / 32];
+#pragma unroll
+  for (int r = 0; r < BL_ROWS; ++r)
+#pragma unroll
+    for (int t = 0; t < EEQ_SB / 32; ++t) {
+      const int k = lane + 32 * t;
+      x[r][t] = (i0 + r < m && k < kb) ? base[(size_t)r * NF + k] : 0.f;
+    }
+  const bool own = lane < BL_ROWS && i0 + lane < m;  // lane r writes row i0 + r
+  const float v0 = own ? V[i0 + lane] : 0.f;
+  const float v1 = own && nr == 2 ? V[N + i0 + lane] : 0.f;
+  float o0 = 0.f, o1 = 0.f;
+#pragma unroll
+  for (int r = 0; r < BL_ROWS; ++r) {
+    float a0 = 0.f, a1 = 0.f;
+#pragma unroll
+    for (int t = 0; t < EEQ_SB / 32; ++t) {
+      const int k = lane + 32 * t;
+      a0 = fmaf(x[r][t], s_y[0][k], a0);
+      a1 = fmaf(x[r][t], s_y[1][k], a1);
+    }
+    a0 = warp_sumf(a0);
+    if (nr == 2) a1 = warp_sumf(a1);
+    if (lane == r) {
+      o0 = a0;
+      o1 = a1;
+    }
+  }
+  if (own) {
+    V[i0 + lane] = v0 - o0;
+    if (nr == 2) V[N + i0 + lane] = v1 - o1;
   }
 }
 
-// Backward sweep update above block s: Y_i -= F[blk][i] . V_blk.  A CTA
-// takes 64 rows i, four threads per row splitting the block's 512 columns
-// (reads coalesced over i), partial sums combined in shared memory.
-constexpr int AB_ROWS = 64;
-__global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
+// Backward sweep update above block s: Y_i -= sum_k F[s0 + k][i] V_{s0+k}
+// for i < s0.  A CTA takes 32 columns i (the lanes: reads coalesced over i)
+// and splits the block's rows k over its eight warps (64 each, sixteen
+// loads in flight per lane); the warps' partial sums meet in shared memory.
+constexpr int AB_COLS = 32;
+__global__ void __launch_bounds__(256, 1) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
   __shared__ float s_v[2][EEQ_SB];
-  __shared__ float s_part[2][4][AB_ROWS];
+  __shared__ float s_part[2][8][AB_COLS];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   const int s0 = sblk * EEQ_SB;
@@ -691,41 +804,46 @@ __global__ void __launch_bounds__(256) eeq_sweep_above_kernel(Ctx c, int sblk, i
   const int N = c.N;
   const float *V = c.w.eeq_V + (size_t)b * 2 * N;
   float *Y = c.w.eeq_Y + (size_t)b * 2 * N;
-  for (int t = threadIdx.x; t < nr * EEQ_SB; t += blockDim.x) {
+  for (int t = threadIdx.x; t < 2 * EEQ_SB; t += blockDim.x) {
     const int r = t / EEQ_SB, k = t % EEQ_SB;
-    s_v[r][k] = k < kb ? V[(size_t)r * N + s0 + k] : 0.f;
+    s_v[r][k] = (r < nr && k < kb) ? V[(size_t)r * N + s0 + k] : 0.f;
   }
   __syncthreads();
-  const int rr = threadIdx.x & (AB_ROWS - 1), qk = threadIdx.x / AB_ROWS;
-  const int i = blockIdx.x * AB_ROWS + rr;
+  const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
+  const int i = blockIdx.x * AB_COLS + lane;
   float a0 = 0.f, a1 = 0.f;
   if (i < s0) {
     const int NF = eeq_ldf(N);
-    const float *F = c.w.eeq_F + (size_t)b * N * NF + (size_t)s0 * NF + i;
-    const int kq = EEQ_SB / 4;
-    const int k_lo = qk * kq, k_hi = min(kb, k_lo + kq);
-    float b0 = 0.f, b1 = 0.f;
-#pragma unroll 4
-    for (int k = k_lo; k < k_hi; ++k) {
-      const float x = F[(size_t)k * NF];
-      if (k & 1) {
-        b0 = fmaf(x, s_v[0][k], b0);
-        if (nr == 2) b1 = fmaf(x, s_v[1][k], b1);
-      } else {
-        a0 = fmaf(x, s_v[0][k], a0);
-        if (nr == 2) a1 = fmaf(x, s_v[1][k], a1);
+    const float *col = c.w.eeq_F + (size_t)b * N * NF + (size_t)s0 * NF + i;
+    const int kbeg = (EEQ_SB / 8) * w;
+#pragma unroll
+    for (int h = 0; h < EEQ_SB / 8; h += 16) {
+      float x[16];
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int k = kbeg + h + t;
+        x[t] = k < kb ? col[(size_t)k * NF] : 0.f;
+      }
+#pragma unroll
+      for (int t = 0; t < 16; ++t) {
+        const int k = kbeg + h + t;
+        a0 = fmaf(x[t], s_v[0][k], a0);
+        a1 = fmaf(x[t], s_v[1][k], a1);
       }
     }
-    a0 += b0;
-    a1 += b1;
   }
-  s_part[0][qk][rr] = a0;
-  s_part[1][qk][rr] = a1;
+  s_part[0][w][lane] = a0;
+  s_part[1][w][lane] = a1;
   __syncthreads();
-  if (qk == 0 && i < s0) {
-    Y[i] -= (s_part[0][0][rr] + s_part[0][1][rr]) + (s_part[0][2][rr] + s_part[0][3][rr]);
-    if (nr == 2)
-      Y[N + i] -= (s_part[1][0][rr] + s_part[1][1][rr]) + (s_part[1][2][rr] + s_part[1][3][rr]);
+  if (w == 0 && i < s0) {
+    float t0 = 0.f, t1 = 0.f;
+#pragma unroll
+    for (int q = 0; q < 8; ++q) {
+      t0 += s_part[0][q][lane];
+      t1 += s_part[1][q][lane];
+    }
+    Y[i] -= t0;
+    if (nr == 2) Y[N + i] -= t1;
   }
 }
 
@@ -744,66 +862,90 @@ __global__ void eeq_big_update_kernel(Ctx c, int it, int nr) {
   }
 }
 
-// r = b - (hi + lo) x in double-float, warp per row; v <- FP32 r and the
-// structure's max |r| of this iteration.
-__global__ void __launch_bounds__(256) eeq_big_residual_kernel(Ctx c, int it, int nr) {
+// r = b - (hi + lo) x in double-float; v <- FP32 r and the structure's max
+// |r| of this iteration.  Four rows per warp, so that every x entry read
+// serves four rows; lanes over columns (32 apart, coalesced), the 32 matrix
+// loads of a lane's step issued together, one step ahead of the sums.  Per
+// row the sum runs in the same order as with one row per warp.
+constexpr int RS_ROWS = 4;
+template <int NR>
+__global__ void __launch_bounds__(256, 2) eeq_big_residual_kernel(Ctx c, int it) {
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   if (big_skip(c, b, it)) return;
-  const int k = blockIdx.x * 8 + (threadIdx.x >> 5);
-  if (k >= m) return;
+  const int k0 = (blockIdx.x * 8 + (threadIdx.x >> 5)) * RS_ROWS;
+  if (k0 >= m) return;
   const int lane = threadIdx.x & 31;
   const int N = c.N;
-  const float *hr = c.w.eeq_hi + (size_t)b * N * N + (size_t)k * N;
-  const float *lr = c.w.eeq_lo + (size_t)b * N * N + (size_t)k * N;
+  const float *hr = c.w.eeq_hi + (size_t)b * N * N + (size_t)k0 * N;
+  const float *lr = c.w.eeq_lo + (size_t)b * N * N + (size_t)k0 * N;
   const float2 *X = c.w.eeq_X + (size_t)b * 2 * N;
-  dfl a0 = {0.f, 0.f}, a1 = {0.f, 0.f};
-  for (int l0 = lane; l0 < m; l0 += 128) {
-    float h[4], lo[4];
+  dfl acc[RS_ROWS][NR];
 #pragma unroll
-    for (int u = 0; u < 4; ++u) {
-      const int l = l0 + 32 * u;
-      h[u] = l < m ? hr[l] : 0.f;
-      lo[u] = l < m ? lr[l] : 0.f;
-    }
+  for (int r = 0; r < RS_ROWS; ++r)
+#pragma unroll
+    for (int q = 0; q < NR; ++q) acc[r][q] = {0.f, 0.f};
+  // two stages of loads: those of the next 128 columns are in flight while
+  // the current ones are summed
+  float h[2][RS_ROWS][4], lo[2][RS_ROWS][4];
+  auto load = [&](float (&hh)[RS_ROWS][4], float (&ll)[RS_ROWS][4], int l0) {
+#pragma unroll
+    for (int r = 0; r < RS_ROWS; ++r)
+#pragma unroll
+      for (int u = 0; u < 4; ++u) {
+        const int l = l0 + 32 * u;
+        const bool ok = l < m && k0 + r < m;
+        hh[r][u] = ok ? hr[(size_t)r * N + l] : 0.f;
+        ll[r][u] = ok ? lr[(size_t)r * N + l] : 0.f;
+      }
+  };
+  auto sum = [&](const float (&hh)[RS_ROWS][4], const float (&ll)[RS_ROWS][4], int l0) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       const int l = l0 + 32 * u;
       if (l < m) {
-        const float2 x0 = X[l];
-        {
-          const float p = h[u] * x0.x;
-          const float e = fmaf(h[u], x0.y, fmaf(lo[u], x0.x, fmaf(h[u], x0.x, -p)));
-          const dfl s = df_two_sum(a0.hi, p);
-          a0 = {s.hi, a0.lo + (s.lo + e)};
-        }
-        if (nr == 2) {
-          const float2 x1 = X[N + l];
-          const float p = h[u] * x1.x;
-          const float e = fmaf(h[u], x1.y, fmaf(lo[u], x1.x, fmaf(h[u], x1.x, -p)));
-          const dfl s = df_two_sum(a1.hi, p);
-          a1 = {s.hi, a1.lo + (s.lo + e)};
+#pragma unroll
+        for (int q = 0; q < NR; ++q) {
+          const float2 x = X[(size_t)q * N + l];
+#pragma unroll
+          for (int r = 0; r < RS_ROWS; ++r) {
+            const float p = hh[r][u] * x.x;
+            const float e = fmaf(hh[r][u], x.y, fmaf(ll[r][u], x.x, fmaf(hh[r][u], x.x, -p)));
+            const dfl s = df_two_sum(acc[r][q].hi, p);
+            acc[r][q] = {s.hi, acc[r][q].lo + (s.lo + e)};
+          }
         }
       }
     }
+  };
+  load(h[0], lo[0], lane);
+  for (int l0 = lane; l0 < m; l0 += 256) {
+    load(h[1], lo[1], l0 + 128);
+    sum(h[0], lo[0], l0);
+    load(h[0], lo[0], l0 + 256);
+    sum(h[1], lo[1], l0 + 128);
   }
   float mx = 0.f;
-  for (int r = 0; r < nr; ++r) {
-    dfl a = r == 0 ? a0 : a1;
 #pragma unroll
-    for (int o = 16; o > 0; o >>= 1) {
-      const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
-      const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
-      const dfl s = df_two_sum(a.hi, oh);
-      a = df_fast(s.hi, s.lo + (a.lo + ol));
+  for (int r = 0; r < RS_ROWS; ++r)
+#pragma unroll
+    for (int q = 0; q < NR; ++q) {
+      dfl a = acc[r][q];
+#pragma unroll
+      for (int o = 16; o > 0; o >>= 1) {
+        const float oh = __shfl_xor_sync(0xffffffffu, a.hi, o);
+        const float ol = __shfl_xor_sync(0xffffffffu, a.lo, o);
+        const dfl s = df_two_sum(a.hi, oh);
+        a = df_fast(s.hi, s.lo + (a.lo + ol));
+      }
+      const int k = k0 + r;
+      if (lane == 0 && k < m) {
+        const float2 bb = c.w.eeq_B[(size_t)b * 2 * N + (size_t)q * N + k];
+        const dfl res = df_add(dfl{bb.x, bb.y}, df_neg(a));
+        c.w.eeq_V[(size_t)b * 2 * N + (size_t)q * N + k] = res.hi;
+        mx = fmaxf(mx, fabsf(res.hi));
+      }
     }
-    if (lane == 0) {
-      const float2 bb = c.w.eeq_B[(size_t)b * 2 * N + (size_t)r * N + k];
-      const dfl res = df_add(dfl{bb.x, bb.y}, df_neg(a));
-      c.w.eeq_V[(size_t)b * 2 * N + (size_t)r * N + k] = res.hi;
-      mx = fmaxf(mx, fabsf(res.hi));
-    }
-  }
   if (lane == 0) atomicMax(&c.w.eeq_res[b * EEQ_BIG_REFINE + it], __float_as_uint(mx));
 }
 
@@ -980,8 +1122,32 @@ static void launch_factor(const Ctx &c, cudaStream_t st) {
   cudaStreamWaitEvent(st, la->done, 0);
 }
 
+// Whether every structure's refinement residual of iteration ``it`` is below
+// the tolerance, read on the host (one small copy and a wait for the
+// stream).  A failed copy or wait answers no, and the device-side skips
+// decide as before.
+static bool converged_on_host(const Ctx &c, cudaStream_t st, int it) {
+  std::vector<unsigned> res((size_t)c.B * EEQ_BIG_REFINE);
+  if (cudaMemcpyAsync(res.data(), c.w.eeq_res, 4 * res.size(), cudaMemcpyDeviceToHost, st) !=
+          cudaSuccess ||
+      cudaStreamSynchronize(st) != cudaSuccess)
+    return false;
+  for (int b = 0; b < c.B; ++b) {
+    float r;
+    std::memcpy(&r, &res[(size_t)b * EEQ_BIG_REFINE + it], 4);
+    if (!(r < BIG_TOL)) return false;
+  }
+  return true;
+}
+
 // Forward (adjoint = 0: factorisation, two right-hand sides, charges) or
 // adjoint (reuses the factor; one right-hand side dE/dq) multi-CTA EEQ.
+// Refinement iterations after the second are launched only while some
+// structure still needs them: for large structures (eight 512-blocks or
+// more, where an iteration is ~130 launches) the host reads the residuals
+// after the second and each later iteration, unless the stream is being
+// captured into a graph; otherwise every iteration is launched and the
+// converged structures skip it on the device.
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int B = c.B, N = c.N;
   if (!adjoint) {
@@ -997,25 +1163,34 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
     ensure_smem(eeq_blkinv_step_kernel, (int)eeq_blkinv_smem());
     for (int r = 1; r < SBP; ++r)
       eeq_blkinv_step_kernel<<<dim3(nsb * r, B), 256, eeq_blkinv_smem(), st>>>(c, r);
+    eeq_blkinv_mirror_kernel<<<dim3(MIR_TILES, nsb, B), 256, 0, st>>>(c);
   }
   const int nr = adjoint ? 1 : 2;
+  cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
+  if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusActive;
+  const bool host_check = nsb >= 8 && cap == cudaStreamCaptureStatusNone;
   eeq_big_rhs_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, adjoint ? 1 : 0);
   for (int it = 0; it < EEQ_BIG_REFINE; ++it) {
+    if (host_check && it >= 2 && converged_on_host(c, st, it - 1)) break;
     // V = L^-T L^-1 V: forward sweep into Y, backward sweep into V
     for (int sb = 0; sb < nsb; ++sb) {
       eeq_sweep_diag_kernel<<<dim3(EEQ_SB / 8, B), 256, 0, st>>>(c, sb, it, 0, nr, 0);
       const int rest = N - (sb + 1) * EEQ_SB;
       if (rest > 0)
-        eeq_sweep_below_kernel<<<dim3((rest + 7) / 8, B), 256, 0, st>>>(c, sb, it, nr);
+        eeq_sweep_below_kernel<<<dim3((rest + 8 * BL_ROWS - 1) / (8 * BL_ROWS), B), 256, 0, st>>>(
+            c, sb, it, nr);
     }
     for (int sb = nsb - 1; sb >= 0; --sb) {
       eeq_sweep_diag_kernel<<<dim3(EEQ_SB / 8, B), 256, 0, st>>>(c, sb, it, 1, nr, 1);
       const int s0 = sb * EEQ_SB;
       if (s0 > 0)
-        eeq_sweep_above_kernel<<<dim3((s0 + AB_ROWS - 1) / AB_ROWS, B), 256, 0, st>>>(c, sb, it, nr);
+        eeq_sweep_above_kernel<<<dim3((s0 + AB_COLS - 1) / AB_COLS, B), 256, 0, st>>>(c, sb, it,
+                                                                                     nr);
     }
     eeq_big_update_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, it, nr);
-    eeq_big_residual_kernel<<<dim3((N + 7) / 8, B), 256, 0, st>>>(c, it, nr);
+    const dim3 rg((N + 8 * RS_ROWS - 1) / (8 * RS_ROWS), B);
+    if (nr == 2) eeq_big_residual_kernel<2><<<rg, 256, 0, st>>>(c, it);
+    else eeq_big_residual_kernel<1><<<rg, 256, 0, st>>>(c, it);
   }
   eeq_big_finish_kernel<<<B, 1024, 0, st>>>(c, adjoint ? 1 : 0);
 }

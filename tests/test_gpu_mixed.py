@@ -116,6 +116,29 @@ def test_charges_refined_to_fp64(d4):
         assert (q[k, :n] - q_ref).abs().max().item() < 1e-9
 
 
+def test_multi_cta_eeq_of_3700_atoms_refined_to_fp64(d4):
+    """3700 atoms (eight 512-row blocks: the refinement's later iterations
+    are launched only after the host has read the residuals): forward and
+    adjoint residuals below 1e-10, charges within 1e-9 of an FP64 solve of
+    the same EEQ system."""
+    from importlib import import_module
+    disp = import_module("tad-dftd4_gb300.disp")
+    wl = package().workloads
+    b = wl.large16k(5, 3700)
+    dev = torch.device("cuda")
+    nt, pt, ct = (torch.from_numpy(x).to(dev) for x in (b.numbers, b.positions, b.charge))
+    runner, _, _ = disp._prepare(nt, pt, ct, PARAM, "d4", None, None, None, None, None,
+                                 None, None, None, "mixed")
+    out = runner.run(pt, gradient=True, charges_out=True, cn_eeq_out=True)
+    q, cnq = out[3].cpu(), out[5].cpu()
+    res = runner.eeq_residuals()
+    assert (res < 1e-10).all() and (res > 0).all(), res
+    tables = oracle.load_tables()
+    q_ref = _eeq_fp64(torch.from_numpy(b.numbers[0]), torch.from_numpy(b.positions[0]),
+                      float(b.charge[0]), cnq[0], tables)
+    assert (q[0] - q_ref).abs().max().item() < 1e-9
+
+
 def test_large_structure_global_accumulation(d4):
     """n > 234 switches the ATM kernel to global accumulation."""
     wl = package().workloads
