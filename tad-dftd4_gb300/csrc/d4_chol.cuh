@@ -60,26 +60,28 @@ static __device__ void chol_diag_factor(float *L, int k0, int kb, int *bad) {
 
 // The inverse X of the factored diagonal block, which replaces it in place
 // (the panel and the triangular solves only need the inverse), by all warps
-// of the CTA (at least eight; every thread calls it): warp w forms the
+// of the CTA (Q x warps >= 32; every thread calls it): warp w forms the
 // columns w, w + nw, ... by forward substitution down the column, lane r =
 // row r, X[r][c] = (delta_rc - sum_{k<r} L[r][k] X[k][c]) / L[r][r]; the
 // columns of a warp advance together, the finished value of row k reaching
 // the other lanes by a shuffle.  (One warp forming all 32 columns took ~12k
-// cycles per block, three times the factorisation; eight warps take ~2.7k.)
+// cycles per block, three times the factorisation; eight warps take ~2.7k.
+// Sixteen warps take Q = 2: with four slots per warp, two of them empty,
+// the shuffles alone doubled the time.)
+template <int Q>
 static __device__ void chol_diag_inverse(float *L, int k0, int kb) {
-  constexpr int QMAX = 4;  // columns per warp for eight warps or more
   const int w = threadIdx.x >> 5, r = threadIdx.x & 31, nw = blockDim.x >> 5;
   const bool live = r < kb;
   const float *lr = L + tri_index(k0 + (live ? r : 0), k0);
   const float dinv = live ? 1.0f / lr[r] : 1.f;
-  float sq[QMAX], xr[QMAX];
+  float sq[Q], xr[Q];
 #pragma unroll
-  for (int q = 0; q < QMAX; ++q) sq[q] = xr[q] = 0.f;
+  for (int q = 0; q < Q; ++q) sq[q] = xr[q] = 0.f;
 #pragma unroll 1
   for (int k = 0; k < kb; ++k) {
-    float xk[QMAX];
+    float xk[Q];
 #pragma unroll
-    for (int q = 0; q < QMAX; ++q) {
+    for (int q = 0; q < Q; ++q) {
       const int cq = w + nw * q;
       const float mine = r == cq ? dinv : (r > cq ? -sq[q] * dinv : 0.f);
       if (r == k) xr[q] = mine;
@@ -87,14 +89,22 @@ static __device__ void chol_diag_inverse(float *L, int k0, int kb) {
     }
     const float lrk = (live && r > k) ? lr[k] : 0.f;
 #pragma unroll
-    for (int q = 0; q < QMAX; ++q) sq[q] = fmaf(lrk, xk[q], sq[q]);
+    for (int q = 0; q < Q; ++q) sq[q] = fmaf(lrk, xk[q], sq[q]);
   }
   __syncthreads();  // every warp has read the factor
 #pragma unroll
-  for (int q = 0; q < QMAX; ++q) {
+  for (int q = 0; q < Q; ++q) {
     const int cq = w + nw * q;
     if (cq < PB && live && r >= cq) L[tri_index(k0 + r, k0 + cq)] = xr[q];
   }
+}
+
+// chol_diag_inverse with the column slots per warp that the CTA's size needs
+static __device__ __forceinline__ void chol_diag_inverse_cta(float *L, int k0, int kb) {
+  if (blockDim.x >= 512)
+    chol_diag_inverse<2>(L, k0, kb);
+  else
+    chol_diag_inverse<4>(L, k0, kb);
 }
 
 // (ti, tj), tj <= ti, of the t-th tile of a packed lower triangle of tiles
@@ -105,14 +115,67 @@ static __device__ __forceinline__ void tri_tile(int t, int &ti, int &tj) {
   tj = t - ti * (ti + 1) / 2;
 }
 
+// A22 -= L21 L21^T for the rows / columns t0 .. m-1 of the packed matrix,
+// from the panel PT (transposed, 32 x ldp), in TS x TS register tiles of
+// the lower triangle (one tile per thread at a time, read as float4).
+template <int TS>
+static __device__ __forceinline__ void chol_update_tiles(float *L, const float *PT, int ldp,
+                                                         int m, int t0, int kb) {
+  const int nrem = m - t0;
+  const int T = (nrem + TS - 1) / TS;
+  const int ntile = T * (T + 1) / 2;
+  for (int t = threadIdx.x; t < ntile; t += blockDim.x) {
+    int ti, tj;
+    tri_tile(t, ti, tj);
+    const int i0 = TS * ti, j0 = TS * tj;  // relative to t0
+    float acc[TS][TS];
+#pragma unroll
+    for (int q = 0; q < TS; ++q)
+#pragma unroll
+      for (int u = 0; u < TS; ++u) acc[q][u] = 0.f;
+    for (int cc = 0; cc < kb; ++cc) {
+      const float4 *p = reinterpret_cast<const float4 *>(PT + cc * ldp);
+      float x[TS], y[TS];
+#pragma unroll
+      for (int h = 0; h < TS / 4; ++h) {
+        const float4 xa = p[(i0 >> 2) + h], ya = p[(j0 >> 2) + h];
+        x[4 * h] = xa.x;
+        x[4 * h + 1] = xa.y;
+        x[4 * h + 2] = xa.z;
+        x[4 * h + 3] = xa.w;
+        y[4 * h] = ya.x;
+        y[4 * h + 1] = ya.y;
+        y[4 * h + 2] = ya.z;
+        y[4 * h + 3] = ya.w;
+      }
+#pragma unroll
+      for (int q = 0; q < TS; ++q)
+#pragma unroll
+        for (int u = 0; u < TS; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
+    }
+#pragma unroll
+    for (int q = 0; q < TS; ++q) {
+      const int i = t0 + i0 + q;
+      if (i < m) {
+        float *ri = L + tri_index(i, 0);
+#pragma unroll
+        for (int u = 0; u < TS; ++u) {
+          const int j = t0 + j0 + u;
+          if (j <= i) ri[j] -= acc[q][u];
+        }
+      }
+    }
+  }
+}
+
 // Blocked right-looking Cholesky (panels of 32 columns) of the packed lower
 // m x m FP32 matrix L, in place, except that each diagonal block holds the
 // inverse of its factor.  Per panel: the diagonal block (factor by warp 0,
 // inverse by all warps), the panel L21 = A21 X^T (X the block inverse; one
 // warp per row, lane = column), and the trailing update A22 -= L21 L21^T.
 // The panel buffer PT (shared memory, 32 x ldp) holds the panel transposed,
-// so that the update runs on 8 x 8 register tiles read as float4 (64 FMAs
-// per four 16-byte loads).
+// so that the update runs on register tiles read as float4 (8 x 8: 64 FMAs
+// per four 16-byte loads; 4 x 4 once the trailing matrix is small).
 static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *bad) {
   const int tid = threadIdx.x, nt = blockDim.x, warp = tid >> 5, lane = tid & 31;
   const int nw = nt >> 5;
@@ -120,7 +183,7 @@ static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *ba
     const int kb = min(PB, m - k0);
     if (warp == 0) chol_diag_factor(L, k0, kb, bad);
     __syncthreads();
-    chol_diag_inverse(L, k0, kb);
+    chol_diag_inverse_cta(L, k0, kb);
     __syncthreads();
     const int t0 = k0 + kb;
     // panel: row i of L21 solves L11 x = A21[i]^T, i.e. x = X A21[i]^T; the
@@ -152,44 +215,14 @@ static __device__ void chol_blocked(float *L, float *PT, int ldp, int m, int *ba
       }
     }
     __syncthreads();
+    // trailing update: 8 x 8 register tiles while they keep at least half of
+    // the threads busy, else 4 x 4 (four times as many tiles)
     const int nrem = m - t0;
-    {
-      const int T8 = (nrem + 7) >> 3;
-      const int ntile = T8 * (T8 + 1) / 2;
-      for (int t = tid; t < ntile; t += nt) {
-        int ti, tj;
-        tri_tile(t, ti, tj);
-        const int i0 = 8 * ti, j0 = 8 * tj;  // relative to t0
-        float acc[8][8];
-#pragma unroll
-        for (int q = 0; q < 8; ++q)
-#pragma unroll
-          for (int u = 0; u < 8; ++u) acc[q][u] = 0.f;
-        for (int cc = 0; cc < kb; ++cc) {
-          const float4 *p = reinterpret_cast<const float4 *>(PT + cc * ldp);
-          const float4 xa = p[i0 >> 2], xb = p[(i0 >> 2) + 1];
-          const float4 ya = p[j0 >> 2], yb = p[(j0 >> 2) + 1];
-          const float x[8] = {xa.x, xa.y, xa.z, xa.w, xb.x, xb.y, xb.z, xb.w};
-          const float y[8] = {ya.x, ya.y, ya.z, ya.w, yb.x, yb.y, yb.z, yb.w};
-#pragma unroll
-          for (int q = 0; q < 8; ++q)
-#pragma unroll
-            for (int u = 0; u < 8; ++u) acc[q][u] = fmaf(x[q], y[u], acc[q][u]);
-        }
-#pragma unroll
-        for (int q = 0; q < 8; ++q) {
-          const int i = t0 + i0 + q;
-          if (i < m) {
-            float *ri = L + tri_index(i, 0);
-#pragma unroll
-            for (int u = 0; u < 8; ++u) {
-              const int j = t0 + j0 + u;
-              if (j <= i) ri[j] -= acc[q][u];
-            }
-          }
-        }
-      }
-    }
+    const int T8 = (nrem + 7) >> 3;
+    if (2 * (T8 * (T8 + 1) / 2) >= nt)
+      chol_update_tiles<8>(L, PT, ldp, m, t0, kb);
+    else
+      chol_update_tiles<4>(L, PT, ldp, m, t0, kb);
     __syncthreads();
   }
 }

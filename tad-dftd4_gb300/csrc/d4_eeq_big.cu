@@ -256,7 +256,9 @@ __global__ void __launch_bounds__(256, 1) eeq_big_panel_kernel(Ctx c, int k0, in
     }
   }
   __syncthreads();
-  const int ty = tid >> 3, tx = tid & 7;  // rows 2 ty, 2 ty + 1; columns 4 tx .. + 3 of a block
+  // rows 2 ty, 2 ty + 1; columns 4 tx .. + 3 of a block: warp w owns rows
+  // 8 w .. 8 w + 7 from here on, so that only its own lanes synchronise
+  const int ty = tid >> 3, tx = tid & 7;
   const int nb32 = (kb + 31) >> 5;
   for (int cb = 0; cb < nb32; ++cb) {
     const int c0 = 32 * cb + 4 * tx;
@@ -284,7 +286,7 @@ __global__ void __launch_bounds__(256, 1) eeq_big_panel_kernel(Ctx c, int k0, in
       z[0] -= acc[0][u];
       z[1] -= acc[1][u];
     }
-    __syncthreads();
+    __syncwarp();
     // Y_c = Z_c D_c^-T: Y[r][c] = sum_q Z[r][q] D^-1[c][q] (LT is 0 above)
     float y[2][4];
 #pragma unroll
@@ -302,21 +304,21 @@ __global__ void __launch_bounds__(256, 1) eeq_big_panel_kernel(Ctx c, int k0, in
         y[1][u] = fmaf(zr.y, lv[u], y[1][u]);
       }
     }
-    __syncthreads();  // every thread has read Z_c
+    __syncwarp();  // every lane has read Z_c
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
       float *z = AT + (c0 + u) * PN_LAT + 2 * ty;
       z[0] = y[0][u];
       z[1] = y[1][u];
     }
-    __syncthreads();
+    __syncwarp();
   }
-  // L21 rows to F (warp per row, lanes over 4-column groups) and, split, to
-  // the operands of the trailing update (only full panels have one)
+  // L21 rows to F (the warp's own rows, lanes over 4-column groups) and,
+  // split, to the operands of the trailing update (only full panels have one)
   const bool split = kb == BNB;
   const int warp = tid >> 5, lane = tid & 31;
   const int col = 4 * lane;
-  for (int rr = warp; rr < 64; rr += 8) {
+  for (int rr = 8 * warp; rr < 8 * warp + 8; ++rr) {
     const int i = r0 + rr;
     if (i >= m || col >= kb) continue;
     float v[4];
@@ -863,13 +865,14 @@ __global__ void eeq_big_update_kernel(Ctx c, int it, int nr) {
 }
 
 // r = b - (hi + lo) x in double-float; v <- FP32 r and the structure's max
-// |r| of this iteration.  Four rows per warp, so that every x entry read
-// serves four rows; lanes over columns (32 apart, coalesced), the 32 matrix
-// loads of a lane's step issued together, one step ahead of the sums.  Per
-// row the sum runs in the same order as with one row per warp.
-constexpr int RS_ROWS = 4;
-template <int NR>
-__global__ void __launch_bounds__(256, 2) eeq_big_residual_kernel(Ctx c, int it) {
+// |r| of this iteration.  RS_ROWS rows per warp (every x entry read serves
+// them all), lanes over columns, the loads of the next 128 columns in
+// flight while the current ones are summed.  VEC (rows 16-byte aligned: N a
+// multiple of four): lane l takes columns 4 l .. 4 l + 3 of each 128 as one
+// float4 per row and plane; else columns l, l + 32, l + 64, l + 96.
+constexpr int RS_ROWS = 2;
+template <int NR, bool VEC>
+__global__ void __launch_bounds__(256, 3) eeq_big_residual_kernel(Ctx c, int it) {
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   if (big_skip(c, b, it)) return;
@@ -885,24 +888,36 @@ __global__ void __launch_bounds__(256, 2) eeq_big_residual_kernel(Ctx c, int it)
   for (int r = 0; r < RS_ROWS; ++r)
 #pragma unroll
     for (int q = 0; q < NR; ++q) acc[r][q] = {0.f, 0.f};
-  // two stages of loads: those of the next 128 columns are in flight while
-  // the current ones are summed
-  float h[2][RS_ROWS][4], lo[2][RS_ROWS][4];
+  // column of element u (0..3) of the lane in the 128-column step at l0
+  auto col = [&](int l0, int u) { return VEC ? l0 + 4 * lane + u : l0 + lane + 32 * u; };
   auto load = [&](float (&hh)[RS_ROWS][4], float (&ll)[RS_ROWS][4], int l0) {
 #pragma unroll
-    for (int r = 0; r < RS_ROWS; ++r)
+    for (int r = 0; r < RS_ROWS; ++r) {
+      const bool rok = k0 + r < m;
+      if (VEC) {
+        const int l = col(l0, 0);
+        const bool ok = rok && l < m;
+        const float4 h4 = ok ? *reinterpret_cast<const float4 *>(hr + (size_t)r * N + l)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        const float4 l4 = ok ? *reinterpret_cast<const float4 *>(lr + (size_t)r * N + l)
+                             : make_float4(0.f, 0.f, 0.f, 0.f);
+        hh[r][0] = h4.x, hh[r][1] = h4.y, hh[r][2] = h4.z, hh[r][3] = h4.w;
+        ll[r][0] = l4.x, ll[r][1] = l4.y, ll[r][2] = l4.z, ll[r][3] = l4.w;
+      } else {
 #pragma unroll
-      for (int u = 0; u < 4; ++u) {
-        const int l = l0 + 32 * u;
-        const bool ok = l < m && k0 + r < m;
-        hh[r][u] = ok ? hr[(size_t)r * N + l] : 0.f;
-        ll[r][u] = ok ? lr[(size_t)r * N + l] : 0.f;
+        for (int u = 0; u < 4; ++u) {
+          const int l = col(l0, u);
+          const bool ok = rok && l < m;
+          hh[r][u] = ok ? hr[(size_t)r * N + l] : 0.f;
+          ll[r][u] = ok ? lr[(size_t)r * N + l] : 0.f;
+        }
       }
+    }
   };
   auto sum = [&](const float (&hh)[RS_ROWS][4], const float (&ll)[RS_ROWS][4], int l0) {
 #pragma unroll
     for (int u = 0; u < 4; ++u) {
-      const int l = l0 + 32 * u;
+      const int l = col(l0, u);
       if (l < m) {
 #pragma unroll
         for (int q = 0; q < NR; ++q) {
@@ -918,8 +933,9 @@ __global__ void __launch_bounds__(256, 2) eeq_big_residual_kernel(Ctx c, int it)
       }
     }
   };
-  load(h[0], lo[0], lane);
-  for (int l0 = lane; l0 < m; l0 += 256) {
+  float h[2][RS_ROWS][4], lo[2][RS_ROWS][4];
+  load(h[0], lo[0], 0);
+  for (int l0 = 0; l0 < m; l0 += 256) {
     load(h[1], lo[1], l0 + 128);
     sum(h[0], lo[0], l0);
     load(h[0], lo[0], l0 + 256);
@@ -1189,8 +1205,13 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
     }
     eeq_big_update_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, it, nr);
     const dim3 rg((N + 8 * RS_ROWS - 1) / (8 * RS_ROWS), B);
-    if (nr == 2) eeq_big_residual_kernel<2><<<rg, 256, 0, st>>>(c, it);
-    else eeq_big_residual_kernel<1><<<rg, 256, 0, st>>>(c, it);
+    if (N % 4 == 0) {
+      if (nr == 2) eeq_big_residual_kernel<2, true><<<rg, 256, 0, st>>>(c, it);
+      else eeq_big_residual_kernel<1, true><<<rg, 256, 0, st>>>(c, it);
+    } else {
+      if (nr == 2) eeq_big_residual_kernel<2, false><<<rg, 256, 0, st>>>(c, it);
+      else eeq_big_residual_kernel<1, false><<<rg, 256, 0, st>>>(c, it);
+    }
   }
   eeq_big_finish_kernel<<<B, 1024, 0, st>>>(c, adjoint ? 1 : 0);
 }
