@@ -1166,11 +1166,7 @@ static bool converged_on_host(const Ctx &c, cudaStream_t st, int it) {
 // converged structures skip it on the device.
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int B = c.B, N = c.N;
-  if (!adjoint) {
-    cudaMemcpy2DAsync(c.w.eeq_F, (size_t)4 * eeq_ldf(N), c.w.eeq_hi, (size_t)4 * N,
-                      (size_t)4 * N, (size_t)B * N, cudaMemcpyDeviceToDevice, st);
-    launch_factor(c, st);
-  }
+  if (!adjoint) launch_factor(c, st);  // F: the lower part of hi, from the build kernel
   const int nsb = eeq_nsb(N);
   if (!adjoint) {  // inverses of the 128- and 512-blocks, kept for the adjoint solve
     ensure_smem(eeq_big_pinv_kernel, (int)eeq_big_pinv_smem());

@@ -1883,13 +1883,16 @@ __global__ void __launch_bounds__(256) pair_cn_bwd_mixed_kernel(Ctx c) {
 // 1/g and the diagonal from per-element tables; no FP64 instruction.
 // Persistent blocks loop over the 32 x 32 tiles of the lower triangles of
 // all structures; a tile and its mirror are both stored coalesced (the
-// mirror through shared memory).
+// mirror through shared memory).  The lower tiles' hi part also goes to the
+// multi-CTA factorisation's matrix F (row stride eeq_ldf(N)), which reads
+// nothing above the diagonal.
 __global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
   __shared__ float4 s_erf[ERF_TAB];
   __shared__ float s_hi[32][33], s_lo[32][33];
   for (int k = threadIdx.x; k < ERF_TAB; k += blockDim.x) s_erf[k] = c.w.erf_tab[k];
   __syncthreads();
   const int N = c.N;
+  const int NF = eeq_ldf(N);
   const int T = (N + 31) / 32;
   const int tp = T * (T + 1) / 2;
   const size_t total = (size_t)c.B * tp;
@@ -1906,6 +1909,7 @@ __global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
     const size_t bN = (size_t)b * N;
     float *Hi = c.w.eeq_hi + bN * N;
     float *Lo = c.w.eeq_lo + bN * N;
+    float *F = c.w.eeq_F + bN * NF;
     const int l = tj * 32 + tx;
     int zl = 0;
     float4 pl = make_float4(0.f, 0.f, 0.f, 0.f), pll = pl;
@@ -1939,6 +1943,7 @@ __global__ void __launch_bounds__(256) eeq_build_df_kernel(Ctx c) {
         }
         Hi[(size_t)k * N + l] = v.hi;
         Lo[(size_t)k * N + l] = v.lo;
+        F[(size_t)k * NF + l] = v.hi;  // the factorisation's input (lower part)
       }
       s_hi[rr][tx] = v.hi;
       s_lo[rr][tx] = v.lo;
