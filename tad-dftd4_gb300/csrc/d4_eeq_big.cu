@@ -965,12 +965,18 @@ __global__ void __launch_bounds__(256, 3) eeq_big_residual_kernel(Ctx c, int it)
   if (lane == 0) atomicMax(&c.w.eeq_res[b * EEQ_BIG_REFINE + it], __float_as_uint(mx));
 }
 
-// Charges (forward) or the adjoint charges (adjoint) from the solutions,
-// one CTA per structure; FP64 sums.
+// Charges (forward) or the adjoint charges (adjoint) from the solutions;
+// FP64 sums.  Grid (FIN_CTAS, structures): every CTA forms the structure's
+// sums itself (same order, same values), CTA 0 records them, and each CTA
+// writes its share of the atoms (real atoms by their compact index,
+// padding slots zeroed -- disjoint sets, so the CTAs never write the same
+// entry).
+constexpr int FIN_CTAS = 16;
 __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint) {
   __shared__ double s_a[32], s_b[32];
   __shared__ double s_par;
-  const int b = blockIdx.x;
+  const int b = blockIdx.y;
+  const bool lead = blockIdx.x == 0;
   const int N = c.N;
   const int m = c.w.n_real[b];
   const float2 *X = c.w.eeq_X + (size_t)b * 2 * N;
@@ -995,7 +1001,7 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
       fin = __uint_as_float(c.w.eeq_res[b * EEQ_BIG_REFINE + it]);
       if (fin < BIG_TOL) break;
     }
-    c.w.eeq_final[2 * b + (adjoint ? 1 : 0)] = fin;
+    if (lead) c.w.eeq_final[2 * b + (adjoint ? 1 : 0)] = fin;
     double ta = 0.0, tb = 0.0;
     for (int w = 0; w < (int)(blockDim.x >> 5); ++w) {
       ta += s_a[w];
@@ -1005,14 +1011,18 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
       s_par = m > 0 ? ta / c.w.eeq_sum[2 * b] : 0.0;
     } else {
       const double lam = m > 0 ? (ta - c.charge[b]) / tb : 0.0;
-      c.w.eeq_sum[2 * b] = tb;
-      c.w.eeq_sum[2 * b + 1] = lam;
+      if (lead) {
+        c.w.eeq_sum[2 * b] = tb;
+        c.w.eeq_sum[2 * b + 1] = lam;
+      }
       s_par = lam;
     }
   }
   __syncthreads();
   const double par = s_par;
-  for (int i = tid; i < N; i += blockDim.x) {
+  const int g0 = blockIdx.x * blockDim.x + tid, gs = gridDim.x * blockDim.x;
+  for (int i = g0; i < N; i += gs) {
+    if (c.w.cidx[(size_t)b * N + i] >= 0) continue;  // a real atom: written below
     if (adjoint) {
       c.w.eeq_w[(size_t)b * N + i] = 0.0;
       c.w.dEdcnq[(size_t)b * N + i] = 0.0;
@@ -1021,8 +1031,7 @@ __global__ void __launch_bounds__(1024) eeq_big_finish_kernel(Ctx c, int adjoint
       c.w.eeq_y[(size_t)b * N + i] = 0.0;
     }
   }
-  __syncthreads();
-  for (int k = tid; k < m; k += blockDim.x) {
+  for (int k = g0; k < m; k += gs) {
     const size_t a = (size_t)b * N + c.w.ridx[(size_t)b * N + k];
     const double x0 = (double)X[k].x + (double)X[k].y;
     if (adjoint) {
@@ -1209,7 +1218,7 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
       else eeq_big_residual_kernel<1, false><<<rg, 256, 0, st>>>(c, it);
     }
   }
-  eeq_big_finish_kernel<<<B, 1024, 0, st>>>(c, adjoint ? 1 : 0);
+  eeq_big_finish_kernel<<<dim3(FIN_CTAS, B), 1024, 0, st>>>(c, adjoint ? 1 : 0);
 }
 
 }  // namespace d4
