@@ -18,8 +18,12 @@
  * size comes from ``d4_workspace_size``.  All pointers named ``d_*`` or
  * documented as "device" are device pointers.  ``stream`` is a
  * ``cudaStream_t`` passed as ``void*``; work is enqueued on it and every
- * call returns without synchronising.  Calls on different streams with
- * different workspaces are independent.
+ * call returns without synchronising, with one exception: for structures
+ * padded beyond 3584 atoms the precision form's EEQ solves wait once each
+ * for ``stream`` (after their second refinement iteration, to launch a
+ * third only if a residual asks for it), unless the stream is being
+ * captured or the call sets D4_FLAG_NO_HOST_WAIT.  Calls on different
+ * streams with different workspaces are independent.
  *
  * Errors: every entry point returns a ``d4_status`` code.  Input problems
  * that can only be seen on the device (atomic number outside the tables,
@@ -70,6 +74,11 @@ typedef enum d4_model_kind { D4_MODEL_D4 = 0, D4_MODEL_D4S = 1 } d4_model_kind;
                                   (D4ATMExact, dispersion/threebody.py:276-302,
                                   dispersion/d4.py:67-84) instead of
                                   sqrt(C6 C6 C6); plain FP64 method only */
+#define D4_FLAG_NO_HOST_WAIT 32u /* never wait for the stream inside the call:
+                                    the multi-CTA EEQ launches all its
+                                    refinement iterations and converged
+                                    structures skip them on the device (no
+                                    reference counterpart) */
 
 /* Test hook of the timeout handling: the tensor-core pair kernel of the
    precision form treats the first wait for its MMAs as timed out and takes

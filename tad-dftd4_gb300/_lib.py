@@ -39,6 +39,7 @@ FLAG_CHARGES_IN = 2
 FLAG_MIXED = 4
 FLAG_PARAM_GRAD = 8
 FLAG_EXACT_C9 = 16
+FLAG_NO_HOST_WAIT = 32  # the multi-CTA EEQ never waits for the stream inside a call
 FLAG_TEST_TIMEOUT = 0x80000000  # test hook: the pair kernel's first MMA wait counts as timed out
 PARAM_GRAD_STRIDE = 12  # D4_PARAM_GRAD_STRIDE: s6 s8 s10 a1 a2 s9 alp rs6 rs8 bet - -
 

@@ -1171,8 +1171,9 @@ static bool converged_on_host(const Ctx &c, cudaStream_t st, int it) {
 // structure still needs them: for large structures (eight 512-blocks or
 // more, where an iteration is ~130 launches) the host reads the residuals
 // after the second and each later iteration, unless the stream is being
-// captured into a graph; otherwise every iteration is launched and the
-// converged structures skip it on the device.
+// captured into a graph or the call sets D4_FLAG_NO_HOST_WAIT; otherwise
+// every iteration is launched and the converged structures skip it on the
+// device.
 void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int B = c.B, N = c.N;
   if (!adjoint) launch_factor(c, st);  // F: the lower part of hi, from the build kernel
@@ -1189,7 +1190,8 @@ void launch_eeq_big(const Ctx &c, cudaStream_t st, bool adjoint) {
   const int nr = adjoint ? 1 : 2;
   cudaStreamCaptureStatus cap = cudaStreamCaptureStatusNone;
   if (cudaStreamIsCapturing(st, &cap) != cudaSuccess) cap = cudaStreamCaptureStatusActive;
-  const bool host_check = nsb >= 8 && cap == cudaStreamCaptureStatusNone;
+  const bool host_check =
+      nsb >= 8 && cap == cudaStreamCaptureStatusNone && !(c.flags & D4_FLAG_NO_HOST_WAIT);
   eeq_big_rhs_kernel<<<dim3((N + 255) / 256, B), 256, 0, st>>>(c, adjoint ? 1 : 0);
   for (int it = 0; it < EEQ_BIG_REFINE; ++it) {
     if (host_check && it >= 2 && converged_on_host(c, st, it - 1)) break;

@@ -32,6 +32,16 @@ def test_library_exports_every_declared_function():
     assert set(names) == set(package()._lib.SIGNATURES)
 
 
+def test_call_flags_match_the_header():
+    """Every D4_FLAG_* of the header has its twin in the ctypes module."""
+    text = HEADER.read_text()
+    flags = dict(re.findall(r"#define D4_FLAG_([A-Z0-9_]+)\s+(0x[0-9a-fA-F]+|\d+)u", text))
+    assert {"GRADIENT", "MIXED", "NO_HOST_WAIT"} <= set(flags)
+    lib = package()._lib
+    for name, value in flags.items():
+        assert getattr(lib, "FLAG_" + name) == int(value, 0), name
+
+
 def test_abi_version_and_status_strings():
     lib = package()._lib.load()
     assert lib.d4_abi_version() == 2
