@@ -731,12 +731,13 @@ __global__ void __launch_bounds__(256, 1) eeq_sweep_diag_kernel(Ctx c, int sblk,
 }
 
 // Forward sweep update below block s: V_i -= F[i][blk] . Y_blk.  Four rows
-// per warp, lanes over the block's columns: a lane's 64 matrix loads and
-// the old V entries of its rows are issued together (one round trip), Y_blk
-// is staged in shared memory once per CTA.
+// per warp, lane l over the block's columns 4 l + 128 t (16-byte loads: the
+// rows of F and the block start are 16-byte aligned): a lane's sixteen
+// matrix loads and the old V entries of its rows are issued together (one
+// round trip), Y_blk is staged in shared memory once per CTA.
 constexpr int BL_ROWS = 4;
 __global__ void __launch_bounds__(256, 2) eeq_sweep_below_kernel(Ctx c, int sblk, int it, int nr) {
-  __shared__ float s_y[2][EEQ_SB];
+  __shared__ __align__(16) float s_y[2][EEQ_SB];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   const int s0 = sblk * EEQ_SB;
@@ -756,13 +757,22 @@ __global__ void __launch_bounds__(256, 2) eeq_sweep_below_kernel(Ctx c, int sblk
   const int NF = eeq_ldf(N);
   const float *base = c.w.eeq_F + (size_t)b * N * NF + (size_t)i0 * NF + s0;
   float *V = c.w.eeq_V + (size_t)b * 2 * N;
-  float x[BL_ROWS][EEQ_SB / 32];
+  constexpr int NT = EEQ_SB / 128;  // float4 steps per row
+  float4 x[BL_ROWS][NT];
 #pragma unroll
   for (int r = 0; r < BL_ROWS; ++r)
 #pragma unroll
-    for (int t = 0; t < EEQ_SB / 32; ++t) {
-      const int k = lane + 32 * t;
-      x[r][t] = (i0 + r < m && k < kb) ? base[(size_t)r * NF + k] : 0.f;
+    for (int t = 0; t < NT; ++t) {
+      const int k = 4 * lane + 128 * t;  // k < kb keeps k + 3 inside the row's NF columns
+      float4 v = (i0 + r < m && k < kb)
+                     ? *reinterpret_cast<const float4 *>(base + (size_t)r * NF + k)
+                     : make_float4(0.f, 0.f, 0.f, 0.f);
+      if (k + 3 >= kb) {  // columns from kb on hold no data of this call
+        if (k + 1 >= kb) v.y = 0.f;
+        if (k + 2 >= kb) v.z = 0.f;
+        v.w = 0.f;
+      }
+      x[r][t] = v;
     }
   const bool own = lane < BL_ROWS && i0 + lane < m;  // lane r writes row i0 + r
   const float v0 = own ? V[i0 + lane] : 0.f;
@@ -772,10 +782,12 @@ __global__ void __launch_bounds__(256, 2) eeq_sweep_below_kernel(Ctx c, int sblk
   for (int r = 0; r < BL_ROWS; ++r) {
     float a0 = 0.f, a1 = 0.f;
 #pragma unroll
-    for (int t = 0; t < EEQ_SB / 32; ++t) {
-      const int k = lane + 32 * t;
-      a0 = fmaf(x[r][t], s_y[0][k], a0);
-      a1 = fmaf(x[r][t], s_y[1][k], a1);
+    for (int t = 0; t < NT; ++t) {
+      const int k = 4 * lane + 128 * t;  // s_y is 0 from kb on
+      const float4 y0 = *reinterpret_cast<const float4 *>(&s_y[0][k]);
+      const float4 y1 = *reinterpret_cast<const float4 *>(&s_y[1][k]);
+      a0 = fmaf(x[r][t].x, y0.x, fmaf(x[r][t].y, y0.y, fmaf(x[r][t].z, y0.z, fmaf(x[r][t].w, y0.w, a0))));
+      a1 = fmaf(x[r][t].x, y1.x, fmaf(x[r][t].y, y1.y, fmaf(x[r][t].z, y1.z, fmaf(x[r][t].w, y1.w, a1))));
     }
     a0 = warp_sumf(a0);
     if (nr == 2) a1 = warp_sumf(a1);
@@ -791,13 +803,14 @@ __global__ void __launch_bounds__(256, 2) eeq_sweep_below_kernel(Ctx c, int sblk
 }
 
 // Backward sweep update above block s: Y_i -= sum_k F[s0 + k][i] V_{s0+k}
-// for i < s0.  A CTA takes 32 columns i (the lanes: reads coalesced over i)
-// and splits the block's rows k over its eight warps (64 each, sixteen
-// loads in flight per lane); the warps' partial sums meet in shared memory.
-constexpr int AB_COLS = 32;
-__global__ void __launch_bounds__(256, 1) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
+// for i < s0.  A CTA takes 64 columns i (lane l: i and i + 1 from 2 l, one
+// 8-byte load per row, coalesced over i) and splits the block's rows k over
+// its eight warps (64 each, sixteen loads in flight per lane); the warps'
+// partial sums meet in shared memory.
+constexpr int AB_COLS = 64;
+__global__ void __launch_bounds__(256, 2) eeq_sweep_above_kernel(Ctx c, int sblk, int it, int nr) {
   __shared__ float s_v[2][EEQ_SB];
-  __shared__ float s_part[2][8][AB_COLS];
+  __shared__ float2 s_part[2][8][AB_COLS / 2];
   const int b = blockIdx.y;
   const int m = c.w.n_real[b];
   const int s0 = sblk * EEQ_SB;
@@ -812,25 +825,28 @@ __global__ void __launch_bounds__(256, 1) eeq_sweep_above_kernel(Ctx c, int sblk
   }
   __syncthreads();
   const int lane = threadIdx.x & 31, w = threadIdx.x >> 5;
-  const int i = blockIdx.x * AB_COLS + lane;
-  float a0 = 0.f, a1 = 0.f;
+  const int i = blockIdx.x * AB_COLS + 2 * lane;  // i + 1 < s0 with i (s0 is even)
+  float2 a0 = make_float2(0.f, 0.f), a1 = make_float2(0.f, 0.f);
   if (i < s0) {
     const int NF = eeq_ldf(N);
     const float *col = c.w.eeq_F + (size_t)b * N * NF + (size_t)s0 * NF + i;
     const int kbeg = (EEQ_SB / 8) * w;
 #pragma unroll
     for (int h = 0; h < EEQ_SB / 8; h += 16) {
-      float x[16];
+      float2 x[16];
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const int k = kbeg + h + t;
-        x[t] = k < kb ? col[(size_t)k * NF] : 0.f;
+        x[t] = k < kb ? *reinterpret_cast<const float2 *>(col + (size_t)k * NF)
+                      : make_float2(0.f, 0.f);
       }
 #pragma unroll
       for (int t = 0; t < 16; ++t) {
         const int k = kbeg + h + t;
-        a0 = fmaf(x[t], s_v[0][k], a0);
-        a1 = fmaf(x[t], s_v[1][k], a1);
+        a0.x = fmaf(x[t].x, s_v[0][k], a0.x);
+        a0.y = fmaf(x[t].y, s_v[0][k], a0.y);
+        a1.x = fmaf(x[t].x, s_v[1][k], a1.x);
+        a1.y = fmaf(x[t].y, s_v[1][k], a1.y);
       }
     }
   }
@@ -838,14 +854,20 @@ __global__ void __launch_bounds__(256, 1) eeq_sweep_above_kernel(Ctx c, int sblk
   s_part[1][w][lane] = a1;
   __syncthreads();
   if (w == 0 && i < s0) {
-    float t0 = 0.f, t1 = 0.f;
+    float2 t0 = make_float2(0.f, 0.f), t1 = make_float2(0.f, 0.f);
 #pragma unroll
     for (int q = 0; q < 8; ++q) {
-      t0 += s_part[0][q][lane];
-      t1 += s_part[1][q][lane];
+      t0.x += s_part[0][q][lane].x;
+      t0.y += s_part[0][q][lane].y;
+      t1.x += s_part[1][q][lane].x;
+      t1.y += s_part[1][q][lane].y;
     }
-    Y[i] -= t0;
-    if (nr == 2) Y[N + i] -= t1;
+    Y[i] -= t0.x;
+    Y[i + 1] -= t0.y;
+    if (nr == 2) {
+      Y[N + i] -= t1.x;
+      Y[N + i + 1] -= t1.y;
+    }
   }
 }
 
